@@ -1,0 +1,493 @@
+#!/usr/bin/env python
+"""Benchmark of the UMI operator hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Default workload `int_pair_1080p` (the integer-pair configuration): one step =
+the integral image of a 1920x1080 uint8 frame (umi_iimg_u8_i32) plus
+full-search motion estimation of a 1920x1080 uint8 pair, 16x16 blocks, +-32,
+fused argmin (umi_full_me_u8).  Metric: full_me Mblocks/s (8040 blocks per
+step).  Other workloads: `filter3x3_1024` (1024x1024 float32, 3x3 N(0,1)
+weights, zero pad; metric GB/s).
+
+Prints ONE JSON line (rank 0).  `value` is timed with CUDA events around
+exactly K steps on inputs already in HBM, rotating through enough input
+copies that the working set of consecutive steps exceeds L2; `e2e` repeats
+the K steps from pinned host buffers with the host->device copies and the
+device->host read of every result inside the timed region.  `--impl
+reference` times the reference's CPU loops (restated in the oracle) on the
+host cores instead.  With N > 1 (torchrun) every rank runs its own replica
+(the operator has no exchange step) and the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 2 ** 20
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
+# from the ncu capture summarised under profiles/ (None until captured).
+NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024"], default="int_pair_1080p")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    return dict(PEAKS_FALLBACK, source="fallback")
+
+
+# --------------------------------------------------------------------- dist
+class Dist:
+    def __init__(self, backend: str):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def done(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.path = None
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(device_index).uuid)
+            sel = uuid if uuid.startswith("GPU-") else f"GPU-{uuid}"
+        except Exception:
+            sel = str(device_index)
+        self.sel = sel
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.sel, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(self.NAMES, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# --------------------------------------------------------------------- workloads
+class IntPair:
+    """iimg of a 1920x1080 u8 frame + full_me (16x16, +-32, argmin) of a 1080p pair."""
+    name = "int_pair_1080p"
+    H, W, B, R = 1080, 1920, 16, 32
+    metric = "full_me Mblocks/s"
+    unit = "Mblocks/s"
+    dtype = "u8"
+
+    def __init__(self, seed=3):
+        from umi_gb300 import workloads
+        self.cur, self.ref, self.true_mv = workloads.me_pair(seed=seed, h=self.H, w=self.W, block=self.B)
+        self.nblk = (self.H // self.B) * (self.W // self.B)
+
+    def config(self):
+        return {"workload": self.name, "frame": f"{self.W}x{self.H} u8", "block": self.B, "search": f"+-{self.R}",
+                "argmin": "fused, first in raster order", "step": "iimg(cur) + full_me(cur, ref)",
+                "l2": "rotating input copies, consecutive steps touch > L2"}
+
+    def units_per_step(self):
+        return self.nblk / 1e6
+
+    # device side
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        self.U = U
+        per = 3 * self.H * self.W + 4 * self.H * self.W
+        self.n_rot = max(2, -(-2 * L2_BYTES // per))
+        c = torch.from_numpy(self.cur).to(dev)
+        r = torch.from_numpy(self.ref).to(dev)
+        self.d_cur = [c.clone() for _ in range(self.n_rot)]
+        self.d_ref = [r.clone() for _ in range(self.n_rot)]
+        self.d_ii = [torch.empty((self.H, self.W), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
+        self.d_mv = [torch.empty((self.nblk, 3), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
+        self.ws = torch.empty(U.iimg_workspace_bytes(self.H, self.W), dtype=torch.uint8, device=dev)
+        # pinned host buffers for e2e
+        self.h_cur = torch.from_numpy(self.cur).pin_memory()
+        self.h_ref = torch.from_numpy(self.ref).pin_memory()
+        self.h_ii = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
+        self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
+        self.launches_per_step = 3  # iimg: 2 kernels, full_me: 1
+
+    def step(self, i):
+        k = i % self.n_rot
+        self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k], workspace=self.ws)
+        self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.R, out=self.d_mv[k])
+
+    def step_e2e(self, i):
+        k = i % self.n_rot
+        self.d_cur[k].copy_(self.h_cur, non_blocking=True)
+        self.d_ref[k].copy_(self.h_ref, non_blocking=True)
+        self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k], workspace=self.ws)
+        self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.R, out=self.d_mv[k])
+        self.h_ii.copy_(self.d_ii[k], non_blocking=True)
+        self.h_mv.copy_(self.d_mv[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return 2 * self.H * self.W, 4 * self.H * self.W + 12 * self.nblk
+
+    def check(self):
+        """Cheap correctness guard on the timed outputs (full check lives in tests)."""
+        mv = self.d_mv[0].cpu().numpy()
+        return float(np.mean(np.all(mv[:, :2] == self.true_mv, axis=1)))
+
+    def kernels(self, dev, peaks, n=200):
+        """Per-launch CUDA-event time of each kernel, on the launching stream."""
+        import torch
+        out = {}
+        st = torch.cuda.current_stream()
+        for name, fn in (("full_me_u8", lambda k: self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.R,
+                                                                      out=self.d_mv[k])),
+                         ("iimg_u8_i32", lambda k: self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k],
+                                                                       workspace=self.ws))):
+            for k in range(3):
+                fn(k)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+            torch.cuda.synchronize()
+            for i in range(n):
+                ev[i][0].record(st)
+                fn(i % self.n_rot)
+                ev[i][1].record(st)
+            torch.cuda.synchronize()
+            out[name] = sum(a.elapsed_time(b) for a, b in ev) / n
+        absdiff = self.nblk * (2 * self.R + 1) ** 2 * self.B * self.B
+        iimg_bytes = 5 * self.H * self.W
+        return out, absdiff, iimg_bytes
+
+    # CPU reference arm / baseline
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+        self.rng = np.random.default_rng(0)
+
+    def cpu_step(self, nblocks, threads):
+        blocks = self.rng.choice(self.nblk, size=nblocks, replace=False).astype(np.int32)
+        rows = max(1, round(self.H * nblocks / self.nblk))
+        self.orc.ref_iimg_u8(self.cur[:rows])
+        self.orc.ref_full_me_u8_argmin(self.cur, self.ref, self.B, self.R, blocks, threads=threads)
+        return nblocks / 1e6
+
+
+class Filter3x3:
+    """1024x1024 float32, 3x3 N(0,1) weights, zero padding."""
+    name = "filter3x3_1024"
+    H = W = 1024
+    metric = "filter3x3 GB/s"
+    unit = "GB/s"
+    dtype = "f32"
+
+    def __init__(self, seed=1):
+        from umi_gb300 import workloads
+        self.img, self.w9 = workloads.filter_image(seed=seed, h=self.H, w=self.W)
+
+    def config(self):
+        return {"workload": self.name, "image": f"{self.W}x{self.H} f32", "weights": "3x3 N(0,1)", "pad": 0.0,
+                "bytes_per_px": 8, "l2": "rotating input/output copies, consecutive steps touch > L2"}
+
+    def units_per_step(self):
+        return 8 * self.H * self.W / 1e9
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        self.U = U
+        per = 8 * self.H * self.W
+        self.n_rot = max(2, -(-2 * L2_BYTES // per))
+        x = torch.from_numpy(self.img).to(dev)
+        self.d_in = [x.clone() for _ in range(self.n_rot)]
+        self.d_out = [torch.empty_like(x) for _ in range(self.n_rot)]
+        self.h_in = torch.from_numpy(self.img).pin_memory()
+        self.h_out = torch.empty_like(self.h_in).pin_memory()
+        self.launches_per_step = 1
+
+    def step(self, i):
+        k = i % self.n_rot
+        self.U.filter3x3_f32(self.d_in[k], self.w9, out=self.d_out[k])
+
+    def step_e2e(self, i):
+        k = i % self.n_rot
+        self.d_in[k].copy_(self.h_in, non_blocking=True)
+        self.U.filter3x3_f32(self.d_in[k], self.w9, out=self.d_out[k])
+        self.h_out.copy_(self.d_out[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return 4 * self.H * self.W, 4 * self.H * self.W
+
+    def check(self):
+        return None
+
+    def kernels(self, dev, peaks, n=500):
+        import torch
+        st = torch.cuda.current_stream()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for k in range(3):
+            self.step(k)
+        torch.cuda.synchronize()
+        for i in range(n):
+            ev[i][0].record(st)
+            self.step(i)
+            ev[i][1].record(st)
+        torch.cuda.synchronize()
+        return {"filter3x3_f32": sum(a.elapsed_time(b) for a, b in ev) / n}, None, 8 * self.H * self.W
+
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+
+    def cpu_step(self, rows, threads):
+        self.orc.filter3x3_f64(self.img[:rows], self.w9, threads=threads)
+        return 8 * rows * self.W / 1e9
+
+
+WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3}
+
+
+# --------------------------------------------------------------------- arms
+def probe_sad4_peak(dev):
+    """Measured throughput (byte absdiffs/s) of the packed SAD instruction."""
+    import ctypes
+    import torch
+    from umi_gb300 import build
+    L = ctypes.CDLL(build.PROBE_LIB)
+    L.umi_probe_sad4_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.umi_probe_sad4_ops.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.umi_probe_sad4_ops.restype = ctypes.c_double
+    ctas, iters = torch.cuda.get_device_properties(dev).multi_processor_count * 8, 2048
+    out = torch.empty(ctas * 256, dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        rc = L.umi_probe_sad4_peak(0, ctas, iters, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(st.cuda_stream))
+        b.record(st)
+        torch.cuda.synchronize()
+        assert rc == 0
+        best = max(best, L.umi_probe_sad4_ops(ctas, iters) / (a.elapsed_time(b) * 1e-3))
+    return best
+
+
+def run_ours(args, wl, dist):
+    import torch
+    import umi_gb300 as U
+    U.lib()  # the CUDA library must be present: no fallback
+    torch.cuda.set_device(dist.local)
+    dev = torch.device("cuda", dist.local)
+    pk = peaks()
+    wl.setup(dev)
+    st = torch.cuda.current_stream()
+    for i in range(args.warmup):
+        wl.step(i)
+    torch.cuda.synchronize()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for i in range(args.steps):
+        wl.step(i)
+    e1.record(st)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(e0.elapsed_time(e1))
+    value = wl.units_per_step() * args.steps * dist.world / (ms * 1e-3)
+    sanity = wl.check()
+
+    # e2e: host buffers, copies inside the timed region
+    for i in range(min(args.warmup, 5)):
+        wl.step_e2e(i)
+    torch.cuda.synchronize()
+    dist.barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(st)
+    for i in range(args.steps):
+        wl.step_e2e(i)
+    e3.record(st)
+    torch.cuda.synchronize()
+    ms_e2e = dist.max(e2.elapsed_time(e3))
+    e2e_value = wl.units_per_step() * args.steps * dist.world / (ms_e2e * 1e-3)
+    h2d, d2h = wl.e2e_bytes()
+
+    # dominant kernel roofline
+    kms, absdiff, hbm_bytes = wl.kernels(dev, pk)
+    kernels = {}
+    if isinstance(wl, IntPair):
+        sad_peak = probe_sad4_peak(dev)
+        ach = absdiff / (kms["full_me_u8"] * 1e-3)
+        roof = {"bound": "int", "kernel": "full_me_u8", "achieved": ach / 1e9, "peak": sad_peak / 1e9,
+                "unit": "Gabsdiff/s", "frac": ach / sad_peak, "traffic": NCU_TRAFFIC[wl.name],
+                "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
+                "work_per_launch": absdiff, "ms_per_launch": kms["full_me_u8"]}
+        ig = hbm_bytes / (kms["iimg_u8_i32"] * 1e-3) / 1e9
+        kernels["iimg_u8_i32"] = {"ms_per_launch": kms["iimg_u8_i32"], "achieved": ig, "unit": "GB/s",
+                                  "peak": pk["hbm_gbs"], "frac": ig / pk["hbm_gbs"], "bytes_per_launch": hbm_bytes,
+                                  "peak_source": pk["source"]}
+    else:
+        ach = hbm_bytes / (kms["filter3x3_f32"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "filter3x3_f32", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / pk["hbm_gbs"], "traffic": NCU_TRAFFIC[wl.name], "peak_source": pk["source"],
+                "bytes_per_launch": hbm_bytes, "ms_per_launch": kms["filter3x3_f32"]}
+
+    line = {
+        "metric": wl.metric, "value": value, "unit": wl.unit, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded numpy generators)",
+        "config": dict(wl.config(), parallelism=f"replicas x{dist.world}"),
+        "e2e": {"value": e2e_value, "unit": wl.unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e / args.steps},
+        "gpu_launches": wl.launches_per_step * args.steps,
+        "roofline": roof, "kernels": kernels, "clocks": clk,
+        "impl": "ours",
+    }
+    if sanity is not None:
+        line["sanity_true_mv_recovered"] = sanity
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, sample_s=10.0)
+    return line
+
+
+def cpu_baseline(wl, sample_s=10.0):
+    """The reference's CPU loop (oracle restatement) on a bounded sample, all host threads."""
+    threads = os.cpu_count() or 1
+    wl.cpu_setup()
+    if isinstance(wl, IntPair):
+        chunk, what = 256, "random blocks of the 1080p pair, +-32 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin, plus the matching rows of iimg (main/iimg.cu:100-111)"
+    else:
+        chunk, what = 128, "rows of the 1024x1024 image, 3x3 weighted sum in FP64"
+    units, t0 = 0.0, time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < sample_s and n < 64:
+        units += wl.cpu_step(chunk, threads)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": units / dt, "unit": wl.unit, "cores": threads, "kind": "port",
+            "sample": f"{n} x {chunk} {what}; {dt:.1f} s"}
+
+
+def run_reference(args, wl, dist):
+    """The reference's own CPU implementation of the path (restated in the oracle), host cores only."""
+    if dist.rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    wl.cpu_setup()
+    per_step = 32 if isinstance(wl, IntPair) else 16
+    for _ in range(args.warmup):
+        wl.cpu_step(per_step, threads)
+    t0 = time.perf_counter()
+    units = 0.0
+    for _ in range(args.steps):
+        units += wl.cpu_step(per_step, threads)
+    dt = time.perf_counter() - t0
+    v = units / dt
+    return {
+        "metric": wl.metric, "value": v, "unit": wl.unit, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded numpy generators)",
+        "config": dict(wl.config(), parallelism="host cores"), "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": wl.unit, "cores": threads, "kind": "port",
+                         "sample": f"{per_step} {'blocks' if isinstance(wl, IntPair) else 'rows'} per step"},
+        "e2e": {"value": v, "unit": wl.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+
+
+def main():
+    args = parse()
+    wl = WORKLOADS[args.workload]()
+    if args.impl == "reference":
+        dist = Dist("gloo")
+        line = run_reference(args, wl, dist)
+    else:
+        dist = Dist("nccl")
+        line = run_ours(args, wl, dist)
+    if dist.rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    dist.done()
+
+
+if __name__ == "__main__":
+    main()

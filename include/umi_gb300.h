@@ -1,0 +1,165 @@
+/* umi_gb300: C ABI of the GB300 (sm_103a) implementation of the UMI operator.
+ *
+ * Everything here is plain C: raw device pointers, sizes, and a CUDA stream
+ * passed as `void*` (a cudaStream_t; NULL = the legacy default stream).  All
+ * entry points are asynchronous on that stream, never allocate device memory
+ * unless stated, keep no mutable global state, and report failures by status
+ * code (the reference aborts or ignores CUDA errors instead).
+ *
+ * The reference exposes one templated entry point, UMI::Execute
+ * (src/UMI_gpu.h:409-623).  Its two halves map onto this library as:
+ *   - validation + tiling (src/UMI.cpp:39-76, src/UMI_gpu.h:423-609)
+ *       -> umi_plan_build(), consumed by the header-only generic kernel in
+ *          include/umi/UMI_gpu.h (user functors are device code and must be
+ *          compiled in the caller's translation unit);
+ *   - the example applications (main/<app>.cu) -> the specialised
+ *     umi_<op>_<dtype> kernels below, each citing the application it
+ *     replaces.
+ */
+#ifndef UMI_GB300_H
+#define UMI_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status                                                              */
+/* ------------------------------------------------------------------ */
+typedef enum umi_status {
+	UMI_OK = 0,
+	UMI_ERR_INVALID_DESC = 1, /* descriptor rejected (reference: abort() at src/UMI.cpp:60,64) */
+	UMI_ERR_INVALID_ARG = 2,  /* null pointer, negative size, misaligned buffer */
+	UMI_ERR_UNSUPPORTED = 3,  /* valid request outside what this build implements */
+	UMI_ERR_CUDA = 4,         /* a CUDA runtime call failed (reference: ignored) */
+	UMI_ERR_NO_MEMORY = 5,    /* workspace too small */
+	UMI_ERR_TIMEOUT = 6       /* a bounded device-side wait gave up */
+} umi_status;
+
+/* Human-readable name of a status code. */
+const char* umi_status_string(int status);
+/* Detail of the last failure on the calling host thread ("" if none). */
+const char* umi_last_error_string(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int umi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* generic operator: descriptor validation and tiling                  */
+/* ------------------------------------------------------------------ */
+#define UMI_DIM 4
+#define UMI_MAX_PTR 4
+#define UMI_MAX_MEMS 16
+
+/* POD mirrors of the descriptor types of src/UMI.h:77-93. */
+typedef struct { int32_t total_size, block_size, warp_size, warp_shuf; } umi_pdim;
+typedef struct { int32_t total_size, block_size; } umi_adim;
+typedef struct { int32_t physical_dim_id, ofs, stride; } umi_vdim;
+typedef struct { int32_t size, mode; } umi_phydim; /* mode 0 = PAD, 1 = WRAP (clamp) */
+
+/* One memory (input or output) of a call.  stage: 0 Pre, 1 Loop, 2 Post. */
+typedef struct {
+	umi_vdim p_view[UMI_DIM];
+	umi_vdim a_view[UMI_DIM];
+	umi_phydim phys[UMI_DIM];
+	int32_t stage;
+	int32_t n_ptr;
+} umi_mem_desc;
+
+/* A whole call: src/UMI_gpu.h:416-422 without the pointers.  Memories are
+ * ordered like the reference: inputs (Pre, Loop, Post), then outputs
+ * (Pre, Loop, Post).  expand is the 16-bit Expand word (E0 = nibble 3). */
+typedef struct {
+	umi_pdim p[UMI_DIM];
+	umi_adim a[UMI_DIM];
+	uint32_t expand;
+	int32_t n_in, n_out;
+	umi_mem_desc mem[UMI_MAX_MEMS];
+} umi_desc;
+
+/* Per-memory closed-form address map: physical coordinate k of the element
+ * read/written for point p and accumulation index a is
+ *   base[k] + sum_d pcoef[k][d]*p[d] + sum_d acoef[k][d]*a[d];
+ * inputs clamp each coordinate to [0, size[k]-1] (pad_mask bit k: the value
+ * becomes the padding value instead), outputs do not clamp.  The linear
+ * element index is sum_k coord[k]*rowstride[k]. */
+typedef struct {
+	int32_t base[UMI_DIM];
+	int32_t pcoef[UMI_DIM][UMI_DIM];
+	int32_t acoef[UMI_DIM][UMI_DIM];
+	int32_t size[UMI_DIM];
+	int64_t rowstride[UMI_DIM];
+	int32_t pad_mask;
+	int32_t stage;
+	int32_t n_ptr;
+	int32_t is_output;
+} umi_mem_plan;
+
+/* Launch geometry of one call.  Tiling never changes results (only the
+ * accumulation order is fixed: blocked row-major over A). */
+typedef struct {
+	int32_t ptotal[UMI_DIM];
+	int32_t block[UMI_DIM];   /* threads per CTA along each P dim */
+	int32_t expand[UMI_DIM];  /* points per thread along each P dim */
+	int32_t grid[UMI_DIM];    /* CTAs along each P dim */
+	int64_t n_cta;
+	int32_t n_threads;
+	int32_t atotal[UMI_DIM];
+	int32_t ablock[UMI_DIM];
+	int32_t agrid[UMI_DIM];
+	int32_t n_ablock;         /* product of agrid (0 when A is empty) */
+	int32_t ablock_size;      /* product of ablock */
+	int32_t n_in, n_out;
+	umi_mem_plan mem[UMI_MAX_MEMS];
+} umi_plan;
+
+/* Validate `desc` (same rules as src/UMI.cpp:39-66: the product of the
+ * warp sizes is 32, every warp_shuf a power of two (0 read as 1), every
+ * block_size divisible by warp_size*warp_shuf; plus: at most 1024 threads,
+ * positive blocks, PtrNum nibbles <= 4, <= 16 memories) and fill `plan`.
+ * Reference: PDims_packed / ADims_packed ctors + the table builders of
+ * Execute (src/UMI.cpp:39-226, src/UMI_gpu.h:423-609), which abort instead of
+ * returning UMI_ERR_INVALID_DESC. */
+umi_status umi_plan_build(const umi_desc* desc, umi_plan* plan);
+
+/* ------------------------------------------------------------------ */
+/* specialised kernels                                                 */
+/* ------------------------------------------------------------------ */
+
+/* 3x3 weighted filter, float32, (h, w) row-major, out-of-image pixels read
+ * as `pad`.  out[y,x] = sum_{dy,dx} w9[3*(dy+1)+(dx+1)] * in[y+dy, x+dx].
+ * w9 is a HOST array of 9 floats (copied into the launch).  in/out must not
+ * alias.  Replaces main/filter3x3.cu:37-58 and main/wfilter3x3.cu:39-69
+ * (their Execute calls) for float images. */
+umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, int32_t w, const float* w9, float pad,
+                             void* stream);
+
+/* Integral image, uint8 -> int32: out[y,x] = sum_{y'<=y, x'<=x} in[y',x'].
+ * Replaces the two Execute calls of main/iimg.cu:37-82 (row prefix through a
+ * Loop output, transposed, twice).  Needs a device workspace of
+ * umi_iimg_u8_i32_workspace_bytes(h, w) bytes (16-byte aligned). */
+size_t umi_iimg_u8_i32_workspace_bytes(int32_t h, int32_t w);
+umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
+/* Full-search block motion estimation with fused argmin, uint8 frames.
+ * For every b x b block of `cur` (blocks truncated at the frame edge:
+ * h/b x w/b, as main/full_me.cu:35), searches displacements (dy, dx) in
+ * [cy-r, cy+r] x [cx-r, cx+r] of `ref`, where (cy, cx) is the block's search
+ * centre (0,0 when `centers` is NULL, else centers[2*blk], centers[2*blk+1]).
+ * Reference pixels outside the frame are edge-replicated (the WRAP mode of
+ * main/full_me.cu:41, checked by its clamp at :75-78).
+ * mv receives (mv_y, mv_x, sad) int32 per block, blocks in raster order: the
+ * minimum SAD, ties resolved to the first displacement in raster order of
+ * (dy, dx).  b in {8, 16}; 1 <= r <= 64; pitch = w. */
+umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
+                          const int32_t* centers, int32_t* mv, void* stream);
+/* The same search without the argmin: writes the whole SAD volume
+ * (h/b, w/b, 2r+1, 2r+1) int32, the output layout of main/full_me.cu:55-62. */
+umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
+                              int32_t* sad, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UMI_GB300_H */

@@ -1,0 +1,166 @@
+"""GPU parity tests of the specialised kernels, through the C ABI, against the
+CPU oracle on the same seeded inputs.
+
+Integer work (iimg, full_me) must be bit-exact.  The float filter is compared
+with the FP64 oracle at rel <= 1e-5 where
+rel = |y - y64| / max(|y64|, sum |w * x|)  (the scale of the sum, so that
+outputs that cancel to ~0 are judged against the magnitude of their terms).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FILTER_REL_TOL = 1e-5
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+# ---------------------------------------------------------------- filter3x3
+def _filter_scale(x, w9, pad):
+    p = np.pad(np.abs(x.astype(np.float64)), 1, constant_values=abs(pad))
+    s = np.zeros(x.shape)
+    for i in range(3):
+        for j in range(3):
+            s += abs(float(w9[3 * i + j])) * p[i:i + x.shape[0], j:j + x.shape[1]]
+    return s
+
+
+@pytest.mark.parametrize("h,w,pad", [(1024, 1024, 0.0), (1, 1, 0.0), (3, 5, 2.5), (37, 131, 0.0), (130, 257, -1.0),
+                                     (64, 128, 0.0), (33, 4, 0.0)])
+def test_filter3x3_f32(umi, orc, dev, h, w, pad):
+    from umi_gb300 import workloads
+    x, w9 = workloads.filter_image(seed=h * 7 + w, h=h, w=w)
+    got = umi.filter3x3_f32(_t(x, dev), w9, pad=pad).cpu().numpy()
+    want = orc.filter3x3_f64(x, w9, pad=pad)
+    rel = np.abs(got - want) / np.maximum(np.abs(want), _filter_scale(x, w9, pad))
+    assert rel.max() <= FILTER_REL_TOL, rel.max()
+
+
+def test_filter3x3_rejects_alias(umi, dev):
+    import torch
+    x = torch.zeros(8, 8, device=dev)
+    with pytest.raises(umi.UmiError):
+        umi.filter3x3_f32(x, [0.0] * 9, out=x)
+
+
+# ---------------------------------------------------------------- iimg
+@pytest.mark.parametrize("h,w", [(1080, 1920), (1, 1), (1, 130), (97, 1), (31, 127), (33, 129), (256, 256),
+                                 (300, 500), (517, 1023)])
+def test_iimg_u8_i32(umi, orc, dev, h, w):
+    from umi_gb300 import workloads
+    x = workloads.iimg_frame(seed=h + w, h=h, w=w)
+    got = umi.iimg_u8_i32(_t(x, dev)).cpu().numpy()
+    assert np.array_equal(got, orc.iimg_u8_i32(x))
+
+
+def test_iimg_all_255_max_value(umi, orc, dev):
+    # the largest value of the 1080p workload: 1920*1080*255 < 2^31
+    x = np.full((1080, 1920), 255, np.uint8)
+    got = umi.iimg_u8_i32(_t(x, dev)).cpu().numpy()
+    assert got[-1, -1] == 1920 * 1080 * 255
+    assert np.array_equal(got, orc.iimg_u8_i32(x))
+
+
+def test_iimg_unaligned_views(umi, orc, dev):
+    import torch
+    x = np.random.default_rng(7).integers(0, 256, (50, 61), dtype=np.uint8)
+    big = torch.zeros(50 * 61 + 3, dtype=torch.uint8, device=dev)
+    big[3:] = _t(x.ravel(), dev)
+    inp = big[3:].view(50, 61)  # 3-byte offset: byte loads path
+    out_big = torch.zeros(50 * 61 + 1, dtype=torch.int32, device=dev)
+    out = out_big[1:].view(50, 61)  # 4-byte offset: scalar stores path
+    umi.iimg_u8_i32(inp, out=out)
+    assert np.array_equal(out.cpu().numpy(), orc.iimg_u8_i32(x))
+
+
+def test_iimg_repeated_calls_reuse_workspace(umi, orc, dev):
+    import torch
+    ws = torch.empty(umi.iimg_workspace_bytes(200, 300), dtype=torch.uint8, device=dev)
+    for seed in range(3):
+        x = np.random.default_rng(seed).integers(0, 256, (200, 300), dtype=np.uint8)
+        got = umi.iimg_u8_i32(_t(x, dev), workspace=ws).cpu().numpy()
+        assert np.array_equal(got, orc.iimg_u8_i32(x))
+
+
+# ---------------------------------------------------------------- full_me
+@pytest.mark.parametrize("h,w,b,r", [(64, 64, 16, 4), (48, 80, 16, 7), (64, 96, 8, 7), (96, 128, 16, 32),
+                                     (40, 56, 8, 3), (17, 33, 16, 5), (130, 70, 16, 64), (50, 70, 8, 13)])
+def test_full_me_u8_random(umi, orc, dev, h, w, b, r):
+    g = np.random.default_rng(h * 1000 + w + r)
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = g.integers(0, 256, (h, w), dtype=np.uint8)
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), b, r).cpu().numpy()
+    assert np.array_equal(got, orc.full_me_u8(cur, ref, b, r))
+
+
+def test_full_me_u8_ties_first_in_raster_order(umi, orc, dev):
+    # flat frames: every displacement ties, the first (-r, -r) must win
+    cur = np.full((64, 64), 7, np.uint8)
+    ref = np.full((64, 64), 9, np.uint8)
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, 6).cpu().numpy()
+    assert np.all(got[:, 0] == -6) and np.all(got[:, 1] == -6) and np.all(got[:, 2] == 2 * 256)
+    assert np.array_equal(got, orc.full_me_u8(cur, ref, 16, 6))
+
+
+def test_full_me_u8_extremes(umi, orc, dev):
+    # maximum SAD: 0 vs 255 everywhere
+    cur = np.zeros((32, 32), np.uint8)
+    ref = np.full((32, 32), 255, np.uint8)
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, 32).cpu().numpy()
+    assert np.all(got[:, 2] == 255 * 256)
+    assert np.array_equal(got, orc.full_me_u8(cur, ref, 16, 32))
+
+
+def test_full_me_u8_centers(umi, orc, dev):
+    import torch
+    g = np.random.default_rng(11)
+    cur = g.integers(0, 256, (64, 80), dtype=np.uint8)
+    ref = g.integers(0, 256, (64, 80), dtype=np.uint8)
+    n = (64 // 16) * (80 // 16)
+    centers = g.integers(-20, 21, (n, 2)).astype(np.int32)
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, 4, centers=_t(centers, dev)).cpu().numpy()
+    for i in range(n):
+        by, bx = divmod(i, 80 // 16)
+        best = None
+        for dy in range(centers[i, 0] - 4, centers[i, 0] + 5):
+            for dx in range(centers[i, 1] - 4, centers[i, 1] + 5):
+                s = orc.block_sad_u8(cur, ref, 16, by, bx, dy, dx)
+                if best is None or s < best[0]:
+                    best = (s, dy, dx)
+        assert tuple(got[i]) == (best[1], best[2], best[0])
+
+
+def test_full_me_sad_volume(umi, orc, dev):
+    g = np.random.default_rng(12)
+    cur = g.integers(0, 256, (48, 64), dtype=np.uint8)
+    ref = g.integers(0, 256, (48, 64), dtype=np.uint8)
+    for b, r in [(16, 5), (8, 7), (16, 32)]:
+        got = umi.full_me_sad_u8(_t(cur, dev), _t(ref, dev), b, r).cpu().numpy()
+        _, want = orc.full_me_u8(cur, ref, b, r, sad_volume=True)
+        assert np.array_equal(got, want)
+
+
+def test_full_me_sad_volume_matches_reference_loop(umi, orc, dev):
+    # the reference example's own check (main/full_me.cu:66-87) on a u8 pair
+    g = np.random.default_rng(13)
+    cur = g.integers(0, 256, (40, 64), dtype=np.uint8)
+    ref = g.integers(0, 256, (40, 64), dtype=np.uint8)
+    got = umi.full_me_sad_u8(_t(cur, dev), _t(ref, dev), 8, 7).cpu().numpy()
+    want = orc.ref_full_me_i32(cur.astype(np.int32), ref.astype(np.int32), 8, -7, 15)
+    assert np.array_equal(got, want)
+
+
+def test_full_me_u8_1080p_workload(umi, orc, dev):
+    """The benchmark workload: 1920x1080 pair, 16x16 blocks, +-32, all 8040 blocks."""
+    from umi_gb300 import workloads
+    cur, ref, true_mv = workloads.me_pair(seed=3)
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, 32).cpu().numpy()
+    assert got.shape == (8040, 3)
+    want = orc.full_me_u8(cur, ref, 16, 32)
+    assert np.array_equal(got, want)
+    # sanity: most blocks recover the planted translation
+    assert np.mean(np.all(got[:, :2] == true_mv, axis=1)) > 0.8

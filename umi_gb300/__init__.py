@@ -1,0 +1,256 @@
+"""umi_gb300: GB300 (sm_103a) implementation of the UMI operator.
+
+Python bindings over the C ABI of libumi_gb300.so (include/umi_gb300.h).
+Every call goes straight to a CUDA kernel of this library on the caller's
+current torch CUDA stream; there is no CPU fallback.  If the library is
+missing, importing works but the first call raises UmiLibraryMissing (build
+it with `python -m umi_gb300.build`).
+
+torch is used only as the device-memory and stream provider: tensors are
+passed to the C ABI as raw pointers.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libumi_gb300.so")
+HEADER = os.path.join(ROOT, "include", "umi_gb300.h")
+
+UMI_OK = 0
+STATUS_NAMES = {
+    0: "UMI_OK", 1: "UMI_ERR_INVALID_DESC", 2: "UMI_ERR_INVALID_ARG", 3: "UMI_ERR_UNSUPPORTED",
+    4: "UMI_ERR_CUDA", 5: "UMI_ERR_NO_MEMORY", 6: "UMI_ERR_TIMEOUT",
+}
+
+
+class UmiLibraryMissing(RuntimeError):
+    pass
+
+
+class UmiError(RuntimeError):
+    def __init__(self, status: int, fn: str, detail: str):
+        self.status = status
+        super().__init__(f"{fn}: {STATUS_NAMES.get(status, status)}: {detail}")
+
+
+_LIB = None
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_f32 = ctypes.c_float
+_sz = ctypes.c_size_t
+
+# C signatures (argtypes, restype) of every entry point in include/umi_gb300.h.
+SIGNATURES = {
+    "umi_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "umi_last_error_string": ([], ctypes.c_char_p),
+    "umi_version": ([], ctypes.c_int),
+    "umi_plan_build": ([_vp, _vp], ctypes.c_int),
+    "umi_filter3x3_f32": ([_vp, _vp, _i32, _i32, _vp, _f32, _vp], ctypes.c_int),
+    "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
+    "umi_iimg_u8_i32": ([_vp, _vp, _i32, _i32, _vp, _sz, _vp], ctypes.c_int),
+    "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+}
+
+
+# ---- descriptor structs (mirror include/umi_gb300.h) ----
+
+class PDim(ctypes.Structure):
+    _fields_ = [("total_size", _i32), ("block_size", _i32), ("warp_size", _i32), ("warp_shuf", _i32)]
+
+
+class ADim(ctypes.Structure):
+    _fields_ = [("total_size", _i32), ("block_size", _i32)]
+
+
+class VDim(ctypes.Structure):
+    _fields_ = [("physical_dim_id", _i32), ("ofs", _i32), ("stride", _i32)]
+
+
+class PhyDim(ctypes.Structure):
+    _fields_ = [("size", _i32), ("mode", _i32)]
+
+
+class MemDesc(ctypes.Structure):
+    _fields_ = [("p_view", VDim * 4), ("a_view", VDim * 4), ("phys", PhyDim * 4), ("stage", _i32), ("n_ptr", _i32)]
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("p", PDim * 4), ("a", ADim * 4), ("expand", ctypes.c_uint32), ("n_in", _i32), ("n_out", _i32),
+                ("mem", MemDesc * 16)]
+
+
+class MemPlan(ctypes.Structure):
+    _fields_ = [("base", _i32 * 4), ("pcoef", (_i32 * 4) * 4), ("acoef", (_i32 * 4) * 4), ("size", _i32 * 4),
+                ("rowstride", ctypes.c_int64 * 4), ("pad_mask", _i32), ("stage", _i32), ("n_ptr", _i32),
+                ("is_output", _i32)]
+
+
+class Plan(ctypes.Structure):
+    _fields_ = [("ptotal", _i32 * 4), ("block", _i32 * 4), ("expand", _i32 * 4), ("grid", _i32 * 4),
+                ("n_cta", ctypes.c_int64), ("n_threads", _i32), ("atotal", _i32 * 4), ("ablock", _i32 * 4),
+                ("agrid", _i32 * 4), ("n_ablock", _i32), ("ablock_size", _i32), ("n_in", _i32), ("n_out", _i32),
+                ("mem", MemPlan * 16)]
+
+
+PAD, WRAP = 0, 1
+
+
+def make_desc(p, a, mems, expand: int = 0x1111, n_in: int | None = None) -> Desc:
+    """Build a Desc from python lists.
+
+    p: 4 tuples (total, block, warp, shuf); a: 4 tuples (total, block);
+    mems: list of dicts {p_view: 4 (dim, ofs, stride), a_view: ..., phys: 4 (size, mode),
+    stage: 0/1/2, n_ptr: int, out: bool}; inputs must precede outputs."""
+    d = Desc()
+    for i, t in enumerate(p):
+        t = tuple(t) + (0,) * (4 - len(t))
+        d.p[i] = PDim(*t)
+    for i, t in enumerate(a):
+        d.a[i] = ADim(*t)
+    d.expand = expand
+    ins = [m for m in mems if not m.get("out")]
+    outs = [m for m in mems if m.get("out")]
+    d.n_in = len(ins) if n_in is None else n_in
+    d.n_out = len(outs)
+    for i, m in enumerate(ins + outs):
+        md = d.mem[i]
+        for k, v in enumerate(m.get("p_view", [()] * 4)):
+            md.p_view[k] = VDim(*(tuple(v) + (0,) * (3 - len(v))))
+        for k, v in enumerate(m.get("a_view", [()] * 4)):
+            md.a_view[k] = VDim(*(tuple(v) + (0,) * (3 - len(v))))
+        for k, v in enumerate(m.get("phys", [()] * 4)):
+            md.phys[k] = PhyDim(*(tuple(v) + (0,) * (2 - len(v))))
+        md.stage = m.get("stage", 1)
+        md.n_ptr = m.get("n_ptr", 1)
+    return d
+
+
+def plan_build(desc: Desc) -> Plan:
+    """Validate a descriptor and return its launch plan (umi_plan_build)."""
+    plan = Plan()
+    check(lib().umi_plan_build(ctypes.byref(desc), ctypes.byref(plan)), "umi_plan_build")
+    return plan
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/umi_gb300.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(umi_[a-z0-9_]+)\s*\(", text, flags=re.M)
+
+
+def lib():
+    """Load libumi_gb300.so (raises UmiLibraryMissing if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise UmiLibraryMissing(f"{LIB_PATH} not built: run `python -m umi_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def check(status: int, fn: str) -> None:
+    if status != UMI_OK:
+        detail = lib().umi_last_error_string().decode(errors="replace")
+        raise UmiError(status, fn, detail)
+
+
+def _stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _need(t, dtype, name):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+def filter3x3_f32(inp, w9, pad: float = 0.0, out=None, stream=None):
+    """3x3 weighted filter of a float32 (h, w) CUDA tensor (umi_filter3x3_f32)."""
+    import torch
+    _need(inp, torch.float32, "inp")
+    h, w = inp.shape
+    if out is None:
+        out = torch.empty_like(inp)
+    _need(out, torch.float32, "out")
+    wv = (ctypes.c_float * 9)(*[float(v) for v in list(w9)])
+    check(lib().umi_filter3x3_f32(_ptr(inp), _ptr(out), h, w, wv, float(pad), _stream_ptr(stream)),
+          "umi_filter3x3_f32")
+    return out
+
+
+def iimg_workspace_bytes(h: int, w: int) -> int:
+    return int(lib().umi_iimg_u8_i32_workspace_bytes(h, w))
+
+
+def iimg_u8_i32(inp, out=None, workspace=None, stream=None):
+    """Integral image of a uint8 (h, w) CUDA tensor into int32 (umi_iimg_u8_i32)."""
+    import torch
+    _need(inp, torch.uint8, "inp")
+    h, w = inp.shape
+    if out is None:
+        out = torch.empty((h, w), dtype=torch.int32, device=inp.device)
+    _need(out, torch.int32, "out")
+    nbytes = iimg_workspace_bytes(h, w)
+    if workspace is None:
+        workspace = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=inp.device)
+    check(lib().umi_iimg_u8_i32(_ptr(inp), _ptr(out), h, w, _ptr(workspace), workspace.numel(),
+                                _stream_ptr(stream)), "umi_iimg_u8_i32")
+    return out
+
+
+def full_me_u8(cur, ref, block: int = 16, search: int = 32, centers=None, out=None, stream=None):
+    """Full-search motion estimation with argmin (umi_full_me_u8).
+
+    Returns an int32 (h//block * w//block, 3) tensor of (mv_y, mv_x, sad)."""
+    import torch
+    _need(cur, torch.uint8, "cur")
+    _need(ref, torch.uint8, "ref")
+    if cur.shape != ref.shape:
+        raise ValueError("cur and ref differ in shape")
+    h, w = cur.shape
+    n = (h // block) * (w // block)
+    if out is None:
+        out = torch.empty((n, 3), dtype=torch.int32, device=cur.device)
+    _need(out, torch.int32, "out")
+    if centers is not None:
+        _need(centers, torch.int32, "centers")
+    check(lib().umi_full_me_u8(_ptr(cur), _ptr(ref), h, w, block, search, _ptr(centers), _ptr(out),
+                               _stream_ptr(stream)), "umi_full_me_u8")
+    return out
+
+
+def full_me_sad_u8(cur, ref, block: int = 16, search: int = 32, out=None, stream=None):
+    """Whole SAD volume (h//b, w//b, 2r+1, 2r+1) int32 (umi_full_me_sad_u8)."""
+    import torch
+    _need(cur, torch.uint8, "cur")
+    _need(ref, torch.uint8, "ref")
+    h, w = cur.shape
+    nd = 2 * search + 1
+    if out is None:
+        out = torch.empty((h // block, w // block, nd, nd), dtype=torch.int32, device=cur.device)
+    _need(out, torch.int32, "out")
+    check(lib().umi_full_me_sad_u8(_ptr(cur), _ptr(ref), h, w, block, search, _ptr(out), _stream_ptr(stream)),
+          "umi_full_me_sad_u8")
+    return out

@@ -1,0 +1,263 @@
+// Full-search block motion estimation on uint8 frames, sm_103a.
+//
+// Replaces the Execute call of main/full_me.cu:34-64 (MotionEst strategy,
+// main/full_me.cu:8-15: sad += |cur - ref| over a b x b block for every
+// displacement, reference pixels clamped to the frame) and adds the argmin
+// the reference leaves to the caller.
+//
+// Design (integer pipe, everything on-chip):
+//  * one CTA searches M macroblocks; the reference window of each
+//    ((b + 2r) x (b + 2r) bytes, edge-replicated) is staged once in shared
+//    memory, in four copies shifted by 0..3 bytes so that any horizontal
+//    displacement reads whole aligned 32-bit words;
+//  * a thread owns one horizontal displacement ix and G consecutive vertical
+//    displacements; the b x b current block lives in registers (b*b/4 words),
+//    window rows stream through registers once, and each (window row, block
+//    row) pair costs b/4 `vabsdiff4 ... .add` instructions (4 byte
+//    |a-b| plus accumulate in one instruction);
+//  * the argmin is fused: key = (sad << 15) | raster index of (dy, dx), a
+//    shared-memory atomicMin per macroblock gives the minimum SAD with the
+//    first displacement in raster order (the reference's output order
+//    (..., sy, sx), main/full_me.cu:70-71).
+#include <algorithm>
+
+#include "common.h"
+
+namespace {
+
+constexpr int kMaxR = 64;
+
+__device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c) {
+	uint32_t d;
+	asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+	return d;
+}
+
+struct MeGeom {
+	int h, w, b, r;
+	int nbx, nblk;
+	int ndx;          // 2r + 1 displacements per axis
+	int ng;           // groups of G vertical displacements
+	int win_rows;     // rows staged per window (ng*G + b - 1)
+	int win_words;    // 32-bit words per staged row
+	int copy_stride;  // words between the four shifted copies
+	int mb_stride;    // words per macroblock (4 copies + current block)
+	int m;            // macroblocks per CTA
+	int tasks_per_mb; // ndx * ng
+	int vec_ok;       // ref is 4-byte aligned and w % 4 == 0: word loads allowed
+};
+
+template <int B, int G, bool VOLUME>
+__global__ void __launch_bounds__(512) full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
+                                                      const int32_t* __restrict__ centers, int32_t* __restrict__ out,
+                                                      const MeGeom g) {
+	extern __shared__ __align__(16) uint32_t smem[];
+	constexpr int BW = B / 4;  // words per block row
+	__shared__ uint32_t best[64];
+	const int tid = threadIdx.x;
+	const int mb0 = blockIdx.x * g.m;
+
+	// 1. Stage windows (copy 0) and current blocks.
+	for (int m = 0; m < g.m; ++m) {
+		const int blk = mb0 + m;
+		if (blk >= g.nblk) break;
+		const int by = blk / g.nbx, bx = blk - by * g.nbx;
+		const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
+		const int gy0 = by * B + cy - g.r, gx0 = bx * B + cx - g.r;
+		uint32_t* win = smem + m * g.mb_stride;
+		const int nwords = g.win_rows * g.win_words;
+		for (int i = tid; i < nwords; i += blockDim.x) {
+			const int row = i / g.win_words, wd = i - row * g.win_words;
+			const int gy = min(max(gy0 + row, 0), g.h - 1);
+			const uint8_t* src = ref + (size_t)gy * g.w;
+			const int gx = gx0 + 4 * wd;
+			uint32_t v;
+			if (g.vec_ok && gx >= 0 && gx + 3 < g.w && (gx & 3) == 0) {
+				v = __ldg(reinterpret_cast<const uint32_t*>(src + gx));
+			} else {
+				v = 0;
+#pragma unroll
+				for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + min(max(gx + k, 0), g.w - 1)) << (8 * k);
+			}
+			win[row * g.win_words + wd] = v;
+		}
+		uint32_t* cb = win + 4 * g.copy_stride;
+		for (int i = tid; i < B * BW; i += blockDim.x) {
+			const int row = i / BW, wd = i - row * BW;
+			const uint8_t* src = cur + (size_t)(by * B + row) * g.w + bx * B + 4 * wd;
+			uint32_t v = 0;
+#pragma unroll
+			for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + k) << (8 * k);
+			cb[i] = v;
+		}
+		if (tid == 0) best[m] = 0xffffffffu;
+	}
+	__syncthreads();
+	// 2. Shifted copies s = 1..3: word k holds bytes [4k+s, 4k+s+4) of the row.
+	for (int m = 0; m < g.m; ++m) {
+		if (mb0 + m >= g.nblk) break;
+		uint32_t* win = smem + m * g.mb_stride;
+		const int nwords = g.win_rows * g.win_words;
+		for (int i = tid; i < 3 * nwords; i += blockDim.x) {
+			const int s = 1 + i / nwords, j = i - (s - 1) * nwords;
+			const int wd = j % g.win_words;
+			const uint32_t lo = win[j], hi = (wd + 1 < g.win_words) ? win[j + 1] : 0u;
+			win[s * g.copy_stride + j] = __funnelshift_r(lo, hi, 8 * s);
+		}
+	}
+	__syncthreads();
+
+	// 3. Search.
+	const int total = g.m * g.tasks_per_mb;
+	for (int t = tid; t < total; t += blockDim.x) {
+		const int m = t / g.tasks_per_mb;
+		const int rem = t - m * g.tasks_per_mb;
+		const int grp = rem / g.ndx, ix = rem - grp * g.ndx;
+		const int blk = mb0 + m;
+		if (blk >= g.nblk) continue;
+		const uint32_t* win = smem + m * g.mb_stride;
+		const uint32_t* cb = win + 4 * g.copy_stride;
+		uint32_t cv[B][BW];
+#pragma unroll
+		for (int py = 0; py < B; ++py)
+#pragma unroll
+			for (int k = 0; k < BW; ++k) cv[py][k] = cb[py * BW + k];
+		const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + grp * G * g.win_words;
+		uint32_t acc[G];
+#pragma unroll
+		for (int q = 0; q < G; ++q) acc[q] = 0;
+#pragma unroll
+		for (int j = 0; j < G + B - 1; ++j) {
+			uint32_t wv[BW];
+#pragma unroll
+			for (int k = 0; k < BW; ++k) wv[k] = wp[j * g.win_words + k];
+#pragma unroll
+			for (int q = 0; q < G; ++q) {
+				const int py = j - q;
+				if (py >= 0 && py < B) {
+#pragma unroll
+					for (int k = 0; k < BW; ++k) acc[q] = sad4_acc(cv[py][k], wv[k], acc[q]);
+				}
+			}
+		}
+		const int iy0 = grp * G;
+		if (VOLUME) {
+			int32_t* o = out + (size_t)blk * g.ndx * g.ndx;
+#pragma unroll
+			for (int q = 0; q < G; ++q)
+				if (iy0 + q < g.ndx) o[(iy0 + q) * g.ndx + ix] = (int32_t)acc[q];
+		} else {
+			uint32_t key = 0xffffffffu;
+#pragma unroll
+			for (int q = 0; q < G; ++q)
+				if (iy0 + q < g.ndx) key = min(key, (acc[q] << 15) | (uint32_t)((iy0 + q) * g.ndx + ix));
+			atomicMin(&best[m], key);
+		}
+	}
+	if (VOLUME) return;
+	__syncthreads();
+	for (int m = tid; m < g.m; m += blockDim.x) {
+		const int blk = mb0 + m;
+		if (blk >= g.nblk) break;
+		const uint32_t key = best[m];
+		const int idx = (int)(key & 0x7fffu);
+		const int iy = idx / g.ndx, ix = idx - iy * g.ndx;
+		const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
+		out[3 * blk + 0] = cy + iy - g.r;
+		out[3 * blk + 1] = cx + ix - g.r;
+		out[3 * blk + 2] = (int32_t)(key >> 15);
+	}
+}
+
+// Vertical displacements per thread: the candidate that wastes the fewest
+// padded rows (ng*G - ndx), larger G on ties (fewer window-row loads).
+int pick_g(int ndx) {
+	const int cands[] = {15, 13, 9, 5};
+	int best = cands[0], waste = 1 << 30;
+	for (int gcand : cands) {
+		const int ng = (ndx + gcand - 1) / gcand;
+		const int wst = ng * gcand - ndx;
+		if (wst < waste) { waste = wst; best = gcand; }
+	}
+	return best;
+}
+
+template <int B, int G, bool V>
+umi_status launch_g(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
+                    int threads, size_t smem, cudaStream_t st) {
+	auto kern = full_me_kernel<B, G, V>;
+	if (smem > 48 * 1024) UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                                                 (int)smem), "cudaFuncSetAttribute"));
+	const int grid = (g.nblk + g.m - 1) / g.m;
+	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
+	return umi::launch_status("full_me_kernel");
+}
+
+template <int B, bool V>
+umi_status launch_b(int G, const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out,
+                    const MeGeom& g, int threads, size_t smem, cudaStream_t st) {
+	switch (G) {
+		case 5: return launch_g<B, 5, V>(cur, ref, centers, out, g, threads, smem, st);
+		case 9: return launch_g<B, 9, V>(cur, ref, centers, out, g, threads, smem, st);
+		case 13: return launch_g<B, 13, V>(cur, ref, centers, out, g, threads, smem, st);
+		default: return launch_g<B, 15, V>(cur, ref, centers, out, g, threads, smem, st);
+	}
+}
+
+umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
+                          const int32_t* centers, int32_t* out, bool volume, void* stream) {
+	if (!cur || !ref || !out) return umi::fail(UMI_ERR_INVALID_ARG, "full_me: null pointer");
+	if (h < 0 || w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "full_me: negative size %dx%d", h, w);
+	if (b != 8 && b != 16) return umi::fail(UMI_ERR_UNSUPPORTED, "full_me: block size %d (supported: 8, 16)", b);
+	if (r < 1 || r > kMaxR) return umi::fail(UMI_ERR_UNSUPPORTED, "full_me: search range %d (supported 1..%d)", r, kMaxR);
+	MeGeom g{};
+	g.h = h; g.w = w; g.b = b; g.r = r;
+	g.nbx = w / b;
+	g.nblk = (h / b) * g.nbx;
+	if (g.nblk == 0) return umi::ok();
+	g.ndx = 2 * r + 1;
+	const int G = pick_g(g.ndx);
+	g.ng = (g.ndx + G - 1) / G;
+	g.win_rows = g.ng * G + b - 1;
+	g.win_words = (2 * r + b + 3) / 4 + 1;
+	const int copy = g.win_rows * g.win_words;
+	g.copy_stride = ((copy + 31) / 32) * 32 + 8;  // copies land 8 banks apart
+	g.mb_stride = 4 * g.copy_stride + b * b / 4 + 4;
+	g.mb_stride = (g.mb_stride + 3) & ~3;         // keep each current block 16-byte aligned
+	g.tasks_per_mb = g.ndx * g.ng;
+	g.vec_ok = umi::aligned(ref, 4) && (w % 4) == 0;
+	// Macroblocks per CTA: enough tasks to fill at least ~256 threads, within
+	// 96 KB of shared memory and the 64-slot argmin table.
+	int m = std::max(1, 256 / g.tasks_per_mb);
+	const int max_m_smem = std::max(1, (int)((96 * 1024) / (g.mb_stride * 4)));
+	m = std::min(std::min(m, max_m_smem), 64);
+	g.m = m;
+	const int total = m * g.tasks_per_mb;
+	int threads = ((total + 31) / 32) * 32;
+	if (threads > 512) {
+		const int iters = (total + 511) / 512;
+		threads = (((total + iters - 1) / iters) + 31) / 32 * 32;
+	}
+	const size_t smem = (size_t)m * g.mb_stride * 4;
+	const cudaStream_t st = umi::as_stream(stream);
+	umi_status rc;
+	if (b == 16)
+		rc = volume ? launch_b<16, true>(G, cur, ref, centers, out, g, threads, smem, st)
+		            : launch_b<16, false>(G, cur, ref, centers, out, g, threads, smem, st);
+	else
+		rc = volume ? launch_b<8, true>(G, cur, ref, centers, out, g, threads, smem, st)
+		            : launch_b<8, false>(G, cur, ref, centers, out, g, threads, smem, st);
+	return rc == UMI_OK ? umi::ok() : rc;
+}
+
+}  // namespace
+
+extern "C" umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b,
+                                     int32_t r, const int32_t* centers, int32_t* mv, void* stream) {
+	return full_me_common(cur, ref, h, w, b, r, centers, mv, false, stream);
+}
+
+extern "C" umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b,
+                                         int32_t r, int32_t* sad, void* stream) {
+	return full_me_common(cur, ref, h, w, b, r, nullptr, sad, true, stream);
+}
