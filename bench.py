@@ -45,12 +45,15 @@ NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024"], default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.steps is None:
+        a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000}[a.workload]
+    return a
 
 
 def peaks():
@@ -213,25 +216,16 @@ class IntPair:
         mv = self.d_mv[0].cpu().numpy()
         return float(np.mean(np.all(mv[:, :2] == self.true_mv, axis=1)))
 
-    def kernels(self, dev, peaks, n=200):
-        """Per-launch CUDA-event time of each kernel, on the launching stream."""
-        import torch
-        out = {}
-        st = torch.cuda.current_stream()
-        for name, fn in (("full_me_u8", lambda k: self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.R,
-                                                                      out=self.d_mv[k])),
-                         ("iimg_u8_i32", lambda k: self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k],
-                                                                       workspace=self.ws))):
-            for k in range(3):
-                fn(k)
-            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
-            torch.cuda.synchronize()
-            for i in range(n):
-                ev[i][0].record(st)
-                fn(i % self.n_rot)
-                ev[i][1].record(st)
-            torch.cuda.synchronize()
-            out[name] = sum(a.elapsed_time(b) for a, b in ev) / n
+    def kernels(self, dev, peaks, n=400):
+        """Average launch duration of each kernel: n back-to-back launches
+        (graph replay, rotating buffers) timed by CUDA events on the stream."""
+        R = self.n_rot
+        fns = {
+            "full_me_u8": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.R,
+                                                      out=self.d_mv[i % R]),
+            "iimg_u8_i32": lambda i: self.U.iimg_u8_i32(self.d_cur[i % R], out=self.d_ii[i % R], workspace=self.ws),
+        }
+        out = {name: time_launches(fn, R, n) for name, fn in fns.items()}
         absdiff = self.nblk * (2 * self.R + 1) ** 2 * self.B * self.B
         iimg_bytes = 5 * self.H * self.W
         return out, absdiff, iimg_bytes
@@ -298,19 +292,8 @@ class Filter3x3:
     def check(self):
         return None
 
-    def kernels(self, dev, peaks, n=500):
-        import torch
-        st = torch.cuda.current_stream()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
-        for k in range(3):
-            self.step(k)
-        torch.cuda.synchronize()
-        for i in range(n):
-            ev[i][0].record(st)
-            self.step(i)
-            ev[i][1].record(st)
-        torch.cuda.synchronize()
-        return {"filter3x3_f32": sum(a.elapsed_time(b) for a, b in ev) / n}, None, 8 * self.H * self.W
+    def kernels(self, dev, peaks, n=2000):
+        return {"filter3x3_f32": time_launches(self.step, self.n_rot, n)}, None, 8 * self.H * self.W
 
     def cpu_setup(self):
         import oracle
@@ -322,6 +305,22 @@ class Filter3x3:
 
 
 WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3}
+
+
+def time_launches(fn, period: int, n: int) -> float:
+    """ms per launch of fn over n launches replayed from CUDA graphs."""
+    import torch
+    g = StepGraphs(fn, period)
+    g.prepare(n)
+    g.run(period)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    g.run(n)
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / n
 
 
 # --------------------------------------------------------------------- arms
@@ -349,6 +348,52 @@ def probe_sad4_peak(dev):
     return best
 
 
+class StepGraphs:
+    """The steps of a workload captured in CUDA graphs (through the same C-ABI
+    calls a user makes), so that the timed loop measures the GPU and not the
+    Python launch path.  `run(k)` replays exactly k steps."""
+
+    def __init__(self, fn, period: int):
+        import torch
+        self.period = period
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for i in range(3):
+                fn(i)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        self.graphs = {}
+        self.fn = fn
+
+    def graph(self, n: int):
+        import torch
+        if n not in self.graphs:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                for i in range(n):
+                    self.fn(i)
+            self.graphs[n] = g
+        return self.graphs[n]
+
+    def run(self, k: int):
+        full, rest = divmod(k, self.period)
+        if full:
+            g = self.graph(self.period)
+            for _ in range(full):
+                g.replay()
+        if rest:
+            self.graph(rest).replay()
+
+    def prepare(self, k: int):
+        """Capture every graph run(k) needs (capture outside the timed region)."""
+        full, rest = divmod(k, self.period)
+        if full:
+            self.graph(self.period)
+        if rest:
+            self.graph(rest)
+
+
 def run_ours(args, wl, dist):
     import torch
     import umi_gb300 as U
@@ -358,8 +403,10 @@ def run_ours(args, wl, dist):
     pk = peaks()
     wl.setup(dev)
     st = torch.cuda.current_stream()
-    for i in range(args.warmup):
-        wl.step(i)
+    steps = StepGraphs(wl.step, wl.n_rot)
+    steps.prepare(args.steps)
+    steps.prepare(args.warmup)
+    steps.run(args.warmup)
     torch.cuda.synchronize()
     clocks = Clocks(dist.local)
     clocks.start()
@@ -367,8 +414,7 @@ def run_ours(args, wl, dist):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    for i in range(args.steps):
-        wl.step(i)
+    steps.run(args.steps)
     e1.record(st)
     torch.cuda.synchronize()
     dist.barrier()
@@ -440,7 +486,7 @@ def cpu_baseline(wl, sample_s=10.0):
         chunk, what = 128, "rows of the 1024x1024 image, 3x3 weighted sum in FP64"
     units, t0 = 0.0, time.perf_counter()
     n = 0
-    while time.perf_counter() - t0 < sample_s and n < 64:
+    while time.perf_counter() - t0 < sample_s and n < 4096:
         units += wl.cpu_step(chunk, threads)
         n += 1
     dt = time.perf_counter() - t0

@@ -28,52 +28,64 @@ struct FilterGeom {
 	int vec;  // in/out 16-byte aligned and w % 4 == 0
 };
 
-// Loads row y, columns x-1 .. x+4 for this lane into r[0..5].
-__device__ __forceinline__ void load_row(const float* __restrict__ in, const FilterGeom& g, int y, int x0, int lane,
-                                         float r[6]) {
+// Row y, columns x .. x+3 of this lane, plus the strip-edge neighbour (x0-1
+// for lane 0, x0+TWC for lane 31) in `edge`.
+__device__ __forceinline__ float4 load_row(const float* __restrict__ in, const FilterGeom& g, int y, int x0, int lane,
+                                           float& edge) {
 	const int x = x0 + 4 * lane;
-	float4 v;
-	if (y < 0 || y >= g.h) {
-		v = make_float4(g.pad, g.pad, g.pad, g.pad);
-	} else {
+	float4 v = make_float4(g.pad, g.pad, g.pad, g.pad);
+	edge = g.pad;
+	if (y >= 0 && y < g.h) {
 		const float* row = in + (size_t)y * g.w;
 		if (g.vec && x + 3 < g.w) {
 			v = __ldg(reinterpret_cast<const float4*>(row + x));
 		} else {
-			v.x = x + 0 < g.w ? __ldg(row + x + 0) : g.pad;
-			v.y = x + 1 < g.w ? __ldg(row + x + 1) : g.pad;
-			v.z = x + 2 < g.w ? __ldg(row + x + 2) : g.pad;
-			v.w = x + 3 < g.w ? __ldg(row + x + 3) : g.pad;
+			if (x + 0 < g.w) v.x = __ldg(row + x + 0);
+			if (x + 1 < g.w) v.y = __ldg(row + x + 1);
+			if (x + 2 < g.w) v.z = __ldg(row + x + 2);
+			if (x + 3 < g.w) v.w = __ldg(row + x + 3);
 		}
+		const int xe = lane == 0 ? x0 - 1 : x0 + TWC;
+		if ((lane == 0 || lane == 31) && xe >= 0 && xe < g.w) edge = __ldg(row + xe);
 	}
+	return v;
+}
+
+// Columns x-1 .. x+4 of a loaded row: neighbours come from the adjacent lanes.
+__device__ __forceinline__ void spread(float4 v, float edge, int lane, float r[6]) {
 	float left = __shfl_up_sync(0xffffffffu, v.w, 1);
 	float right = __shfl_down_sync(0xffffffffu, v.x, 1);
-	if (lane == 0) {
-		const int xl = x0 - 1;
-		left = (y < 0 || y >= g.h || xl < 0) ? g.pad : __ldg(in + (size_t)y * g.w + xl);
-	}
-	if (lane == 31) {
-		const int xr = x0 + TWC;
-		right = (y < 0 || y >= g.h || xr >= g.w) ? g.pad : __ldg(in + (size_t)y * g.w + xr);
-	}
+	if (lane == 0) left = edge;
+	if (lane == 31) right = edge;
 	r[0] = left; r[1] = v.x; r[2] = v.y; r[3] = v.z; r[4] = v.w; r[5] = right;
 }
 
 __global__ void __launch_bounds__(WARPS * 32) filter3x3_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                                    const FilterGeom g, const Weights9 wt) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+	// Programmatic dependent launch: let the next launch in the stream start
+	// its CTAs early, and wait for the previous one before touching memory.
+	asm volatile("griddepcontrol.launch_dependents;");
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int x0 = blockIdx.x * TWC;
 	const int y0 = (blockIdx.y * WARPS + warp) * RY;
 	if (y0 >= g.h) return;  // whole warp leaves together
+	// Issue all RY + 2 row loads before any use.
+	float4 raw[RY + 2];
+	float edge[RY + 2];
+#pragma unroll
+	for (int i = 0; i < RY + 2; ++i) raw[i] = load_row(in, g, y0 - 1 + i, x0, lane, edge[i]);
 	float r0[6], r1[6], r2[6];
-	load_row(in, g, y0 - 1, x0, lane, r0);
-	load_row(in, g, y0, x0, lane, r1);
+	spread(raw[0], edge[0], lane, r0);
+	spread(raw[1], edge[1], lane, r1);
 	const int x = x0 + 4 * lane;
 #pragma unroll
 	for (int i = 0; i < RY; ++i) {
 		const int y = y0 + i;
 		if (y >= g.h) break;
-		load_row(in, g, y + 1, x0, lane, r2);
+		spread(raw[i + 2], edge[i + 2], lane, r2);
 		float o[4];
 #pragma unroll
 		for (int k = 0; k < 4; ++k) {
@@ -107,8 +119,15 @@ extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, 
 	FilterGeom g{h, w, pad, umi::aligned(in, 16) && umi::aligned(out, 16) && (w % 4) == 0};
 	Weights9 wt;
 	for (int i = 0; i < 9; ++i) wt.w[i] = w9[i];
-	const dim3 grid(umi::ceil_div(w, TWC), umi::ceil_div(h, WARPS * RY));
-	filter3x3_f32_kernel<<<grid, WARPS * 32, 0, umi::as_stream(stream)>>>(in, out, g, wt);
-	UMI_TRY(umi::launch_status("filter3x3_f32_kernel"));
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(umi::ceil_div(w, TWC), umi::ceil_div(h, WARPS * RY));
+	cfg.blockDim = dim3(WARPS * 32);
+	cfg.stream = umi::as_stream(stream);
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_f32_kernel, in, out, g, wt), "filter3x3_f32_kernel"));
 	return umi::ok();
 }

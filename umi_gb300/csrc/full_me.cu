@@ -11,10 +11,11 @@
 //    memory, in four copies shifted by 0..3 bytes so that any horizontal
 //    displacement reads whole aligned 32-bit words;
 //  * a thread owns one horizontal displacement ix and G consecutive vertical
-//    displacements; the b x b current block lives in registers (b*b/4 words),
-//    window rows stream through registers once, and each (window row, block
-//    row) pair costs b/4 `vabsdiff4 ... .add` instructions (4 byte
-//    |a-b| plus accumulate in one instruction);
+//    displacements; it keeps a ring of G window rows in registers and streams
+//    the current block's rows through one broadcast 128-bit shared load each
+//    (5G+4 live words), so two CTAs fit an SM; every (block row, window row)
+//    pair costs b/4 `vabsdiff4 ... .add` instructions (4 byte |a-b| plus
+//    accumulate in one instruction, the native packed-SAD path);
 //  * the argmin is fused: key = (sad << 15) | raster index of (dy, dx), a
 //    shared-memory atomicMin per macroblock gives the minimum SAD with the
 //    first displacement in raster order (the reference's output order
@@ -45,18 +46,32 @@ struct MeGeom {
 	int m;            // macroblocks per CTA
 	int tasks_per_mb; // ndx * ng
 	int vec_ok;       // ref is 4-byte aligned and w % 4 == 0: word loads allowed
+	int nx32;         // largest multiple of 32 <= ndx: displacements served by whole warps
 };
 
+// Register budget per instantiation: the benchmark shape (b = 16, G = 13,
+// 352 threads) is held to 80 registers so that two CTAs (6 warps per SM
+// sub-partition x 80 x 32 <= 16K registers) fit an SM.
+// The other shapes get a budget of about 5G + 30 (ring + accumulators + addressing).
+template <int B, int G> struct MeRegs { static constexpr int value = B == 16 ? (5 * G + 31) / 8 * 8 + 8 : 64; };
+template <> struct MeRegs<16, 13> { static constexpr int value = 80; };
+
 template <int B, int G, bool VOLUME>
-__global__ void __launch_bounds__(512) full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
-                                                      const int32_t* __restrict__ centers, int32_t* __restrict__ out,
-                                                      const MeGeom g) {
+__global__ void __launch_bounds__(512) __maxnreg__((MeRegs<B, G>::value))
+full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref, const int32_t* __restrict__ centers,
+               int32_t* __restrict__ out, const MeGeom g) {
 	extern __shared__ __align__(16) uint32_t smem[];
 	constexpr int BW = B / 4;  // words per block row
 	__shared__ uint32_t best[64];
 	const int tid = threadIdx.x;
 	const int mb0 = blockIdx.x * g.m;
 
+	// Staging walks (row, word) pairs: a thread starts at word t % win_words of
+	// row t / win_words and advances by whole rows (one division per thread).
+	const int rstep = blockDim.x / g.win_words;  // host guarantees blockDim >= win_words
+	const int wd0 = tid - (tid / g.win_words) * g.win_words;
+	const int row0 = tid / g.win_words;
+	const bool stager = row0 < rstep;  // threads past rstep*win_words idle while staging
 	// 1. Stage windows (copy 0) and current blocks.
 	for (int m = 0; m < g.m; ++m) {
 		const int blk = mb0 + m;
@@ -65,44 +80,49 @@ __global__ void __launch_bounds__(512) full_me_kernel(const uint8_t* __restrict_
 		const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
 		const int gy0 = by * B + cy - g.r, gx0 = bx * B + cx - g.r;
 		uint32_t* win = smem + m * g.mb_stride;
-		const int nwords = g.win_rows * g.win_words;
-		for (int i = tid; i < nwords; i += blockDim.x) {
-			const int row = i / g.win_words, wd = i - row * g.win_words;
-			const int gy = min(max(gy0 + row, 0), g.h - 1);
-			const uint8_t* src = ref + (size_t)gy * g.w;
-			const int gx = gx0 + 4 * wd;
-			uint32_t v;
-			if (g.vec_ok && gx >= 0 && gx + 3 < g.w && (gx & 3) == 0) {
-				v = __ldg(reinterpret_cast<const uint32_t*>(src + gx));
-			} else {
-				v = 0;
+		const int gx = gx0 + 4 * wd0;
+		const bool vec = g.vec_ok && gx >= 0 && gx + 3 < g.w && (gx & 3) == 0;
+		int xs[4];
 #pragma unroll
-				for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + min(max(gx + k, 0), g.w - 1)) << (8 * k);
+		for (int k = 0; k < 4; ++k) xs[k] = min(max(gx + k, 0), g.w - 1);
+		if (stager) {
+			for (int row = row0; row < g.win_rows; row += rstep) {
+				const int gy = min(max(gy0 + row, 0), g.h - 1);
+				const uint8_t* src = ref + (size_t)gy * g.w;
+				uint32_t v;
+				if (vec) {
+					v = __ldg(reinterpret_cast<const uint32_t*>(src + gx));
+				} else {
+					v = 0;
+#pragma unroll
+					for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + xs[k]) << (8 * k);
+				}
+				win[row * g.win_words + wd0] = v;
 			}
-			win[row * g.win_words + wd] = v;
 		}
 		uint32_t* cb = win + 4 * g.copy_stride;
-		for (int i = tid; i < B * BW; i += blockDim.x) {
-			const int row = i / BW, wd = i - row * BW;
+		if (tid < B * BW) {
+			const int row = tid / BW, wd = tid - row * BW;
 			const uint8_t* src = cur + (size_t)(by * B + row) * g.w + bx * B + 4 * wd;
 			uint32_t v = 0;
 #pragma unroll
 			for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + k) << (8 * k);
-			cb[i] = v;
+			cb[tid] = v;
 		}
 		if (tid == 0) best[m] = 0xffffffffu;
 	}
 	__syncthreads();
 	// 2. Shifted copies s = 1..3: word k holds bytes [4k+s, 4k+s+4) of the row.
 	for (int m = 0; m < g.m; ++m) {
-		if (mb0 + m >= g.nblk) break;
+		if (mb0 + m >= g.nblk || !stager) break;
 		uint32_t* win = smem + m * g.mb_stride;
-		const int nwords = g.win_rows * g.win_words;
-		for (int i = tid; i < 3 * nwords; i += blockDim.x) {
-			const int s = 1 + i / nwords, j = i - (s - 1) * nwords;
-			const int wd = j % g.win_words;
-			const uint32_t lo = win[j], hi = (wd + 1 < g.win_words) ? win[j + 1] : 0u;
-			win[s * g.copy_stride + j] = __funnelshift_r(lo, hi, 8 * s);
+		const bool last = wd0 + 1 == g.win_words;
+		for (int row = row0; row < g.win_rows; row += rstep) {
+			const int j = row * g.win_words + wd0;
+			const uint32_t lo = win[j], hi = last ? 0u : win[j + 1];
+			win[g.copy_stride + j] = __funnelshift_r(lo, hi, 8);
+			win[2 * g.copy_stride + j] = __funnelshift_r(lo, hi, 16);
+			win[3 * g.copy_stride + j] = __funnelshift_r(lo, hi, 24);
 		}
 	}
 	__syncthreads();
@@ -112,33 +132,54 @@ __global__ void __launch_bounds__(512) full_me_kernel(const uint8_t* __restrict_
 	for (int t = tid; t < total; t += blockDim.x) {
 		const int m = t / g.tasks_per_mb;
 		const int rem = t - m * g.tasks_per_mb;
-		const int grp = rem / g.ndx, ix = rem - grp * g.ndx;
+		// Tasks [0, ng*nx32) cover ix < nx32 with whole warps per group (one
+		// row per warp-wide load: conflict-free); the remaining columns of all
+		// groups follow.
+		int grp, ix;
+		const int main_tasks = g.ng * g.nx32;
+		if (rem < main_tasks) {
+			grp = rem / g.nx32;
+			ix = rem - grp * g.nx32;
+		} else {
+			const int rw = g.ndx - g.nx32, r2 = rem - main_tasks;
+			grp = r2 / rw;
+			ix = g.nx32 + (r2 - grp * rw);
+		}
 		const int blk = mb0 + m;
 		if (blk >= g.nblk) continue;
 		const uint32_t* win = smem + m * g.mb_stride;
 		const uint32_t* cb = win + 4 * g.copy_stride;
-		uint32_t cv[B][BW];
-#pragma unroll
-		for (int py = 0; py < B; ++py)
-#pragma unroll
-			for (int k = 0; k < BW; ++k) cv[py][k] = cb[py * BW + k];
 		const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + grp * G * g.win_words;
+		// ring[s] holds window row r with r % G == s; at block row py the G
+		// candidates q = 0..G-1 need window rows py .. py+G-1.
+		uint32_t ring[G][BW];
 		uint32_t acc[G];
 #pragma unroll
-		for (int q = 0; q < G; ++q) acc[q] = 0;
+		for (int q = 0; q < G; ++q) {
+			acc[q] = 0;
 #pragma unroll
-		for (int j = 0; j < G + B - 1; ++j) {
-			uint32_t wv[BW];
+			for (int k = 0; k < BW; ++k) ring[q][k] = wp[q * g.win_words + k];
+		}
 #pragma unroll
-			for (int k = 0; k < BW; ++k) wv[k] = wp[j * g.win_words + k];
+		for (int py = 0; py < B; ++py) {
+			uint32_t cv[BW];
+			if (BW == 4) {
+				const uint4 c4 = *reinterpret_cast<const uint4*>(cb + py * BW);  // same address in every lane
+				cv[0] = c4.x; cv[1] = c4.y; cv[2 % BW] = c4.z; cv[3 % BW] = c4.w;
+			} else {
 #pragma unroll
-			for (int q = 0; q < G; ++q) {
-				const int py = j - q;
-				if (py >= 0 && py < B) {
-#pragma unroll
-					for (int k = 0; k < BW; ++k) acc[q] = sad4_acc(cv[py][k], wv[k], acc[q]);
-				}
+				for (int k = 0; k < BW; ++k) cv[k] = cb[py * BW + k];
 			}
+			if (py > 0) {
+				const int r = py + G - 1;
+#pragma unroll
+				for (int k = 0; k < BW; ++k) ring[r % G][k] = wp[r * g.win_words + k];
+			}
+			// k outer, q inner: consecutive instructions update different accumulators.
+#pragma unroll
+			for (int k = 0; k < BW; ++k)
+#pragma unroll
+				for (int q = 0; q < G; ++q) acc[q] = sad4_acc(cv[k], ring[(py + q) % G][k], acc[q]);
 		}
 		const int iy0 = grp * G;
 		if (VOLUME) {
@@ -188,6 +229,10 @@ umi_status launch_g(const uint8_t* cur, const uint8_t* ref, const int32_t* cente
 	auto kern = full_me_kernel<B, G, V>;
 	if (smem > 48 * 1024) UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                                                                 (int)smem), "cudaFuncSetAttribute"));
+	// Without this the driver may pick a small shared-memory carveout and
+	// allow only one CTA per SM.
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+	                                              (int)cudaSharedmemCarveoutMaxShared), "cudaFuncSetAttribute"));
 	const int grid = (g.nblk + g.m - 1) / g.m;
 	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
 	return umi::launch_status("full_me_kernel");
@@ -225,6 +270,7 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.mb_stride = 4 * g.copy_stride + b * b / 4 + 4;
 	g.mb_stride = (g.mb_stride + 3) & ~3;         // keep each current block 16-byte aligned
 	g.tasks_per_mb = g.ndx * g.ng;
+	g.nx32 = (g.ndx / 32) * 32;
 	g.vec_ok = umi::aligned(ref, 4) && (w % 4) == 0;
 	// Macroblocks per CTA: enough tasks to fill at least ~256 threads, within
 	// 96 KB of shared memory and the 64-slot argmin table.
@@ -238,6 +284,9 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 		const int iters = (total + 511) / 512;
 		threads = (((total + iters - 1) / iters) + 31) / 32 * 32;
 	}
+	// Staging needs one thread per current-block word (b*b/4 <= 64) and per
+	// window word of a row (<= 37).
+	threads = std::max(threads, 64);
 	const size_t smem = (size_t)m * g.mb_stride * 4;
 	const cudaStream_t st = umi::as_stream(stream);
 	umi_status rc;

@@ -4,46 +4,72 @@
 // scan along x written transposed, applied twice) with one read of the uint8
 // frame from HBM and one write of the int32 result.
 //
-// The frame is cut into TH x TW tiles.  With the inclusive integral image
-// ii[y][x] and a tile at (Y0, X0):
+// The frame is cut into TH x TW tiles (64 x 256: a 1080p frame is 136 tiles,
+// about one per SM).  With the inclusive integral image ii and a tile at
+// (Y0, X0):
 //   ii[y][x] = corner + sum_{X0<=x'<=x} top[x'] + sum_{Y0<=y'<=y} left[y'] + local[y][x]
 //   top[x]   = sum over all rows above the tile of column x,
 //   left[y]  = sum over all columns left of the tile of row y,
 //   corner   = sum over the whole rectangle above-left of the tile,
 //   local    = the 2-D prefix inside the tile.
 // Kernel 1 (iimg_tile_sums) writes per-tile row sums, column sums and tile
-// totals to a small workspace (about 4% of the output).  Kernel 2
+// totals to a small workspace (about 3% of the output).  Kernel 2
 // (iimg_tiles) loads its tile and computes the local prefix with warp-shuffle
-// scans, then waits on kernel 1 (programmatic dependent launch: the wait is
+// scans, then waits for kernel 1 (programmatic dependent launch: the wait is
 // griddepcontrol.wait, so everything before it overlaps kernel 1), adds the
-// carries from the workspace and writes the tile with 16-byte stores.
+// carries (at most nty + ntx + nty*ntx small-array reads per tile, issued as
+// independent loads) and writes the tile with 16-byte stores.
 #include "common.h"
 
 namespace {
 
-constexpr int TH = 32;   // tile rows: 8 warps x 4 rows
-constexpr int TW = 128;  // tile columns: 32 lanes x 4 columns
-constexpr int RPW = 4;   // rows per warp
-constexpr int NT = 256;
+constexpr int NT = 256;         // threads: 8 warps
+constexpr int NW = NT / 32;
+constexpr int RPW = 8;          // rows per warp
+constexpr int TH = NW * RPW;    // 64 tile rows
+constexpr int CPL = 8;          // columns per lane
+constexpr int TW = 32 * CPL;    // 256 tile columns
+constexpr int MAXNTY = 64;      // carries unrolled up to this many tile rows (frames up to 4096 rows)
 
 struct IimgGeom {
 	int h, w, ntx, nty;
-	int vec_in;   // in is 4-byte aligned and w % 4 == 0
+	int vec_in;   // in is 8-byte aligned and w % 8 == 0
 	int vec_out;  // out is 16-byte aligned and w % 4 == 0
 	int32_t* rowsum;   // [h][ntx]
 	int32_t* colsum;   // [nty][w]
 	int32_t* tilesum;  // [nty][ntx]
 };
 
-// Four consecutive pixels of row y starting at column x (zeros past the edge).
-__device__ __forceinline__ void load4(const uint8_t* __restrict__ in, const IimgGeom& g, int y, int x, uint32_t v[4]) {
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void pdl_trigger() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+	asm volatile("griddepcontrol.launch_dependents;");
+#endif
+}
+
+// The lane's 8 pixels of row y starting at column x, zeros past the edges.
+__device__ __forceinline__ uint2 load8(const uint8_t* __restrict__ in, const IimgGeom& g, int y, int x) {
+	if (y >= g.h) return make_uint2(0, 0);
 	const uint8_t* row = in + (size_t)y * g.w;
-	if (g.vec_in && x + 3 < g.w) {
-		const uint32_t p = __ldg(reinterpret_cast<const uint32_t*>(row + x));
-		v[0] = p & 0xff; v[1] = (p >> 8) & 0xff; v[2] = (p >> 16) & 0xff; v[3] = p >> 24;
-	} else {
+	if (g.vec_in && x + 7 < g.w) return __ldg(reinterpret_cast<const uint2*>(row + x));
+	uint32_t lo = 0, hi = 0;
 #pragma unroll
-		for (int k = 0; k < 4; ++k) v[k] = (x + k < g.w) ? __ldg(row + x + k) : 0u;
+	for (int k = 0; k < 4; ++k) {
+		if (x + k < g.w) lo |= (uint32_t)__ldg(row + x + k) << (8 * k);
+		if (x + 4 + k < g.w) hi |= (uint32_t)__ldg(row + x + 4 + k) << (8 * k);
+	}
+	return make_uint2(lo, hi);
+}
+
+__device__ __forceinline__ void unpack8(uint2 p, uint32_t v[8]) {
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		v[k] = (p.x >> (8 * k)) & 0xffu;
+		v[4 + k] = (p.y >> (8 * k)) & 0xffu;
 	}
 }
 
@@ -57,104 +83,118 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
 }
 
 __global__ void __launch_bounds__(NT) iimg_tile_sums(const uint8_t* __restrict__ in, const IimgGeom g) {
-	__shared__ uint32_t colpart[NT / 32][TW];
-	__shared__ uint32_t warptot[TW / 32];
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-	// Let the dependent tile kernel get scheduled as soon as SMs free up; it
-	// waits for this grid's results with griddepcontrol.wait.
-	asm volatile("griddepcontrol.launch_dependents;");
-#endif
+	__shared__ uint32_t colpart[NW][TW];
+	__shared__ uint32_t warptot[NW];
+	pdl_wait();  // when launched after an earlier kernel that may write `in`
+	pdl_trigger();
 	const int tx = blockIdx.x, ty = blockIdx.y;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int X0 = tx * TW, Y0 = ty * TH;
-	uint32_t col[4] = {0, 0, 0, 0};
+	const int y0 = Y0 + warp * RPW, x = X0 + CPL * lane;
+	uint2 raw[RPW];
+#pragma unroll
+	for (int r = 0; r < RPW; ++r) raw[r] = load8(in, g, y0 + r, x);
+	uint32_t col[CPL] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
 	for (int r = 0; r < RPW; ++r) {
-		const int y = Y0 + warp * RPW + r;
-		uint32_t v[4] = {0, 0, 0, 0};
-		if (y < g.h) load4(in, g, y, X0 + 4 * lane, v);
-		uint32_t s = v[0] + v[1] + v[2] + v[3];
-		s = __reduce_add_sync(0xffffffffu, s);
-		if (lane == 0 && y < g.h) g.rowsum[(size_t)y * g.ntx + tx] = (int32_t)s;
-#pragma unroll
-		for (int k = 0; k < 4; ++k) col[k] += v[k];
-	}
-#pragma unroll
-	for (int k = 0; k < 4; ++k) colpart[warp][4 * lane + k] = col[k];
-	__syncthreads();
-	if (threadIdx.x < TW) {
+		uint32_t v[CPL];
+		unpack8(raw[r], v);
 		uint32_t s = 0;
 #pragma unroll
-		for (int i = 0; i < NT / 32; ++i) s += colpart[i][threadIdx.x];
-		const int x = X0 + threadIdx.x;
-		if (x < g.w) g.colsum[(size_t)ty * g.w + x] = (int32_t)s;
+		for (int k = 0; k < CPL; ++k) { s += v[k]; col[k] += v[k]; }
 		s = __reduce_add_sync(0xffffffffu, s);
-		if ((threadIdx.x & 31) == 0) warptot[threadIdx.x >> 5] = s;
+		if (lane == 0 && y0 + r < g.h) g.rowsum[(size_t)(y0 + r) * g.ntx + tx] = (int32_t)s;
+	}
+#pragma unroll
+	for (int k = 0; k < CPL; ++k) colpart[warp][CPL * lane + k] = col[k];
+	__syncthreads();
+	{
+		const int c = threadIdx.x;  // NT == TW: one column per thread
+		uint32_t s = 0;
+#pragma unroll
+		for (int i = 0; i < NW; ++i) s += colpart[i][c];
+		if (X0 + c < g.w) g.colsum[(size_t)ty * g.w + X0 + c] = (int32_t)s;
+		s = __reduce_add_sync(0xffffffffu, s);
+		if (lane == 0) warptot[warp] = s;
 	}
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		const uint32_t t = warptot[0] + warptot[1] + warptot[2] + warptot[3];
+		uint32_t t = 0;
+#pragma unroll
+		for (int i = 0; i < NW; ++i) t += warptot[i];
 		g.tilesum[(size_t)ty * g.ntx + tx] = (int32_t)t;
 	}
 }
 
 __global__ void __launch_bounds__(NT) iimg_tiles(const uint8_t* __restrict__ in, int32_t* __restrict__ out,
                                                  const IimgGeom g) {
-	__shared__ uint32_t wtot[NT / 32][TW];  // per-warp column totals, then their exclusive prefix
-	__shared__ uint32_t topx[TW];           // inclusive x-prefix of the top carries
-	__shared__ uint32_t lefty[TH];          // inclusive y-prefix of the left carries
-	__shared__ uint32_t cornerp[NT / 32];
+	__shared__ uint32_t wtot[NW][TW];  // per-warp column totals, then their exclusive prefix over warps
+	__shared__ uint32_t topw[NW];      // per-warp totals of the top-carry x-scan
+	__shared__ uint32_t lefty[TH];     // inclusive y-prefix of the left carries
+	__shared__ uint32_t cornerp[NW];
 	const int tx = blockIdx.x, ty = blockIdx.y;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int X0 = tx * TW, Y0 = ty * TH;
+	const int y0 = Y0 + warp * RPW, x = X0 + CPL * lane;
 
-	// Local 2-D prefix (needs only the input: runs before the dependency wait).
-	uint32_t loc[RPW][4];
-	uint32_t col[4] = {0, 0, 0, 0};
+	// Local 2-D prefix.  The input is not written by kernel 1, so it is read
+	// before the dependency wait and overlaps kernel 1.
+	uint2 raw[RPW];
+#pragma unroll
+	for (int r = 0; r < RPW; ++r) raw[r] = load8(in, g, y0 + r, x);
+	uint32_t loc[RPW][CPL];
+	uint32_t col[CPL] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
 	for (int r = 0; r < RPW; ++r) {
-		const int y = Y0 + warp * RPW + r;
-		uint32_t v[4] = {0, 0, 0, 0};
-		if (y < g.h) load4(in, g, y, X0 + 4 * lane, v);
-		v[1] += v[0]; v[2] += v[1]; v[3] += v[2];
-		const uint32_t excl = warp_incl_scan(v[3], lane) - v[3];
+		uint32_t v[CPL];
+		unpack8(raw[r], v);
 #pragma unroll
-		for (int k = 0; k < 4; ++k) {
+		for (int k = 1; k < CPL; ++k) v[k] += v[k - 1];
+		const uint32_t excl = warp_incl_scan(v[CPL - 1], lane) - v[CPL - 1];
+#pragma unroll
+		for (int k = 0; k < CPL; ++k) {
 			col[k] += v[k] + excl;
 			loc[r][k] = col[k];
 		}
 	}
 #pragma unroll
-	for (int k = 0; k < 4; ++k) wtot[warp][4 * lane + k] = col[k];
+	for (int k = 0; k < CPL; ++k) wtot[warp][CPL * lane + k] = col[k];
 	__syncthreads();
-	if (threadIdx.x < TW) {
+	{
+		const int c = threadIdx.x;
 		uint32_t run = 0;
 #pragma unroll
-		for (int i = 0; i < NT / 32; ++i) {
-			const uint32_t t = wtot[i][threadIdx.x];
-			wtot[i][threadIdx.x] = run;
+		for (int i = 0; i < NW; ++i) {
+			const uint32_t t = wtot[i][c];
+			wtot[i][c] = run;
 			run += t;
 		}
 	}
 
 	// Carries from kernel 1.
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-	asm volatile("griddepcontrol.wait;" ::: "memory");
-#endif
-	if (threadIdx.x < TW) {
-		const int x = X0 + threadIdx.x;
+	pdl_wait();
+	pdl_trigger();
+	uint32_t topc;  // inclusive x-prefix (within this warp's 32 columns) of the top carries
+	{
+		const int c = threadIdx.x, xc = X0 + c;
 		uint32_t s = 0;
-		if (x < g.w)
-			for (int t = 0; t < ty; ++t) s += (uint32_t)__ldcg(g.colsum + (size_t)t * g.w + x);
-		s = warp_incl_scan(s, lane);
-		topx[threadIdx.x] = s;
-	} else if (threadIdx.x < TW + TH) {
-		const int r = threadIdx.x - TW;
-		const int y = Y0 + r;
+		if (xc < g.w) {
+#pragma unroll
+			for (int t = 0; t < MAXNTY; ++t)
+				if (t < ty) s += (uint32_t)__ldcg(g.colsum + (size_t)t * g.w + xc);
+		}
+		topc = warp_incl_scan(s, lane);
+		if (lane == 31) topw[warp] = topc;
+	}
+	if (threadIdx.x < TH) {
+		const int y = Y0 + threadIdx.x;
 		uint32_t s = 0;
-		if (y < g.h)
+		if (y < g.h) {
+#pragma unroll 8
 			for (int t = 0; t < tx; ++t) s += (uint32_t)__ldcg(g.rowsum + (size_t)y * g.ntx + t);
-		lefty[r] = warp_incl_scan(s, lane);
+		}
+		// rows are spread over warps 0 and 1: scan within each, stitch below
+		lefty[threadIdx.x] = warp_incl_scan(s, lane);
 	}
 	{
 		uint32_t s = 0;
@@ -167,33 +207,41 @@ __global__ void __launch_bounds__(NT) iimg_tiles(const uint8_t* __restrict__ in,
 		if (lane == 0) cornerp[warp] = s;
 	}
 	__syncthreads();
-	// Stitch the four warps' x-prefix pieces of topx (each warp scanned 32 columns).
 	uint32_t corner = 0;
 #pragma unroll
-	for (int i = 0; i < NT / 32; ++i) corner += cornerp[i];
-	uint32_t topv[4];
+	for (int i = 0; i < NW; ++i) corner += cornerp[i];
+	// Top carry prefix for this lane's 8 columns: the warp-level scans of
+	// columns [32*wv, 32*wv+32) are in topc of warp wv; columns of this lane
+	// are CPL*lane .. CPL*lane+7, owned by warp (CPL*lane)/32.
+	__shared__ uint32_t topx[TW];
+	topx[threadIdx.x] = topc;
+	__syncthreads();
+	uint32_t topv[CPL];
 #pragma unroll
-	for (int k = 0; k < 4; ++k) {
-		const int c = 4 * lane + k;
+	for (int k = 0; k < CPL; ++k) {
+		const int c = CPL * lane + k;
 		uint32_t t = topx[c];
-		for (int seg = 0; seg < (c >> 5); ++seg) t += topx[seg * 32 + 31];
+		const int seg = c >> 5;
+		for (int sgi = 0; sgi < seg; ++sgi) t += topw[sgi];
 		topv[k] = t + corner + wtot[warp][c];
 	}
+	uint32_t lbase = 0;
+	if (warp * RPW >= 32) lbase = lefty[31];  // rows 32..63: add the total of rows 0..31
 #pragma unroll
 	for (int r = 0; r < RPW; ++r) {
-		const int y = Y0 + warp * RPW + r;
+		const int y = y0 + r;
 		if (y >= g.h) break;
-		const uint32_t lv = lefty[warp * RPW + r];
-		int32_t o[4];
+		const uint32_t lv = lefty[warp * RPW + r] + lbase;
+		int32_t o[CPL];
 #pragma unroll
-		for (int k = 0; k < 4; ++k) o[k] = (int32_t)(loc[r][k] + topv[k] + lv);
-		const int x = X0 + 4 * lane;
+		for (int k = 0; k < CPL; ++k) o[k] = (int32_t)(loc[r][k] + topv[k] + lv);
 		int32_t* dst = out + (size_t)y * g.w + x;
-		if (g.vec_out && x + 3 < g.w) {
-			*reinterpret_cast<int4*>(dst) = make_int4(o[0], o[1], o[2], o[3]);
+		if (g.vec_out && x + 7 < g.w) {
+			reinterpret_cast<int4*>(dst)[0] = make_int4(o[0], o[1], o[2], o[3]);
+			reinterpret_cast<int4*>(dst)[1] = make_int4(o[4], o[5], o[6], o[7]);
 		} else {
 #pragma unroll
-			for (int k = 0; k < 4; ++k)
+			for (int k = 0; k < CPL; ++k)
 				if (x + k < g.w) dst[k] = o[k];
 		}
 	}
@@ -203,6 +251,13 @@ size_t ws_bytes(int h, int w) {
 	const size_t ntx = umi::ceil_div(w, TW), nty = umi::ceil_div(h, TH);
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
 	return al((size_t)h * ntx * 4) + al(nty * (size_t)w * 4) + al(nty * ntx * 4);
+}
+
+cudaLaunchAttribute pdl_attr() {
+	cudaLaunchAttribute a;
+	a.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	a.val.programmaticStreamSerializationAllowed = 1;
+	return a;
 }
 
 }  // namespace
@@ -220,31 +275,29 @@ extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h
 	if (!umi::aligned(workspace, 16)) return umi::fail(UMI_ERR_INVALID_ARG, "iimg: workspace not 16-byte aligned");
 	if (workspace_bytes < ws_bytes(h, w))
 		return umi::fail(UMI_ERR_NO_MEMORY, "iimg: workspace of %zu bytes, need %zu", workspace_bytes, ws_bytes(h, w));
-	if ((int64_t)h * w > (int64_t)1 << 31) return umi::fail(UMI_ERR_UNSUPPORTED, "iimg: frame larger than 2^31 pixels");
+	if (umi::ceil_div(h, TH) > MAXNTY)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg: %d rows (max %d)", h, MAXNTY * TH);
+	if ((int64_t)h * w > ((int64_t)1 << 31) / 255)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg: %dx%d frame: sums could exceed int32", h, w);
 	IimgGeom g{};
 	g.h = h; g.w = w;
 	g.ntx = umi::ceil_div(w, TW);
 	g.nty = umi::ceil_div(h, TH);
-	g.vec_in = umi::aligned(in, 4) && (w % 4) == 0;
+	g.vec_in = umi::aligned(in, 8) && (w % 8) == 0;
 	g.vec_out = umi::aligned(out, 16) && (w % 4) == 0;
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
 	char* ws = static_cast<char*>(workspace);
 	g.rowsum = reinterpret_cast<int32_t*>(ws);
 	g.colsum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4));
 	g.tilesum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4) + al((size_t)g.nty * w * 4));
-	const cudaStream_t st = umi::as_stream(stream);
-	const dim3 grid(g.ntx, g.nty);
-	iimg_tile_sums<<<grid, NT, 0, st>>>(in, g);
-	UMI_TRY(umi::launch_status("iimg_tile_sums"));
 	cudaLaunchConfig_t cfg{};
-	cfg.gridDim = grid;
+	cfg.gridDim = dim3(g.ntx, g.nty);
 	cfg.blockDim = dim3(NT);
-	cfg.stream = st;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.stream = umi::as_stream(stream);
+	cudaLaunchAttribute attr[1] = {pdl_attr()};
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tile_sums, in, g), "iimg_tile_sums"));
 	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tiles, in, out, g), "iimg_tiles"));
 	return umi::ok();
 }
