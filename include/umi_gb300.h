@@ -142,6 +142,20 @@ size_t umi_iimg_u8_i32_workspace_bytes(int32_t h, int32_t w);
 umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* workspace,
                            size_t workspace_bytes, void* stream);
 
+/* The same integral image for callers that cannot allocate device memory
+ * (no allocator to take a workspace from, or a context where cudaMalloc is
+ * not allowed).  No counterpart in the reference.  The tile sums go to a
+ * scratch array built into the library, UMI_IIMG_NOALLOC_SCRATCH_BYTES
+ * (1 MiB) per GPU, held until the process exits; frames whose workspace
+ * (umi_iimg_u8_i32_workspace_bytes) exceeds it are rejected with
+ * UMI_ERR_NO_MEMORY (3840x2160 and 4096x2160 fit).  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress) with that
+ * device current: make it before any stream capture.  All calls share the
+ * scratch: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Allocates nothing. */
+#define UMI_IIMG_NOALLOC_SCRATCH_BYTES (1u << 20)
+umi_status umi_iimg_u8_i32_noalloc(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* stream);
+
 /* Full-search block motion estimation with fused argmin, uint8 frames.
  * For every b x b block of `cur` (blocks truncated at the frame edge:
  * h/b x w/b, as main/full_me.cu:35), searches displacements (dy, dx) in

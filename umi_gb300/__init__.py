@@ -53,6 +53,7 @@ SIGNATURES = {
     "umi_filter3x3_f32": ([_vp, _vp, _i32, _i32, _vp, _f32, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
     "umi_iimg_u8_i32": ([_vp, _vp, _i32, _i32, _vp, _sz, _vp], ctypes.c_int),
+    "umi_iimg_u8_i32_noalloc": ([_vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
 }

@@ -19,6 +19,8 @@
 // griddepcontrol.wait, so everything before it overlaps kernel 1), adds the
 // carries (at most nty + ntx + nty*ntx small-array reads per tile, issued as
 // independent loads) and writes the tile with 16-byte stores.
+#include <mutex>
+
 #include "common.h"
 
 namespace {
@@ -287,6 +289,89 @@ extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h
 	g.vec_out = umi::aligned(out, 16) && (w % 4) == 0;
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
 	char* ws = static_cast<char*>(workspace);
+	g.rowsum = reinterpret_cast<int32_t*>(ws);
+	g.colsum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4));
+	g.tilesum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4) + al((size_t)g.nty * w * 4));
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(g.ntx, g.nty);
+	cfg.blockDim = dim3(NT);
+	cfg.stream = umi::as_stream(stream);
+	cudaLaunchAttribute attr[1] = {pdl_attr()};
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tile_sums, in, g), "iimg_tile_sums"));
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tiles, in, out, g), "iimg_tiles"));
+	return umi::ok();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free integral image.
+//
+// Some callers of this library cannot allocate device memory at all: a plugin
+// inside a host application that owns the GPU memory budget, code that runs
+// where cudaMalloc is not allowed (a real-time loop with a no-allocation
+// rule, a host callback), or a caller that simply has no allocator to hand a
+// workspace from.  umi_iimg_u8_i32_noalloc serves them: the tile sums go to
+// a scratch array compiled into this library, so the caller passes only the
+// frame and the output.
+//
+// The scratch is a file-scope __device__ array of kNoAllocScratchBytes
+// (1 MiB: enough for frames up to 3840x2160 and 4096x2160); every GPU that
+// loads the library holds it until the process exits.  Host code cannot use
+// the array's name as a device address, so the first call on each device
+// (with that device current) looks the address up with cudaGetSymbolAddress
+// and caches it; make that first call before any stream capture.  All calls
+// share the one array: calls that overlap on the GPU (different streams,
+// different host threads) race on it and must be serialised by the caller.
+// Nothing in the scratch needs to start at zero: kernel 1 writes every entry
+// kernel 2 reads.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
+static_assert(kNoAllocScratchBytes == UMI_IIMG_NOALLOC_SCRATCH_BYTES, "header and library disagree");
+static __device__ __align__(256) unsigned char g_iimg_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+umi_status scratch_address(void** out) {
+	int dev = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	if (dev < 0 || dev >= kMaxDevices) return umi::fail(UMI_ERR_UNSUPPORTED, "iimg_noalloc: device %d", dev);
+	std::lock_guard<std::mutex> lock(g_scratch_mu);
+	if (!g_scratch_addr[dev]) {
+		void* p = nullptr;
+		UMI_TRY(umi::cuda_status(cudaGetSymbolAddress(&p, g_iimg_scratch), "cudaGetSymbolAddress"));
+		g_scratch_addr[dev] = p;
+	}
+	*out = g_scratch_addr[dev];
+	return UMI_OK;
+}
+
+}  // namespace
+
+extern "C" umi_status umi_iimg_u8_i32_noalloc(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* stream) {
+	if (h < 0 || w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "iimg_noalloc: negative size %dx%d", h, w);
+	if (h == 0 || w == 0) return umi::ok();
+	if (!in || !out) return umi::fail(UMI_ERR_INVALID_ARG, "iimg_noalloc: null pointer");
+	if (ws_bytes(h, w) > kNoAllocScratchBytes)
+		return umi::fail(UMI_ERR_NO_MEMORY, "iimg_noalloc: a %dx%d frame needs %zu scratch bytes, the built-in scratch holds %zu",
+		                 h, w, ws_bytes(h, w), kNoAllocScratchBytes);
+	if (umi::ceil_div(h, TH) > MAXNTY)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg_noalloc: %d rows (max %d)", h, MAXNTY * TH);
+	if ((int64_t)h * w > ((int64_t)1 << 31) / 255)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg_noalloc: %dx%d frame: sums could exceed int32", h, w);
+	void* scratch = nullptr;
+	UMI_TRY(scratch_address(&scratch));
+	IimgGeom g{};
+	g.h = h; g.w = w;
+	g.ntx = umi::ceil_div(w, TW);
+	g.nty = umi::ceil_div(h, TH);
+	g.vec_in = umi::aligned(in, 8) && (w % 8) == 0;
+	g.vec_out = umi::aligned(out, 16) && (w % 4) == 0;
+	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+	char* ws = static_cast<char*>(scratch);
 	g.rowsum = reinterpret_cast<int32_t*>(ws);
 	g.colsum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4));
 	g.tilesum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4) + al((size_t)g.nty * w * 4));
