@@ -1,0 +1,278 @@
+// UMI operator, generic path: UMI::Execute for arbitrary strategies on sm_103a.
+//
+// Drop-in for the reference's templated launcher (johnjohnlin/UMI
+// src/UMI_gpu.h:409-623): same template parameters, same descriptor
+// arguments, so applications written against the reference compile
+// unchanged.  Strategy callbacks are device code of the application, so the
+// kernel is a template instantiated in the caller's translation unit; the
+// descriptor validation and address maps come from the library's C ABI
+// (umi_plan_build in libumi_gb300.so, link with -lumi_gb300).
+//
+// Differences from the reference launcher:
+//  * no index tables, no cudaMalloc/cudaMemcpy/__constant__ LUT per call:
+//    every address is a closed-form affine map of (p, a) passed by value;
+//  * returns umi_status (the reference returns void and aborts on bad
+//    descriptors); an extra trailing argument selects the CUDA stream;
+//  * asynchronous on that stream (the reference synchronises by freeing its
+//    tables);
+//  * inputs are read through the read-only data path with the same
+//    clamp/pad rule instead of a 64-thread shared-memory fill; ZeroStrideOpt
+//    is accepted and has no effect on results (the cache deduplicates the
+//    loads it would have saved).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "umi/UMI.h"
+#include "umi_gb300.h"
+
+namespace UMI {
+namespace gpu_detail {
+
+template <class EType, int NI, int NO>
+struct Pointers {
+	const EType* in[SafeArrayLength(NI) * MAX_PTR];
+	EType pad[SafeArrayLength(NI) * MAX_PTR];
+	EType* out[SafeArrayLength(NO) * MAX_PTR];
+};
+
+// Physical coordinates of memory `m` at point p (and accumulation index a
+// when `with_a`), folded into a linear element index; `outside` reports a
+// clamped PAD coordinate (inputs only).
+template <bool CLAMP>
+__device__ __forceinline__ int64_t address(const umi_mem_plan& m, const int (&p)[4], const int (&a)[4], bool with_a,
+                                           bool& outside) {
+	int64_t addr = 0;
+	outside = false;
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		int64_t c = m.base[k];
+#pragma unroll
+		for (int d = 0; d < 4; ++d) {
+			c += (int64_t)m.pcoef[k][d] * p[d];
+			if (with_a) c += (int64_t)m.acoef[k][d] * a[d];
+		}
+		if (CLAMP) {
+			const int64_t cl = c < 0 ? 0 : (c > m.size[k] - 1 ? m.size[k] - 1 : c);
+			outside |= (cl != c) && ((m.pad_mask >> k) & 1);
+			c = cl;
+		}
+		addr += c * m.rowstride[k];
+	}
+	return addr;
+}
+
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+__device__ __forceinline__ void gather(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
+                                       bool with_a, Arr& in) {
+#pragma unroll
+	for (int i = 0; i < N; ++i) {
+		const int mem = OFS + i;
+		bool outside;
+		const int64_t addr = address<true>(plan.mem[mem], p, a, with_a, outside);
+#pragma unroll
+		for (int j = 0; j < MAX_PTR; ++j) {
+			if (j < (int)Slice(PtrNum, 4, mem)) {
+				in[i * MAX_PTR + j] = outside ? ptrs.pad[mem * MAX_PTR + j] : ptrs.in[mem * MAX_PTR + j][addr];
+			}
+		}
+	}
+}
+
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+__device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
+                                        bool with_a, const Arr& out) {
+#pragma unroll
+	for (int i = 0; i < N; ++i) {
+		const int mem = OFS + i;
+		bool outside;
+		const int64_t addr = address<false>(plan.mem[Umi::TOTAL_IN + mem], p, a, with_a, outside);
+#pragma unroll
+		for (int j = 0; j < MAX_PTR; ++j) {
+			if (j < (int)Slice(PtrNum, 4, Umi::TOTAL_IN + mem)) ptrs.out[mem * MAX_PTR + j][addr] = out[i * MAX_PTR + j];
+		}
+	}
+}
+
+// One thread runs E0*E1*E2*E3 output points: p = cta_origin + e*block + t
+// (the reference's expand layout, src/UMI.cpp:153-155).  Each point runs Pre,
+// the Loop over A in blocked row-major order (src/UMI_gpu.h:287-346), then
+// Post; points outside P are skipped (the reference runs them and drops the
+// writes).
+template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType>
+__global__ void __launch_bounds__(1024) generic_kernel(const umi_plan plan, const CType uc,
+                                                        const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs) {
+	constexpr int E0 = (int)Slice(Expand, 4, 3), E1 = (int)Slice(Expand, 4, 2);
+	constexpr int E2 = (int)Slice(Expand, 4, 1), E3 = (int)Slice(Expand, 4, 0);
+	constexpr int ES = E0 * E1 * E2 * E3;
+	constexpr int PRE_I = 0, LOOP_I = Umi::N_PRE_IN, POST_I = Umi::N_PRE_IN + Umi::N_LOOP_IN;
+	constexpr int PRE_O = 0, LOOP_O = Umi::N_PRE_OUT, POST_O = Umi::N_PRE_OUT + Umi::N_LOOP_OUT;
+	const int zero[4] = {0, 0, 0, 0};
+	for (int64_t cta = blockIdx.x; cta < plan.n_cta; cta += gridDim.x) {
+		int g[4], t[4];
+		{
+			int64_t r = cta;
+#pragma unroll
+			for (int d = 3; d >= 0; --d) {
+				g[d] = (int)(r % plan.grid[d]);
+				r /= plan.grid[d];
+			}
+			int s = threadIdx.x;
+#pragma unroll
+			for (int d = 3; d >= 0; --d) {
+				t[d] = s % plan.block[d];
+				s /= plan.block[d];
+			}
+		}
+		int pts[ES][4];
+		bool valid[ES];
+#pragma unroll
+		for (int e = 0; e < ES; ++e) {
+			const int ex[4] = {e / (E1 * E2 * E3), (e / (E2 * E3)) % E1, (e / E3) % E2, e % E3};
+			bool v = true;
+#pragma unroll
+			for (int d = 0; d < 4; ++d) {
+				pts[e][d] = g[d] * plan.expand[d] * plan.block[d] + ex[d] * plan.block[d] + t[d];
+				v &= pts[e][d] < plan.ptotal[d];
+			}
+			valid[e] = v;
+		}
+		Umi ctx[ES];
+		// Pre
+#pragma unroll
+		for (int e = 0; e < ES; ++e) {
+			if (!valid[e]) continue;
+			simple_array<EType, Umi::N_PRE_IN * MAX_PTR> in;
+			simple_array<EType, Umi::N_PRE_OUT * MAX_PTR> out;
+			gather<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType>(plan, ptrs, pts[e], zero, false, in);
+			ctx[e].Pre(uc, in, out);
+			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, ptrs, pts[e], zero, false, out);
+		}
+		// Loop: accumulation blocks row-major, steps row-major inside a block.
+		if (plan.n_ablock > 0) {
+			int ab[4] = {0, 0, 0, 0};
+			for (int bi = 0; bi < plan.n_ablock; ++bi) {
+				int as[4] = {0, 0, 0, 0};
+				for (int si = 0; si < plan.ablock_size; ++si) {
+					int a[4];
+					bool ok = true;
+#pragma unroll
+					for (int d = 0; d < 4; ++d) {
+						a[d] = ab[d] * plan.ablock[d] + as[d];
+						ok &= a[d] < plan.atotal[d];
+					}
+					if (ok) {
+#pragma unroll
+						for (int e = 0; e < ES; ++e) {
+							if (!valid[e]) continue;
+							simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
+							simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
+							gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+							ctx[e].Loop(uc, in, out);
+							scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, ptrs, pts[e], a, true, out);
+						}
+					}
+#pragma unroll
+					for (int d = 3; d >= 0; --d) {
+						if (++as[d] < plan.ablock[d]) break;
+						as[d] = 0;
+					}
+				}
+#pragma unroll
+				for (int d = 3; d >= 0; --d) {
+					if (++ab[d] < plan.agrid[d]) break;
+					ab[d] = 0;
+				}
+			}
+		}
+		// Post
+#pragma unroll
+		for (int e = 0; e < ES; ++e) {
+			if (!valid[e]) continue;
+			simple_array<EType, Umi::N_POST_IN * MAX_PTR> in;
+			simple_array<EType, Umi::N_POST_OUT * MAX_PTR> out;
+			gather<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType>(plan, ptrs, pts[e], zero, false, in);
+			ctx[e].Post(uc, in, out);
+			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType>(plan, ptrs, pts[e], zero, false, out);
+		}
+	}
+}
+
+inline umi_vdim lower(const ViewDim& v) { return umi_vdim{v.physical_dim_id, v.ofs, v.stride}; }
+inline umi_phydim lower(const PhysicalDim& p) { return umi_phydim{p.size, (int32_t)p.mode}; }
+
+}  // namespace gpu_detail
+
+// Generic UMI operator (reference interface: src/UMI_gpu.h:409-422).
+template <
+	class Umi,
+	uint64_t PtrNum = 0x1111111111111111ull,
+	uint64_t Expand = 0x1111,
+	uint64_t ZeroStrideOpt = 0,
+	class EType = typename std::remove_cv<typename Umi::ElementType>::type,
+	class CType = typename std::remove_cv<typename Umi::UserConstantType>::type>
+umi_status Execute(
+	const NDTuple<ParallelDim>& p_dims,
+	const NDTuple<AccumulationDim>& a_dims,
+	const std::array<UnrolledI<EType>, Umi::TOTAL_IN>& imems,
+	const std::array<UnrolledO<EType>, Umi::TOTAL_OUT>& omems,
+	const CType& c = CType(),
+	cudaStream_t stream = 0) {
+	static_assert(Umi::TOTAL_IN + Umi::TOTAL_OUT <= UMI_MAX_MEMS, "at most 16 memories per call");
+	static_assert(((Expand >> 12) & 0xf) * ((Expand >> 8) & 0xf) * ((Expand >> 4) & 0xf) * (Expand & 0xf) > 0,
+	              "every Expand nibble must be >= 1");
+	(void)ZeroStrideOpt;
+	umi_desc d;
+	std::memset(&d, 0, sizeof(d));
+	for (int i = 0; i < DIM; ++i) {
+		d.p[i] = umi_pdim{p_dims[i].total_size, p_dims[i].block_size, p_dims[i].warp_size, p_dims[i].warp_shuf};
+		d.a[i] = umi_adim{a_dims[i].total_size, a_dims[i].block_size};
+	}
+	d.expand = (uint32_t)(Expand & 0xffff);
+	d.n_in = Umi::TOTAL_IN;
+	d.n_out = Umi::TOTAL_OUT;
+	auto stage_in = [](int i) { return i < Umi::N_PRE_IN ? 0 : (i < Umi::N_PRE_IN + Umi::N_LOOP_IN ? 1 : 2); };
+	auto stage_out = [](int i) { return i < Umi::N_PRE_OUT ? 0 : (i < Umi::N_PRE_OUT + Umi::N_LOOP_OUT ? 1 : 2); };
+	gpu_detail::Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs;
+	std::memset(&ptrs, 0, sizeof(ptrs));
+	for (int i = 0; i < Umi::TOTAL_IN; ++i) {
+		umi_mem_desc& m = d.mem[i];
+		for (int k = 0; k < DIM; ++k) {
+			m.p_view[k] = gpu_detail::lower(imems[i].p_view_dims[k]);
+			m.a_view[k] = gpu_detail::lower(imems[i].a_view_dims[k]);
+			m.phys[k] = gpu_detail::lower(imems[i].physical_dims[k]);
+		}
+		m.stage = stage_in(i);
+		m.n_ptr = (int32_t)Slice(PtrNum, 4, i);
+		for (int j = 0; j < MAX_PTR; ++j) {
+			ptrs.in[i * MAX_PTR + j] = imems[i].ptr[j];
+			ptrs.pad[i * MAX_PTR + j] = imems[i].padding[j];
+		}
+	}
+	for (int i = 0; i < Umi::TOTAL_OUT; ++i) {
+		umi_mem_desc& m = d.mem[Umi::TOTAL_IN + i];
+		for (int k = 0; k < DIM; ++k) {
+			m.p_view[k] = gpu_detail::lower(omems[i].p_view_dims[k]);
+			m.a_view[k] = gpu_detail::lower(omems[i].a_view_dims[k]);
+			m.phys[k] = gpu_detail::lower(omems[i].physical_dims[k]);
+		}
+		m.stage = stage_out(i);
+		m.n_ptr = (int32_t)Slice(PtrNum, 4, Umi::TOTAL_IN + i);
+		for (int j = 0; j < MAX_PTR; ++j) ptrs.out[i * MAX_PTR + j] = omems[i].ptr[j];
+	}
+	umi_plan plan;
+	const umi_status st = umi_plan_build(&d, &plan);
+	if (st != UMI_OK) return st;
+	for (int i = 0; i < Umi::TOTAL_IN + Umi::TOTAL_OUT; ++i)
+		for (int j = 0; j < d.mem[i].n_ptr; ++j)
+			if (i < Umi::TOTAL_IN ? ptrs.in[i * MAX_PTR + j] == nullptr
+			                      : ptrs.out[(i - Umi::TOTAL_IN) * MAX_PTR + j] == nullptr)
+				return UMI_ERR_INVALID_ARG;
+	if (plan.n_cta == 0) return UMI_OK;
+	const unsigned grid = (unsigned)(plan.n_cta < 0x7fffffff ? plan.n_cta : 0x7fffffff);
+	gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
+	return cudaGetLastError() == cudaSuccess ? UMI_OK : UMI_ERR_CUDA;
+}
+
+}  // namespace UMI
