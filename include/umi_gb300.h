@@ -173,6 +173,61 @@ umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
                               int32_t* sad, void* stream);
 
+/* Bilateral filter, float32 (h, w), (2*radius+1)^2 window, radius 1..3.
+ * out = sum(w*n) / sum(w) with w = exp(-(n-c)^2 / (2 sigma_r^2)) *
+ * ws[dy] * ws[dx], ws[i] = exp(-(i-radius)^2 / (2 sigma_s^2)), c the centre
+ * pixel; neighbours outside the image read as 0 and still contribute.
+ * Replaces the Execute call of main/bilateral.cu:54-100 (Bilateral strategy,
+ * main/bilateral.cu:9-24: there the spatial weights are a memory and the
+ * window is 25x25; the arithmetic per neighbour is the same). */
+umi_status umi_bilateral_f32(const float* in, float* out, int32_t h, int32_t w, int32_t radius, float sigma_s,
+                             float sigma_r, void* stream);
+
+/* 3x3 filter with a weight per pixel: out[y,x] = sum_{dy,dx}
+ * wts[y,x,dy+1,dx+1] * in[y+dy, x+dx], zero outside the image; wts is
+ * (h, w, 3, 3) float32.  The per-pixel form of main/wfilter3x3.cu:39-69
+ * (there the weight memory is one 3x3 kernel). */
+umi_status umi_wfilter3x3_pp_f32(const float* in, const float* wts, float* out, int32_t h, int32_t w, void* stream);
+
+/* Dot-product cost volume: left, right are (c, h, w) float32 feature maps,
+ * cv is (h, w, nd) float32 with cv[y,x,d] = sum_ch left[ch,y,x] *
+ * right[ch,y,x+d], right zero beyond the image.  nd in {16, 32, 64}.  The
+ * dot-product form of the horizontal cost volume of main/cost_volume.cu:17-65
+ * (there: |a-b| over a 7-tap window). */
+umi_status umi_cost_volume_dot_f32(const float* left, const float* right, float* cv, int32_t c, int32_t h, int32_t w,
+                                   int32_t nd, void* stream);
+
+/* ---- batched launches: many images of uneven sizes in one persistent
+ * launch.  The image table is copied into the launch (no device allocation);
+ * CTAs walk a prefix-summed queue of tiles across all images.  `variant`
+ * selects a tile shape (0 .. umi_batch_variants(op)-1; -1 = default), as
+ * chosen by umi_autotune_batch.  The reference launches once per image and
+ * allocates its index tables per call (src/UMI_gpu.h:374-381). */
+#define UMI_BATCH_MAX_IMAGES 256
+typedef enum { UMI_OP_BILATERAL = 0, UMI_OP_WFILTER_PP = 1, UMI_OP_COST_VOLUME = 2 } umi_batch_op;
+typedef struct {
+	const float* in;   /* bilateral / wfilter: image; cost volume: left features */
+	const float* aux;  /* wfilter: weights (h,w,3,3); cost volume: right features; else NULL */
+	float* out;
+	int32_t h, w;
+} umi_batch_image;
+typedef struct {
+	int32_t radius;    /* bilateral */
+	float sigma_s, sigma_r;
+	int32_t channels;  /* cost volume */
+	int32_t nd;        /* cost volume */
+} umi_batch_params;
+
+int32_t umi_batch_variants(int32_t op);
+umi_status umi_batch_run(int32_t op, const umi_batch_image* images, int32_t n_images, const umi_batch_params* params,
+                         int32_t variant, void* stream);
+/* Times every variant of `op` on this batch (CUDA events, `reps` launches
+ * each after one warm-up) and returns the fastest in *best_variant and its
+ * time in *best_ms.  The batch's outputs are overwritten. */
+umi_status umi_autotune_batch(int32_t op, const umi_batch_image* images, int32_t n_images,
+                              const umi_batch_params* params, int32_t reps, int32_t* best_variant, float* best_ms,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

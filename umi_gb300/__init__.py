@@ -56,6 +56,12 @@ SIGNATURES = {
     "umi_iimg_u8_i32_noalloc": ([_vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_bilateral_f32": ([_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp], ctypes.c_int),
+    "umi_wfilter3x3_pp_f32": ([_vp, _vp, _vp, _i32, _i32, _vp], ctypes.c_int),
+    "umi_cost_volume_dot_f32": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
+    "umi_batch_variants": ([_i32], _i32),
+    "umi_batch_run": ([_i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "umi_autotune_batch": ([_i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
 }
 
 
@@ -255,3 +261,90 @@ def full_me_sad_u8(cur, ref, block: int = 16, search: int = 32, out=None, stream
     check(lib().umi_full_me_sad_u8(_ptr(cur), _ptr(ref), h, w, block, search, _ptr(out), _stream_ptr(stream)),
           "umi_full_me_sad_u8")
     return out
+
+
+# ---- image operators and batches ----
+
+OP_BILATERAL, OP_WFILTER_PP, OP_COST_VOLUME = 0, 1, 2
+BATCH_MAX_IMAGES = 256
+
+
+class BatchImage(ctypes.Structure):
+    _fields_ = [("inp", _vp), ("aux", _vp), ("out", _vp), ("h", _i32), ("w", _i32)]
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("radius", _i32), ("sigma_s", _f32), ("sigma_r", _f32), ("channels", _i32), ("nd", _i32)]
+
+
+def bilateral_f32(inp, radius=2, sigma_s=2.0, sigma_r=0.1, out=None, stream=None):
+    """Bilateral filter of a float32 (h, w) CUDA tensor (umi_bilateral_f32)."""
+    import torch
+    _need(inp, torch.float32, "inp")
+    h, w = inp.shape
+    out = torch.empty_like(inp) if out is None else out
+    _need(out, torch.float32, "out")
+    check(lib().umi_bilateral_f32(_ptr(inp), _ptr(out), h, w, radius, sigma_s, sigma_r, _stream_ptr(stream)),
+          "umi_bilateral_f32")
+    return out
+
+
+def wfilter3x3_pp_f32(inp, wts, out=None, stream=None):
+    """Per-pixel-weight 3x3 filter; wts is (h, w, 3, 3) float32 (umi_wfilter3x3_pp_f32)."""
+    import torch
+    _need(inp, torch.float32, "inp")
+    _need(wts, torch.float32, "wts")
+    h, w = inp.shape
+    if tuple(wts.shape) != (h, w, 3, 3):
+        raise ValueError("wts must be (h, w, 3, 3)")
+    out = torch.empty_like(inp) if out is None else out
+    _need(out, torch.float32, "out")
+    check(lib().umi_wfilter3x3_pp_f32(_ptr(inp), _ptr(wts), _ptr(out), h, w, _stream_ptr(stream)),
+          "umi_wfilter3x3_pp_f32")
+    return out
+
+
+def cost_volume_dot_f32(left, right, nd=64, out=None, stream=None):
+    """Dot-product cost volume of (c, h, w) features into (h, w, nd) (umi_cost_volume_dot_f32)."""
+    import torch
+    _need(left, torch.float32, "left")
+    _need(right, torch.float32, "right")
+    c, h, w = left.shape
+    out = torch.empty((h, w, nd), dtype=torch.float32, device=left.device) if out is None else out
+    _need(out, torch.float32, "out")
+    check(lib().umi_cost_volume_dot_f32(_ptr(left), _ptr(right), _ptr(out), c, h, w, nd, _stream_ptr(stream)),
+          "umi_cost_volume_dot_f32")
+    return out
+
+
+def _batch_table(images):
+    n = len(images)
+    if n > BATCH_MAX_IMAGES:
+        raise ValueError("too many images")
+    tab = (BatchImage * max(n, 1))()
+    for i, (inp, aux, out) in enumerate(images):
+        h, w = inp.shape[-2], inp.shape[-1]
+        tab[i] = BatchImage(inp.data_ptr(), aux.data_ptr() if aux is not None else None, out.data_ptr(), h, w)
+    return tab
+
+
+def batch_run(op, images, params=None, variant=-1, stream=None):
+    """One persistent launch over a batch: images = [(in, aux_or_None, out), ...] (umi_batch_run)."""
+    tab = _batch_table(images)
+    prm = params if params is not None else BatchParams()
+    check(lib().umi_batch_run(op, tab, len(images), ctypes.byref(prm), variant, _stream_ptr(stream)), "umi_batch_run")
+
+
+def batch_variants(op):
+    return int(lib().umi_batch_variants(op))
+
+
+def autotune_batch(op, images, params=None, reps=3, stream=None):
+    """Time every tile variant of `op` on this batch; returns (variant, ms) (umi_autotune_batch)."""
+    tab = _batch_table(images)
+    prm = params if params is not None else BatchParams()
+    v = ctypes.c_int32(-1)
+    ms = ctypes.c_float(0)
+    check(lib().umi_autotune_batch(op, tab, len(images), ctypes.byref(prm), reps, ctypes.byref(v), ctypes.byref(ms),
+                                   _stream_ptr(stream)), "umi_autotune_batch")
+    return v.value, ms.value

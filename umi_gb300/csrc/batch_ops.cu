@@ -1,0 +1,481 @@
+// Image operators for batches of uneven images, sm_103a: bilateral filter,
+// per-pixel-weight 3x3 filter, dot-product cost volume.
+//
+// One persistent launch serves a whole batch: the image table (pointers and
+// sizes, up to UMI_BATCH_MAX_IMAGES) and the exclusive prefix of per-image
+// tile counts are kernel parameters (no allocation); CTA b takes tiles b,
+// b + grid, ... and finds each tile's image by binary search in the prefix.
+// The single-image entry points are batches of one.  Each operator has
+// several tile shapes ("variants") for the autotuner.
+//
+// Reference counterparts: the Bilateral strategy (main/bilateral.cu:9-24),
+// the WFilter3x3 strategy with a per-pixel weight memory
+// (main/wfilter3x3.cu:8-15), and the horizontal cost volume
+// (main/cost_volume.cu:8-65) with a dot-product cost.  The reference launches
+// one Execute per image.
+#include <algorithm>
+#include <cmath>
+
+#include "common.h"
+
+namespace {
+
+constexpr int MAXIMG = UMI_BATCH_MAX_IMAGES;
+constexpr int NT = 256;  // threads per CTA for every operator
+
+struct Img {
+	const float* in;
+	const float* aux;
+	float* out;
+	int h, w, tiles_x;
+	int vec;  // all pointers 16-byte aligned and w % 4 == 0
+};
+
+struct Table {
+	int n;
+	int start[MAXIMG + 1];
+	Img img[MAXIMG];
+};
+
+__device__ __forceinline__ int find_image(const Table& t, int tile) {
+	int lo = 0, hi = t.n;
+	while (hi - lo > 1) {
+		const int mid = (lo + hi) >> 1;
+		if (t.start[mid] <= tile) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
+// 2^x on the special-function unit (PTX ex2.approx, relative error ~2^-22).
+__device__ __forceinline__ float ex2(float x) {
+	float y;
+	asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+
+// ------------------------------------------------------------------ bilateral
+// Weight of neighbour n around centre c: 2^(fma((n-c)^2, k, lsw[dy][dx]))
+// with k = -log2(e) / (2 sigma_r^2) and lsw = log2(ws[dy] * ws[dx]): one
+// SFU instruction per neighbour.  Accumulation order (dy, dx) row-major as
+// main/bilateral.cu:111-117.
+struct BilParams {
+	float k;
+	float lsw[7][7];
+};
+
+template <int R, int TW, int TH, int PPT>
+struct Bilateral {
+	static constexpr int SW = TW + 2 * R, SH = TH + 2 * R;
+	static_assert(TW * TH / PPT == NT, "one pixel column of PPT per thread");
+	static constexpr size_t smem = sizeof(float) * SW * SH;
+	static int tiles_x(int w) { return umi::ceil_div(w, TW); }
+	static int tiles(int h, int w) { return tiles_x(w) * umi::ceil_div(h, TH); }
+	__device__ static void tile(const Img& im, int t, const BilParams& p, float* sm) {
+		const int ty = t / im.tiles_x, tx = t - ty * im.tiles_x;
+		const int X0 = tx * TW, Y0 = ty * TH;
+		for (int i = threadIdx.x; i < SW * SH; i += NT) {
+			const int sy = i / SW, sx = i - sy * SW;
+			const int gy = Y0 + sy - R, gx = X0 + sx - R;
+			sm[i] = (gy >= 0 && gy < im.h && gx >= 0 && gx < im.w) ? __ldg(im.in + (size_t)gy * im.w + gx) : 0.0f;
+		}
+		__syncthreads();
+		const int lx = threadIdx.x % TW, ly0 = (threadIdx.x / TW) * PPT;
+#pragma unroll
+		for (int q = 0; q < PPT; ++q) {
+			const int ly = ly0 + q;
+			const float c = sm[(ly + R) * SW + lx + R];
+			float ws = 0.0f, wx = 0.0f;
+#pragma unroll
+			for (int dy = 0; dy <= 2 * R; ++dy)
+#pragma unroll
+				for (int dx = 0; dx <= 2 * R; ++dx) {
+					const float n = sm[(ly + dy) * SW + lx + dx];
+					const float d = n - c;
+					const float wt = ex2(fmaf(d * d, p.k, p.lsw[dy][dx]));
+					ws += wt;
+					wx = fmaf(wt, n, wx);
+				}
+			const int gy = Y0 + ly, gx = X0 + lx;
+			if (gy < im.h && gx < im.w) im.out[(size_t)gy * im.w + gx] = wx / ws;
+		}
+		__syncthreads();
+	}
+};
+
+// ------------------------------------------------------------------ wfilter
+// A warp owns a 128-column strip and RY rows (4 pixels per lane, halo
+// columns by shuffle, every input row loaded once); the 9 weights of 4
+// pixels are 9 float4 loads.
+struct NoParams {};
+
+__device__ __forceinline__ float4 row4(const Img& im, int y, int x) {
+	if (y < 0 || y >= im.h) return make_float4(0.f, 0.f, 0.f, 0.f);
+	const float* r = im.in + (size_t)y * im.w;
+	if (im.vec && x + 3 < im.w) return __ldg(reinterpret_cast<const float4*>(r + x));
+	float4 v;
+	v.x = x < im.w ? __ldg(r + x) : 0.f;
+	v.y = x + 1 < im.w ? __ldg(r + x + 1) : 0.f;
+	v.z = x + 2 < im.w ? __ldg(r + x + 2) : 0.f;
+	v.w = x + 3 < im.w ? __ldg(r + x + 3) : 0.f;
+	return v;
+}
+
+template <int RY>
+struct WFilter {
+	static constexpr int WARPS = NT / 32;
+	static constexpr int TH = WARPS * RY;
+	static constexpr size_t smem = 0;
+	static int tiles_x(int w) { return umi::ceil_div(w, 128); }
+	static int tiles(int h, int w) { return tiles_x(w) * umi::ceil_div(h, TH); }
+	__device__ static void tile(const Img& im, int t, const NoParams&, float*) {
+		const int ty = t / im.tiles_x, tx = t - ty * im.tiles_x;
+		const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+		const int x0 = tx * 128, x = x0 + 4 * lane;
+		const int y0 = ty * TH + warp * RY;
+		if (y0 >= im.h) return;  // no barrier in this operator
+		float r[RY + 2][6];
+#pragma unroll
+		for (int i = 0; i < RY + 2; ++i) {
+			const int y = y0 - 1 + i;
+			const float4 v = row4(im, y, x);
+			float left = __shfl_up_sync(0xffffffffu, v.w, 1);
+			float right = __shfl_down_sync(0xffffffffu, v.x, 1);
+			const bool rowok = y >= 0 && y < im.h;
+			if (lane == 0) left = (rowok && x0 > 0) ? __ldg(im.in + (size_t)y * im.w + x0 - 1) : 0.f;
+			if (lane == 31) right = (rowok && x0 + 128 < im.w) ? __ldg(im.in + (size_t)y * im.w + x0 + 128) : 0.f;
+			r[i][0] = left; r[i][1] = v.x; r[i][2] = v.y; r[i][3] = v.z; r[i][4] = v.w; r[i][5] = right;
+		}
+#pragma unroll
+		for (int i = 0; i < RY; ++i) {
+			const int y = y0 + i;
+			if (y >= im.h) break;
+			float wv[36];
+			const float* wp = im.aux + ((size_t)y * im.w + x) * 9;
+			if (im.vec && x + 3 < im.w) {
+#pragma unroll
+				for (int k = 0; k < 9; ++k) {
+					const float4 q = __ldg(reinterpret_cast<const float4*>(wp) + k);
+					wv[4 * k] = q.x; wv[4 * k + 1] = q.y; wv[4 * k + 2] = q.z; wv[4 * k + 3] = q.w;
+				}
+			} else {
+#pragma unroll
+				for (int k = 0; k < 36; ++k) wv[k] = (x + k / 9 < im.w) ? __ldg(wp + k) : 0.f;
+			}
+			float o[4];
+#pragma unroll
+			for (int px = 0; px < 4; ++px) {
+				float s = 0.0f;
+#pragma unroll
+				for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+					for (int dx = 0; dx < 3; ++dx) s = fmaf(wv[9 * px + 3 * dy + dx], r[i + dy][px + dx], s);
+				o[px] = s;
+			}
+			float* dst = im.out + (size_t)y * im.w + x;
+			if (im.vec && x + 3 < im.w) {
+				*reinterpret_cast<float4*>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+			} else {
+#pragma unroll
+				for (int px = 0; px < 4; ++px)
+					if (x + px < im.w) dst[px] = o[px];
+			}
+		}
+	}
+};
+
+// ------------------------------------------------------------------ cost volume
+// One CTA computes one image row segment of TX pixels x ND disparities.
+// Lane (xb, db) of warp wv owns pixels x = wv*TXW + 8*xb + i and disparities
+// d = 8*db + j (i, j < 8): 64 accumulators; per channel it reads 8 left and
+// 15 right features from shared memory (right padded by one word per 8 so
+// the 15 reads are conflict-free).  Channels are staged in chunks of CC
+// with cp.async double buffering.  Channel order 0..c-1 per output.
+struct CvParams {
+	int channels;
+};
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+	const int n = valid ? 4 : 0;  // src-size 0: zero fill
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+template <int DB>
+struct CostVolume {
+	static constexpr int ND = 8 * DB;
+	static constexpr int XB = 32 / DB;
+	static constexpr int TXW = 8 * XB;          // pixels per warp
+	static constexpr int TX = (NT / 32) * TXW;  // pixels per CTA
+	static constexpr int CC = 8;                // channels per stage
+	static constexpr int RW = TX + ND - 1;      // right-feature columns per stage
+	static constexpr int RWP = RW + RW / 8 + 1; // padded
+	static constexpr int STAGE = CC * TX + CC * RWP;
+	static constexpr size_t smem = sizeof(float) * 2 * STAGE;
+	static int tiles_x(int w) { return umi::ceil_div(w, TX); }
+	static int tiles(int h, int w) { return tiles_x(w) * h; }
+	__device__ static int pad(int i) { return i + (i >> 3); }
+
+	__device__ static void stage(const Img& im, int y, int X0, int c0, int C, float* buf) {
+		const size_t plane = (size_t)im.h * im.w;
+		float* L = buf;
+		float* Rr = buf + CC * TX;
+		for (int i = threadIdx.x; i < CC * TX; i += NT) {
+			const int cc = i / TX, x = X0 + (i - cc * TX);
+			const bool ok = (c0 + cc < C) && x < im.w;
+			const float* src = ok ? im.in + (size_t)(c0 + cc) * plane + (size_t)y * im.w + x : im.in;
+			cp_async4(L + i, src, ok);
+		}
+		for (int i = threadIdx.x; i < CC * RW; i += NT) {
+			const int cc = i / RW, xi = i - cc * RW, x = X0 + xi;
+			const bool ok = (c0 + cc < C) && x < im.w;
+			const float* src = ok ? im.aux + (size_t)(c0 + cc) * plane + (size_t)y * im.w + x : im.aux;
+			cp_async4(Rr + cc * RWP + pad(xi), src, ok);
+		}
+		cp_async_commit();
+	}
+
+	__device__ static void tile(const Img& im, int t, const CvParams& p, float* sm) {
+		const int y = t / im.tiles_x, tx = t - y * im.tiles_x;
+		const int X0 = tx * TX;
+		const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+		const int xb = lane / DB, db = lane - xb * DB;
+		const int xl = warp * TXW + 8 * xb;  // first local pixel of this thread
+		const int C = p.channels;
+		float acc[8][8];
+#pragma unroll
+		for (int i = 0; i < 8; ++i)
+#pragma unroll
+			for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+		const int nst = (C + CC - 1) / CC;
+		stage(im, y, X0, 0, C, sm);
+		for (int s = 0; s < nst; ++s) {
+			float* cur = sm + (s & 1) * STAGE;
+			if (s + 1 < nst) {
+				stage(im, y, X0, (s + 1) * CC, C, sm + ((s + 1) & 1) * STAGE);
+				cp_async_wait_one();
+			} else {
+				cp_async_wait_all();
+			}
+			__syncthreads();
+			const float* L = cur;
+			const float* Rr = cur + CC * TX;
+#pragma unroll 2
+			for (int cc = 0; cc < CC; ++cc) {
+				float lv[8], rv[15];
+				const float4 l0 = *reinterpret_cast<const float4*>(L + cc * TX + xl);
+				const float4 l1 = *reinterpret_cast<const float4*>(L + cc * TX + xl + 4);
+				lv[0] = l0.x; lv[1] = l0.y; lv[2] = l0.z; lv[3] = l0.w;
+				lv[4] = l1.x; lv[5] = l1.y; lv[6] = l1.z; lv[7] = l1.w;
+#pragma unroll
+				for (int j = 0; j < 15; ++j) rv[j] = Rr[cc * RWP + pad(xl + 8 * db + j)];
+#pragma unroll
+				for (int i = 0; i < 8; ++i)
+#pragma unroll
+					for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(lv[i], rv[i + j], acc[i][j]);
+			}
+			__syncthreads();  // the next stage overwrites this buffer
+		}
+#pragma unroll
+		for (int i = 0; i < 8; ++i) {
+			const int x = X0 + xl + i;
+			if (x >= im.w) break;
+			float* dst = im.out + ((size_t)y * im.w + x) * ND + 8 * db;
+			if (im.vec) {
+				reinterpret_cast<float4*>(dst)[0] = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+				reinterpret_cast<float4*>(dst)[1] = make_float4(acc[i][4], acc[i][5], acc[i][6], acc[i][7]);
+			} else {
+#pragma unroll
+				for (int j = 0; j < 8; ++j) dst[j] = acc[i][j];
+			}
+		}
+	}
+};
+
+// ------------------------------------------------------------------ launcher
+template <class Op, class P>
+__global__ void __launch_bounds__(NT) batch_kernel(const Table t, const P p) {
+	extern __shared__ __align__(16) float sm[];
+	const int total = t.start[t.n];
+	for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+		const int i = find_image(t, tile);
+		Op::tile(t.img[i], tile - t.start[i], p, sm);
+	}
+}
+
+template <class Op, class P>
+umi_status launch(const umi_batch_image* images, int n, const P& p, bool need_aux, cudaStream_t st) {
+	Table t;
+	t.n = n;
+	t.start[0] = 0;
+	for (int i = 0; i < n; ++i) {
+		const umi_batch_image& b = images[i];
+		if (b.h < 0 || b.w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "batch image %d: negative size", i);
+		const bool empty = b.h == 0 || b.w == 0;
+		if (!empty && (!b.in || !b.out || (need_aux && !b.aux)))
+			return umi::fail(UMI_ERR_INVALID_ARG, "batch image %d: null pointer", i);
+		Img& m = t.img[i];
+		m.in = b.in; m.aux = b.aux; m.out = b.out; m.h = b.h; m.w = b.w;
+		m.tiles_x = empty ? 1 : Op::tiles_x(b.w);
+		m.vec = umi::aligned(b.in, 16) && umi::aligned(b.out, 16) && (!b.aux || umi::aligned(b.aux, 16)) &&
+		        (b.w % 4) == 0;
+		const int64_t nt = empty ? 0 : (int64_t)Op::tiles(b.h, b.w);
+		if (t.start[i] + nt > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "batch too large");
+		t.start[i + 1] = t.start[i] + (int)nt;
+	}
+	if (t.start[n] == 0) return UMI_OK;
+	auto kern = batch_kernel<Op, P>;
+	const size_t smem = Op::smem;
+	if (smem > 48 * 1024)
+		UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+		                         "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0, per_sm = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem),
+	                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
+	const int grid = std::max(1, std::min(t.start[n], sms * std::max(per_sm, 1)));
+	kern<<<grid, NT, smem, st>>>(t, p);
+	return umi::launch_status("batch_kernel");
+}
+
+// Variant tables.
+constexpr int kBilVariants = 4;
+template <int R>
+umi_status run_bilateral_r(const umi_batch_image* im, int n, const BilParams& p, int v, cudaStream_t st) {
+	switch (v) {
+		case 1: return launch<Bilateral<R, 32, 32, 4>>(im, n, p, false, st);
+		case 2: return launch<Bilateral<R, 64, 16, 4>>(im, n, p, false, st);
+		case 3: return launch<Bilateral<R, 32, 8, 1>>(im, n, p, false, st);
+		default: return launch<Bilateral<R, 32, 16, 2>>(im, n, p, false, st);
+	}
+}
+constexpr int kWfVariants = 3;
+constexpr int kCvVariants = 1;
+
+umi_status run_bilateral(const umi_batch_image* im, int n, const umi_batch_params& bp, int v, cudaStream_t st) {
+	if (bp.radius < 1 || bp.radius > 3) return umi::fail(UMI_ERR_UNSUPPORTED, "bilateral: radius %d (1..3)", bp.radius);
+	if (!(bp.sigma_s > 0.0f) || !(bp.sigma_r > 0.0f)) return umi::fail(UMI_ERR_INVALID_ARG, "bilateral: sigmas must be > 0");
+	BilParams p{};
+	const double log2e = 1.4426950408889634;
+	p.k = (float)(-log2e / (2.0 * (double)bp.sigma_r * (double)bp.sigma_r));
+	const int r = bp.radius;
+	for (int dy = 0; dy <= 2 * r; ++dy)
+		for (int dx = 0; dx <= 2 * r; ++dx) {
+			const double a = (double)((dy - r) * (dy - r) + (dx - r) * (dx - r));
+			p.lsw[dy][dx] = (float)(-a / (2.0 * (double)bp.sigma_s * (double)bp.sigma_s) * log2e);
+		}
+	switch (r) {
+		case 1: return run_bilateral_r<1>(im, n, p, v, st);
+		case 2: return run_bilateral_r<2>(im, n, p, v, st);
+		default: return run_bilateral_r<3>(im, n, p, v, st);
+	}
+}
+
+umi_status run_wfilter(const umi_batch_image* im, int n, int v, cudaStream_t st) {
+	switch (v) {
+		case 1: return launch<WFilter<2>>(im, n, NoParams{}, true, st);
+		case 2: return launch<WFilter<1>>(im, n, NoParams{}, true, st);
+		default: return launch<WFilter<4>>(im, n, NoParams{}, true, st);
+	}
+}
+
+umi_status run_cost_volume(const umi_batch_image* im, int n, const umi_batch_params& bp, int v, cudaStream_t st) {
+	(void)v;
+	if (bp.channels < 1) return umi::fail(UMI_ERR_INVALID_ARG, "cost volume: %d channels", bp.channels);
+	const CvParams p{bp.channels};
+	switch (bp.nd) {
+		case 16: return launch<CostVolume<2>>(im, n, p, true, st);
+		case 32: return launch<CostVolume<4>>(im, n, p, true, st);
+		case 64: return launch<CostVolume<8>>(im, n, p, true, st);
+		default: return umi::fail(UMI_ERR_UNSUPPORTED, "cost volume: nd %d (16, 32 or 64)", bp.nd);
+	}
+}
+
+umi_status run(int op, const umi_batch_image* im, int n, const umi_batch_params* bp, int v, cudaStream_t st) {
+	if (n < 0 || n > MAXIMG) return umi::fail(UMI_ERR_INVALID_ARG, "batch of %d images (max %d)", n, MAXIMG);
+	if (n > 0 && !im) return umi::fail(UMI_ERR_INVALID_ARG, "null image table");
+	if (!bp && op != UMI_OP_WFILTER_PP) return umi::fail(UMI_ERR_INVALID_ARG, "null params");
+	switch (op) {
+		case UMI_OP_BILATERAL: return run_bilateral(im, n, *bp, v, st);
+		case UMI_OP_WFILTER_PP: return run_wfilter(im, n, v, st);
+		case UMI_OP_COST_VOLUME: return run_cost_volume(im, n, *bp, v, st);
+		default: return umi::fail(UMI_ERR_INVALID_ARG, "unknown batch op %d", op);
+	}
+}
+
+}  // namespace
+
+extern "C" int32_t umi_batch_variants(int32_t op) {
+	switch (op) {
+		case UMI_OP_BILATERAL: return kBilVariants;
+		case UMI_OP_WFILTER_PP: return kWfVariants;
+		case UMI_OP_COST_VOLUME: return kCvVariants;
+		default: return 0;
+	}
+}
+
+extern "C" umi_status umi_batch_run(int32_t op, const umi_batch_image* images, int32_t n_images,
+                                    const umi_batch_params* params, int32_t variant, void* stream) {
+	const umi_status st = run(op, images, n_images, params, variant, umi::as_stream(stream));
+	return st == UMI_OK ? umi::ok() : st;
+}
+
+extern "C" umi_status umi_bilateral_f32(const float* in, float* out, int32_t h, int32_t w, int32_t radius, float sigma_s,
+                                        float sigma_r, void* stream) {
+	const umi_batch_image im{in, nullptr, out, h, w};
+	umi_batch_params p{};
+	p.radius = radius; p.sigma_s = sigma_s; p.sigma_r = sigma_r;
+	return umi_batch_run(UMI_OP_BILATERAL, &im, 1, &p, -1, stream);
+}
+
+extern "C" umi_status umi_wfilter3x3_pp_f32(const float* in, const float* wts, float* out, int32_t h, int32_t w,
+                                            void* stream) {
+	const umi_batch_image im{in, wts, out, h, w};
+	return umi_batch_run(UMI_OP_WFILTER_PP, &im, 1, nullptr, -1, stream);
+}
+
+extern "C" umi_status umi_cost_volume_dot_f32(const float* left, const float* right, float* cv, int32_t c, int32_t h,
+                                              int32_t w, int32_t nd, void* stream) {
+	const umi_batch_image im{left, right, cv, h, w};
+	umi_batch_params p{};
+	p.channels = c; p.nd = nd;
+	return umi_batch_run(UMI_OP_COST_VOLUME, &im, 1, &p, -1, stream);
+}
+
+extern "C" umi_status umi_autotune_batch(int32_t op, const umi_batch_image* images, int32_t n_images,
+                                         const umi_batch_params* params, int32_t reps, int32_t* best_variant,
+                                         float* best_ms, void* stream) {
+	if (!best_variant || !best_ms || reps < 1) return umi::fail(UMI_ERR_INVALID_ARG, "autotune: bad arguments");
+	const int nv = umi_batch_variants(op);
+	if (nv == 0) return umi::fail(UMI_ERR_INVALID_ARG, "autotune: unknown op %d", op);
+	const cudaStream_t st = umi::as_stream(stream);
+	cudaEvent_t a, b;
+	UMI_TRY(umi::cuda_status(cudaEventCreate(&a), "cudaEventCreate"));
+	UMI_TRY(umi::cuda_status(cudaEventCreate(&b), "cudaEventCreate"));
+	int best = 0;
+	float best_t = 0.0f;
+	umi_status rc = UMI_OK;
+	for (int v = 0; v < nv && rc == UMI_OK; ++v) {
+		rc = run(op, images, n_images, params, v, st);  // warm-up
+		if (rc != UMI_OK) break;
+		cudaEventRecord(a, st);
+		for (int r = 0; r < reps && rc == UMI_OK; ++r) rc = run(op, images, n_images, params, v, st);
+		cudaEventRecord(b, st);
+		if (rc != UMI_OK) break;
+		rc = umi::cuda_status(cudaEventSynchronize(b), "cudaEventSynchronize");
+		float ms = 0.0f;
+		cudaEventElapsedTime(&ms, a, b);
+		ms /= reps;
+		if (v == 0 || ms < best_t) { best_t = ms; best = v; }
+	}
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	if (rc != UMI_OK) return rc;
+	*best_variant = best;
+	*best_ms = best_t;
+	return umi::ok();
+}
