@@ -39,7 +39,7 @@ L2_BYTES = 129 * 2 ** 20
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
 # from the ncu capture summarised under profiles/ (None until captured).
-NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None}
+NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None}
 
 
 def parse():
@@ -48,11 +48,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024"], default="int_pair_1080p")
+    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven"],
+                    default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
     a = ap.parse_args()
     if a.steps is None:
-        a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000}[a.workload]
+        a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100}[a.workload]
     return a
 
 
@@ -304,7 +306,130 @@ class Filter3x3:
         return 8 * rows * self.W / 1e9
 
 
-WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3}
+class Batched:
+    """64 float images, H and W uniform in [256, 2048] (seeded), one persistent
+    launch per operator over the whole batch: bilateral 5x5 (sigma_s 2,
+    sigma_r 0.1), per-pixel-weight 3x3 filter (weights U[0,1)), dot-product
+    cost volume (32-channel N(0,1) features, right = left shifted by a
+    per-pixel disparity U{0..63} plus N(0, 0.1^2), 64 disparities)."""
+    name = "batched_uneven"
+    metric = "UMI batched ops GB/s"
+    unit = "GB/s"
+    dtype = "f32"
+    BYTES = {"bilateral": 8, "wfilter_pp": 44, "cost_volume": 512}  # algorithmic bytes per pixel
+    e2e_max_steps = 3  # each e2e step moves ~47 GB across the host link
+
+    def __init__(self, seed=7, n=64, lo=256, hi=2048):
+        g = np.random.default_rng(seed)
+        self.seed = seed
+        self.sizes = [(int(g.integers(lo, hi + 1)), int(g.integers(lo, hi + 1))) for _ in range(n)]
+        self.px = sum(h * w for h, w in self.sizes)
+
+    def config(self):
+        return {"workload": self.name, "images": len(self.sizes), "sides": "U{256..2048} (seeded)",
+                "total_px": self.px, "ops": "bilateral 5x5 s_s=2 s_r=0.1; wfilter3x3 per-pixel; "
+                "cost volume dot C=32 D=64", "bytes_per_px": self.BYTES, "l2": "inputs far larger than L2",
+                "variants": getattr(self, "variants", None)}
+
+    def units_per_step(self):
+        return sum(self.BYTES.values()) * self.px / 1e9
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        from umi_gb300 import autotune
+        self.U = U
+        gen = torch.Generator(device=dev).manual_seed(self.seed)
+        self.bil, self.wf, self.cv = [], [], []
+        for h, w in self.sizes:
+            img = torch.rand((h, w), generator=gen, device=dev)
+            wts = torch.rand((h, w, 3, 3), generator=gen, device=dev)
+            L = torch.randn((32, h, w), generator=gen, device=dev)
+            disp = torch.randint(0, 64, (h, w), generator=gen, device=dev)
+            src = (torch.arange(w, device=dev).view(1, w) - disp).clamp(0, w - 1)
+            R = torch.gather(L, 2, src.unsqueeze(0).expand(32, h, w)) + 0.1 * torch.randn((32, h, w), generator=gen,
+                                                                                         device=dev)
+            del src, disp
+            self.bil.append((img, None, torch.empty((h, w), device=dev)))
+            self.wf.append((img, wts, torch.empty((h, w), device=dev)))
+            self.cv.append((L, R.contiguous(), torch.empty((h, w, 64), device=dev)))
+        torch.cuda.synchronize()
+        self.pb = U.BatchParams(2, 2.0, 0.1, 0, 0)
+        self.pc = U.BatchParams(0, 0.0, 0.0, 32, 64)
+        self.variants = {}
+        for name, op, imgs, prm in (("bilateral", U.OP_BILATERAL, self.bil, self.pb),
+                                    ("wfilter_pp", U.OP_WFILTER_PP, self.wf, None),
+                                    ("cost_volume", U.OP_COST_VOLUME, self.cv, self.pc)):
+            v, ms, cached = autotune.tuned_variant(op, imgs, prm)
+            self.variants[name] = {"variant": v, "ms": ms, "cached": cached}
+        self.n_rot = 1
+        self.launches_per_step = 3
+
+    def _ops(self):
+        U = self.U
+        return (("bilateral", lambda: U.batch_run(U.OP_BILATERAL, self.bil, self.pb, self.variants["bilateral"]["variant"])),
+                ("wfilter_pp", lambda: U.batch_run(U.OP_WFILTER_PP, self.wf, None, self.variants["wfilter_pp"]["variant"])),
+                ("cost_volume", lambda: U.batch_run(U.OP_COST_VOLUME, self.cv, self.pc,
+                                                    self.variants["cost_volume"]["variant"])))
+
+    def step(self, i):
+        for _, fn in self._ops():
+            fn()
+
+    def e2e_setup(self):
+        import torch
+        self.h_in = [[t.cpu().pin_memory() for t in (a, b) if t is not None] for a, b, _ in self.wf + self.cv]
+        self.h_out = [o.cpu().pin_memory() for _, _, o in self.bil + self.wf + self.cv]
+        torch.cuda.synchronize()
+
+    def step_e2e(self, i):
+        dev_in = [[t for t in (a, b) if t is not None] for a, b, _ in self.wf + self.cv]
+        for hs, ds in zip(self.h_in, dev_in):
+            for h, d in zip(hs, ds):
+                d.copy_(h, non_blocking=True)
+        self.step(i)
+        for h, (_, _, o) in zip(self.h_out, self.bil + self.wf + self.cv):
+            h.copy_(o, non_blocking=True)
+
+    def e2e_bytes(self):
+        h2d = sum(t.numel() * 4 for a, b, _ in self.wf + self.cv for t in (a, b) if t is not None)
+        d2h = sum(o.numel() * 4 for _, _, o in self.bil + self.wf + self.cv)
+        return h2d, d2h
+
+    def check(self):
+        """Sampled FP64 check of the timed outputs (full parity lives in the tests)."""
+        g = np.random.default_rng(0)
+        worst = 0.0
+        for k in g.choice(len(self.sizes), 4, replace=False):
+            L, R, cv = (t.cpu().numpy() if t is not None else None for t in self.cv[k])
+            h, w = L.shape[1:]
+            for _ in range(50):
+                y, x, d = int(g.integers(h)), int(g.integers(w)), int(g.integers(64))
+                want = float(np.dot(L[:, y, x].astype(np.float64), R[:, y, x + d].astype(np.float64))) if x + d < w else 0.0
+                scale = float(np.abs(L[:, y, x]).astype(np.float64) @ np.abs(R[:, y, min(x + d, w - 1)]).astype(np.float64))
+                worst = max(worst, float(abs(float(cv[y, x, d]) - want) / max(abs(want), scale, 1e-30)))
+        return worst
+
+    def kernels(self, dev, peaks, n=3):
+        return {name: time_launches(lambda i, f=fn: f(), 1, n) for name, fn in self._ops()}, None, None
+
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+        self.rng = np.random.default_rng(1)
+
+    def cpu_step(self, rows, threads):
+        """FP64 oracle of the three operators on `rows` rows of a 1024-wide crop."""
+        g = self.rng
+        x = g.random((rows, 1024), dtype=np.float32)
+        self.orc.bilateral_f64(x, 2, 2.0, 0.1, threads=threads)
+        self.orc.wfilter_pp_f64(x, g.random((rows, 1024, 3, 3), dtype=np.float32), threads=threads)
+        L = g.standard_normal((32, rows, 1024)).astype(np.float32)
+        self.orc.cost_volume_dot_f64(L, L, 64, threads=threads)
+        return sum(self.BYTES.values()) * rows * 1024 / 1e9
+
+
+WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -423,19 +548,22 @@ def run_ours(args, wl, dist):
     value = wl.units_per_step() * args.steps * dist.world / (ms * 1e-3)
     sanity = wl.check()
 
-    # e2e: host buffers, copies inside the timed region
-    for i in range(min(args.warmup, 5)):
+    # e2e: host buffers, copies inside the timed region (eager C-ABI calls)
+    if hasattr(wl, "e2e_setup"):
+        wl.e2e_setup()
+    e2e_steps = min(args.steps, getattr(wl, "e2e_max_steps", args.steps))
+    for i in range(min(args.warmup, 2)):
         wl.step_e2e(i)
     torch.cuda.synchronize()
     dist.barrier()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2.record(st)
-    for i in range(args.steps):
+    for i in range(e2e_steps):
         wl.step_e2e(i)
     e3.record(st)
     torch.cuda.synchronize()
     ms_e2e = dist.max(e2.elapsed_time(e3))
-    e2e_value = wl.units_per_step() * args.steps * dist.world / (ms_e2e * 1e-3)
+    e2e_value = wl.units_per_step() * e2e_steps * dist.world / (ms_e2e * 1e-3)
     h2d, d2h = wl.e2e_bytes()
 
     # dominant kernel roofline
@@ -452,6 +580,15 @@ def run_ours(args, wl, dist):
         kernels["iimg_u8_i32"] = {"ms_per_launch": kms["iimg_u8_i32"], "achieved": ig, "unit": "GB/s",
                                   "peak": pk["hbm_gbs"], "frac": ig / pk["hbm_gbs"], "bytes_per_launch": hbm_bytes,
                                   "peak_source": pk["source"]}
+    elif isinstance(wl, Batched):
+        for name, kt in kms.items():
+            b = wl.BYTES[name] * wl.px
+            kernels[name] = {"ms_per_launch": kt, "achieved": b / (kt * 1e-3) / 1e9, "unit": "GB/s",
+                             "frac": b / (kt * 1e-3) / 1e9 / pk["hbm_gbs"], "bytes_per_launch": b}
+        kernels["bilateral"]["ex2_per_s"] = 25 * wl.px / (kms["bilateral"] * 1e-3)
+        dom = max(kms, key=kms.get)
+        roof = dict(kernels[dom], bound="hbm", kernel=dom, peak=pk["hbm_gbs"], traffic=NCU_TRAFFIC.get(wl.name),
+                    peak_source=pk["source"])
     else:
         ach = hbm_bytes / (kms["filter3x3_f32"] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": "filter3x3_f32", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -464,13 +601,13 @@ def run_ours(args, wl, dist):
         "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded numpy generators)",
         "config": dict(wl.config(), parallelism=f"replicas x{dist.world}"),
         "e2e": {"value": e2e_value, "unit": wl.unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": ms_e2e / args.steps},
+                "ms_per_step": ms_e2e / e2e_steps, "steps": e2e_steps},
         "gpu_launches": wl.launches_per_step * args.steps,
         "roofline": roof, "kernels": kernels, "clocks": clk,
         "impl": "ours",
     }
     if sanity is not None:
-        line["sanity_true_mv_recovered"] = sanity
+        line["sanity_true_mv_recovered" if isinstance(wl, IntPair) else "sanity_max_rel_err_sampled"] = sanity
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, sample_s=10.0)
     return line
@@ -482,6 +619,8 @@ def cpu_baseline(wl, sample_s=10.0):
     wl.cpu_setup()
     if isinstance(wl, IntPair):
         chunk, what = 256, "random blocks of the 1080p pair, +-32 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin, plus the matching rows of iimg (main/iimg.cu:100-111)"
+    elif isinstance(wl, Batched):
+        chunk, what = 8, "rows of 1024-wide crops through the FP64 restatements of bilateral 5x5, per-pixel wfilter3x3 and the 32x64 dot cost volume"
     else:
         chunk, what = 128, "rows of the 1024x1024 image, 3x3 weighted sum in FP64"
     units, t0 = 0.0, time.perf_counter()
@@ -500,7 +639,7 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = 32 if isinstance(wl, IntPair) else 16
+    per_step = 32 if isinstance(wl, IntPair) else (2 if isinstance(wl, Batched) else 16)
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()
@@ -523,7 +662,7 @@ def run_reference(args, wl, dist):
 
 def main():
     args = parse()
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload](n=args.images) if args.workload == "batched_uneven" else WORKLOADS[args.workload]()
     if args.impl == "reference":
         dist = Dist("gloo")
         line = run_reference(args, wl, dist)
@@ -531,7 +670,7 @@ def main():
         dist = Dist("nccl")
         line = run_ours(args, wl, dist)
     if dist.rank == 0 and line is not None:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=float), flush=True)
     dist.done()
 
 

@@ -187,14 +187,22 @@ struct WFilter {
 // ------------------------------------------------------------------ cost volume
 // One CTA computes one image row segment of TX pixels x ND disparities.
 // Lane (xb, db) of warp wv owns pixels x = wv*TXW + 8*xb + i and disparities
-// d = 8*db + j (i, j < 8): 64 accumulators; per channel it reads 8 left and
-// 15 right features from shared memory (right padded by one word per 8 so
-// the 15 reads are conflict-free).  Channels are staged in chunks of CC
-// with cp.async double buffering.  Channel order 0..c-1 per output.
+// d = 8*db + j (i, j < 8): 64 accumulators.  Per channel it reads its 8 left
+// features (two 128-bit loads) and the 15 right features x + d it needs
+// (four 128-bit loads) from shared memory.  Right rows are stored with 4
+// floats of padding after every 32, which keeps 16-byte chunks whole and puts
+// the 8 chunks one quarter-warp reads in 8 distinct bank groups.  Channels are
+// staged CC at a time (one channel row per warp) with 16-byte cp.async,
+// double-buffered; the image edge is zero-filled by partial copies.  Channel
+// order 0..c-1 per output.
 struct CvParams {
 	int channels;
 };
 
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, int bytes) {
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
 	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
 	const int n = valid ? 4 : 0;  // src-size 0: zero fill
@@ -203,37 +211,47 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool val
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_two() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
 
 template <int DB>
 struct CostVolume {
 	static constexpr int ND = 8 * DB;
 	static constexpr int XB = 32 / DB;
-	static constexpr int TXW = 8 * XB;          // pixels per warp
-	static constexpr int TX = (NT / 32) * TXW;  // pixels per CTA
-	static constexpr int CC = 8;                // channels per stage
-	static constexpr int RW = TX + ND - 1;      // right-feature columns per stage
-	static constexpr int RWP = RW + RW / 8 + 1; // padded
+	static constexpr int TXW = 8 * XB;                  // pixels per warp
+	static constexpr int TX = (NT / 32) * TXW;          // pixels per CTA
+	static constexpr int CC = NT / 32;                  // channels per stage: one per warp
+	static constexpr int RW = (TX + ND + 3) / 4 * 4;    // right columns staged (>= TX + ND - 1, whole chunks)
+	static constexpr int RWP = RW + 4 * (RW / 32) + 4;  // padded row
 	static constexpr int STAGE = CC * TX + CC * RWP;
-	static constexpr size_t smem = sizeof(float) * 2 * STAGE;
+	static constexpr int NBUF = 3;  // stages in flight: covers DRAM latency at two CTAs per SM
+	static constexpr size_t smem = sizeof(float) * NBUF * STAGE;
+	static_assert(TX % 4 == 0 && RWP % 4 == 0 && STAGE % 4 == 0, "16-byte aligned rows");
 	static int tiles_x(int w) { return umi::ceil_div(w, TX); }
 	static int tiles(int h, int w) { return tiles_x(w) * h; }
-	__device__ static int pad(int i) { return i + (i >> 3); }
+	__device__ static int pad(int e) { return e + 4 * (e >> 5); }
 
 	__device__ static void stage(const Img& im, int y, int X0, int c0, int C, float* buf) {
-		const size_t plane = (size_t)im.h * im.w;
-		float* L = buf;
-		float* Rr = buf + CC * TX;
-		for (int i = threadIdx.x; i < CC * TX; i += NT) {
-			const int cc = i / TX, x = X0 + (i - cc * TX);
-			const bool ok = (c0 + cc < C) && x < im.w;
-			const float* src = ok ? im.in + (size_t)(c0 + cc) * plane + (size_t)y * im.w + x : im.in;
-			cp_async4(L + i, src, ok);
-		}
-		for (int i = threadIdx.x; i < CC * RW; i += NT) {
-			const int cc = i / RW, xi = i - cc * RW, x = X0 + xi;
-			const bool ok = (c0 + cc < C) && x < im.w;
-			const float* src = ok ? im.aux + (size_t)(c0 + cc) * plane + (size_t)y * im.w + x : im.aux;
-			cp_async4(Rr + cc * RWP + pad(xi), src, ok);
+		const int cc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+		const bool chan = c0 + cc < C;
+		const size_t off = (size_t)(chan ? c0 + cc : 0) * im.h * im.w + (size_t)y * im.w + X0;
+		const float* lsrc = im.in + off;
+		const float* rsrc = im.aux + off;
+		float* L = buf + cc * TX;
+		float* Rr = buf + CC * TX + cc * RWP;
+		const int lim = chan ? im.w - X0 : 0;  // valid columns from X0
+		if (im.vec) {
+			// rows are 16-byte aligned: whole chunks, partial (zero-filled) at the edge
+			for (int q = lane; q < TX / 4; q += 32) {
+				const int v = min(max(lim - 4 * q, 0), 4);
+				cp_async16(L + 4 * q, v ? lsrc + 4 * q : im.in, 4 * v);
+			}
+			for (int q = lane; q < RW / 4; q += 32) {
+				const int v = min(max(lim - 4 * q, 0), 4);
+				cp_async16(Rr + pad(4 * q), v ? rsrc + 4 * q : im.aux, 4 * v);
+			}
+		} else {
+			for (int x = lane; x < TX; x += 32) cp_async4(L + x, x < lim ? lsrc + x : im.in, x < lim);
+			for (int x = lane; x < RW; x += 32) cp_async4(Rr + pad(x), x < lim ? rsrc + x : im.aux, x < lim);
 		}
 		cp_async_commit();
 	}
@@ -244,6 +262,10 @@ struct CostVolume {
 		const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 		const int xb = lane / DB, db = lane - xb * DB;
 		const int xl = warp * TXW + 8 * xb;  // first local pixel of this thread
+		const int e0 = xl + 8 * db;          // first right column it reads
+		int roff[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) roff[q] = pad(e0 + 4 * q);
 		const int C = p.channels;
 		float acc[8][8];
 #pragma unroll
@@ -252,26 +274,33 @@ struct CostVolume {
 			for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 		const int nst = (C + CC - 1) / CC;
 		stage(im, y, X0, 0, C, sm);
+		if (nst > 1) stage(im, y, X0, CC, C, sm + STAGE);
 		for (int s = 0; s < nst; ++s) {
-			float* cur = sm + (s & 1) * STAGE;
-			if (s + 1 < nst) {
-				stage(im, y, X0, (s + 1) * CC, C, sm + ((s + 1) & 1) * STAGE);
+			const float* cur = sm + (s % NBUF) * STAGE;
+			// keep up to NBUF stages in flight; wait until stage s has landed
+			if (s + 2 < nst) {
+				stage(im, y, X0, (s + 2) * CC, C, sm + ((s + 2) % NBUF) * STAGE);
+				cp_async_wait_two();
+			} else if (s + 1 < nst) {
 				cp_async_wait_one();
 			} else {
 				cp_async_wait_all();
 			}
 			__syncthreads();
-			const float* L = cur;
+			const float* L = cur + xl;
 			const float* Rr = cur + CC * TX;
-#pragma unroll 2
+#pragma unroll 1
 			for (int cc = 0; cc < CC; ++cc) {
-				float lv[8], rv[15];
-				const float4 l0 = *reinterpret_cast<const float4*>(L + cc * TX + xl);
-				const float4 l1 = *reinterpret_cast<const float4*>(L + cc * TX + xl + 4);
+				float lv[8], rv[16];
+				const float4 l0 = *reinterpret_cast<const float4*>(L + cc * TX);
+				const float4 l1 = *reinterpret_cast<const float4*>(L + cc * TX + 4);
 				lv[0] = l0.x; lv[1] = l0.y; lv[2] = l0.z; lv[3] = l0.w;
 				lv[4] = l1.x; lv[5] = l1.y; lv[6] = l1.z; lv[7] = l1.w;
 #pragma unroll
-				for (int j = 0; j < 15; ++j) rv[j] = Rr[cc * RWP + pad(xl + 8 * db + j)];
+				for (int q = 0; q < 4; ++q) {
+					const float4 r4 = *reinterpret_cast<const float4*>(Rr + cc * RWP + roff[q]);
+					rv[4 * q] = r4.x; rv[4 * q + 1] = r4.y; rv[4 * q + 2] = r4.z; rv[4 * q + 3] = r4.w;
+				}
 #pragma unroll
 				for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -297,7 +326,7 @@ struct CostVolume {
 
 // ------------------------------------------------------------------ launcher
 template <class Op, class P>
-__global__ void __launch_bounds__(NT) batch_kernel(const Table t, const P p) {
+__global__ void __launch_bounds__(NT, 2) batch_kernel(const Table t, const P p) {
 	extern __shared__ __align__(16) float sm[];
 	const int total = t.start[t.n];
 	for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
