@@ -39,7 +39,7 @@ L2_BYTES = 129 * 2 ** 20
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
 # from the ncu capture summarised under profiles/ (None until captured).
-NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None}
+NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None, "gemm_4096": None}
 
 
 def parse():
@@ -48,13 +48,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven"],
+    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
     a = ap.parse_args()
     if a.steps is None:
-        a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100}[a.workload]
+        a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
+                   "gemm_4096": 3000}[a.workload]
     return a
 
 
@@ -429,7 +430,120 @@ class Batched:
         return sum(self.BYTES.values()) * rows * 1024 / 1e9
 
 
-WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched}
+class Gemm:
+    """C = A @ B^T, M = N = K = 4096, A and B ~ N(0,1), bf16 operands, fp32
+    accumulation on the tcgen05 tensor cores.  The f16 and bf16x3 (fp32
+    emulation) variants are timed beside it; each reports max / RMS error
+    against FP64 on sampled rows."""
+    name = "gemm_4096"
+    metric = "gemm TFLOP/s (4096^3, bf16 in, fp32 accumulate)"
+    unit = "TFLOP/s"
+    dtype = "bf16"
+    M = N = K = 4096
+
+    def __init__(self, seed=11, **_):
+        self.seed = seed
+        self.flops = 2.0 * self.M * self.N * self.K
+
+    def config(self):
+        return {"workload": self.name, "M": self.M, "N": self.N, "K": self.K, "layout": "A (M,K), B (N,K) row-major",
+                "inputs": "N(0,1)", "l2": "3 rotating operand sets (384 MB)"}
+
+    def units_per_step(self):
+        return self.flops / 1e12
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        self.U = U
+        gen = torch.Generator(device=dev).manual_seed(self.seed)
+        self.a32 = torch.randn((self.M, self.K), generator=gen, device=dev)
+        self.b32 = torch.randn((self.N, self.K), generator=gen, device=dev)
+        self.n_rot = 3
+        self.A = [self.a32.to(torch.bfloat16) for _ in range(self.n_rot)]
+        self.B = [self.b32.to(torch.bfloat16) for _ in range(self.n_rot)]
+        self.C = [torch.empty((self.M, self.N), device=dev) for _ in range(self.n_rot)]
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.launches_per_step = 1
+        self.hA = self.A[0].cpu().pin_memory()
+        self.hB = self.B[0].cpu().pin_memory()
+        self.hC = torch.empty((self.M, self.N)).pin_memory()
+
+    def step(self, i):
+        k = i % self.n_rot
+        self.U.gemm(self.A[k], self.B[k], out=self.C[k], err=self.err)
+
+    def step_e2e(self, i):
+        k = i % self.n_rot
+        self.A[k].copy_(self.hA, non_blocking=True)
+        self.B[k].copy_(self.hB, non_blocking=True)
+        self.U.gemm(self.A[k], self.B[k], out=self.C[k], err=self.err)
+        self.hC.copy_(self.C[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return 2 * 2 * self.M * self.K, 4 * self.M * self.N
+
+    @staticmethod
+    def _err(C, ref, rows):
+        got = C[rows].double().cpu().numpy()
+        d = np.abs(got - ref)
+        rel = d / np.maximum(np.abs(ref), 1e-30)
+        return {"max_abs": float(d.max()), "rms_abs": float(np.sqrt((d ** 2).mean())),
+                "max_rel_to_scale": None, "rms_rel": float(np.sqrt(np.mean(np.minimum(rel, 1.0) ** 2)))}
+
+    def check(self):
+        import torch
+        rows = np.random.default_rng(0).choice(self.M, 32, replace=False)
+        a64 = self.A[0][rows].double().cpu().numpy()
+        b64 = self.B[0].double().cpu().numpy()
+        ref = a64 @ b64.T
+        scale = np.abs(a64) @ np.abs(b64).T
+        C = self.C[0][rows].double().cpu().numpy()
+        out = {"bf16_max_err_over_scale": float((np.abs(C - ref) / scale).max())}
+        # fp32-emulation variant against the fp32 inputs
+        a32 = self.a32[rows].double().cpu().numpy()
+        b32 = self.b32.double().cpu().numpy()
+        ref32 = a32 @ b32.T
+        C3 = self.U.gemm_f32_bf16x3(self.a32, self.b32)[rows].double().cpu().numpy()
+        d3 = np.abs(C3 - ref32)
+        out["bf16x3_vs_fp32_inputs"] = {"max_abs": float(d3.max()), "rms_abs": float(np.sqrt((d3 ** 2).mean())),
+                                        "max_rel": float((d3 / np.abs(ref32)).max()),
+                                        "median_rel": float(np.median(d3 / np.abs(ref32)))}
+        Cb = self.C[0][rows].double().cpu().numpy()
+        db = np.abs(Cb - ref32)
+        out["bf16_vs_fp32_inputs"] = {"max_abs": float(db.max()), "rms_abs": float(np.sqrt((db ** 2).mean())),
+                                      "median_rel": float(np.median(db / np.abs(ref32)))}
+        out["err_word"] = int(self.err.item())
+        return out
+
+    def kernels(self, dev, peaks, n=30):
+        import torch
+        R = self.n_rot
+        A16 = [a.to(torch.float16) for a in self.A]
+        B16 = [b.to(torch.float16) for b in self.B]
+        ws = torch.empty(self.U.lib().umi_gemm_f32_bf16x3_workspace_bytes(self.M, self.N, self.K), dtype=torch.uint8,
+                         device=dev)
+        a32, b32 = self.a32, self.b32
+        fns = {"gemm_bf16": lambda i: self.U.gemm(self.A[i % R], self.B[i % R], out=self.C[i % R], err=self.err),
+               "gemm_f16": lambda i: self.U.gemm(A16[i % R], B16[i % R], out=self.C[i % R], err=self.err),
+               "gemm_f32_bf16x3": lambda i: self.U.gemm_f32_bf16x3(a32, b32, out=self.C[i % R], workspace=ws,
+                                                                   err=self.err)}
+        return {k: time_launches(f, R, n) for k, f in fns.items()}, None, None
+
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+        g = np.random.default_rng(1)
+        self.ha = g.standard_normal((256, self.K)).astype(np.float32)
+        self.hb = g.standard_normal((self.N, self.K)).astype(np.float32)
+
+    def cpu_step(self, rows, threads):
+        """The reference's gemm loop (main/gemm.cu:69-78, restated with FP64 accumulation) on `rows` rows of C."""
+        self.orc.gemm_f64(self.ha[:rows], self.hb, b_is_nk=True, threads=threads)
+        return 2.0 * rows * self.N * self.K / 1e12
+
+
+WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -580,6 +694,17 @@ def run_ours(args, wl, dist):
         kernels["iimg_u8_i32"] = {"ms_per_launch": kms["iimg_u8_i32"], "achieved": ig, "unit": "GB/s",
                                   "peak": pk["hbm_gbs"], "frac": ig / pk["hbm_gbs"], "bytes_per_launch": hbm_bytes,
                                   "peak_source": pk["source"]}
+    elif isinstance(wl, Gemm):
+        for name, kt in kms.items():
+            f = wl.flops * (3 if name == "gemm_f32_bf16x3" else 1)
+            kernels[name] = {"ms_per_launch": kt, "achieved": f / (kt * 1e-3) / 1e12, "unit": "TFLOP/s",
+                             "frac": f / (kt * 1e-3) / 1e12 / pk["bf16_tflops"],
+                             "note": "bf16x3 does 3 bf16 GEMMs per fp32 GEMM; achieved counts tensor FLOPs"
+                             if name == "gemm_f32_bf16x3" else None}
+        kernels["gemm_f32_bf16x3"]["fp32_gemm_tflops"] = wl.flops / (kms["gemm_f32_bf16x3"] * 1e-3) / 1e12
+        roof = dict(kernels["gemm_bf16"], bound="tensor", kernel="gemm_tc_kernel (bf16)", peak=pk["bf16_tflops"],
+                    traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
+                    flops_per_launch=wl.flops)
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
             b = wl.BYTES[name] * wl.px
@@ -607,7 +732,9 @@ def run_ours(args, wl, dist):
         "impl": "ours",
     }
     if sanity is not None:
-        line["sanity_true_mv_recovered" if isinstance(wl, IntPair) else "sanity_max_rel_err_sampled"] = sanity
+        key = {IntPair: "sanity_true_mv_recovered", Gemm: "errors_vs_fp64_sampled_rows"}.get(type(wl),
+                                                                                           "sanity_max_rel_err_sampled")
+        line[key] = sanity
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, sample_s=10.0)
     return line
@@ -619,6 +746,8 @@ def cpu_baseline(wl, sample_s=10.0):
     wl.cpu_setup()
     if isinstance(wl, IntPair):
         chunk, what = 256, "random blocks of the 1080p pair, +-32 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin, plus the matching rows of iimg (main/iimg.cu:100-111)"
+    elif isinstance(wl, Gemm):
+        chunk, what = 4, "rows of the 4096^3 product, the reference's gemm loop (main/gemm.cu:69-78) with FP64 accumulation"
     elif isinstance(wl, Batched):
         chunk, what = 8, "rows of 1024-wide crops through the FP64 restatements of bilateral 5x5, per-pixel wfilter3x3 and the 32x64 dot cost volume"
     else:
@@ -639,7 +768,7 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = 32 if isinstance(wl, IntPair) else (2 if isinstance(wl, Batched) else 16)
+    per_step = {IntPair: 32, Batched: 2, Gemm: 2}.get(type(wl), 16)
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()

@@ -197,6 +197,28 @@ umi_status umi_wfilter3x3_pp_f32(const float* in, const float* wts, float* out, 
 umi_status umi_cost_volume_dot_f32(const float* left, const float* right, float* cv, int32_t c, int32_t h, int32_t w,
                                    int32_t nd, void* stream);
 
+/* Tensor-core GEMM (tcgen05, sm_103a): C[M,N] = A[M,K] * B[N,K]^T with A and
+ * B row-major bf16 (umi_gemm_bf16) or f16 (umi_gemm_f16), fp32 accumulation
+ * and fp32 row-major C.  K must be a multiple of 8; A, B 16-byte aligned.
+ * `err` (optional, device int) receives error bits if a bounded internal wait
+ * gave up (then the call also leaves C unspecified); it is never cleared by the
+ * library.  Replaces the Execute call of main/gemm.cu:37-67 (Gemm strategy,
+ * main/gemm.cu:8-15) for half-precision operands; note B is taken transposed
+ * (N x K), the layout both tensor-core operands share. */
+umi_status umi_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t* err,
+                         void* stream);
+umi_status umi_gemm_f16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t* err,
+                        void* stream);
+/* FP32 GEMM emulated on the bf16 tensor cores by operand splitting (bf16x3:
+ * A = A_hi + A_lo, B = B_hi + B_lo, C = A_hi B_hi + A_lo B_hi + A_hi B_lo, fp32
+ * accumulation; Henry, Tang & Heinecke, ARITH 2019).  A is (M,K), B is (N,K),
+ * both fp32 row-major.  Needs a workspace of
+ * umi_gemm_f32_bf16x3_workspace_bytes(M, N, K) bytes (256-byte aligned) for the
+ * split operands. */
+size_t umi_gemm_f32_bf16x3_workspace_bytes(int32_t M, int32_t N, int32_t K);
+umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float* C, int32_t M, int32_t N, int32_t K,
+                               void* workspace, size_t workspace_bytes, int32_t* err, void* stream);
+
 /* ---- batched launches: many images of uneven sizes in one persistent
  * launch.  The image table is copied into the launch (no device allocation);
  * CTAs walk a prefix-summed queue of tiles across all images.  `variant`

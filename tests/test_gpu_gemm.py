@@ -1,0 +1,56 @@
+"""GPU parity tests of the tcgen05 GEMM (through the C ABI) against the FP64 CPU oracle.
+
+bf16/f16: the oracle multiplies the same rounded inputs in FP64; the tensor
+cores multiply exactly and accumulate in FP32, so |C - C64| <= 1e-5 * sum_k |a b|.
+bf16x3 (fp32 inputs): the split keeps ~16 significant bits per operand, so
+|C - C64| <= 1e-4 * sum_k |a b| against the FP64 product of the fp32 inputs.
+Every test also checks that no bounded device wait gave up (err word stays 0).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(got, want, scale, tol):
+    err = np.abs(got - want) / np.maximum(scale, 1e-30)
+    assert err.max() <= tol, err.max()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 1024), (128, 256, 8), (200, 300, 72), (1, 1, 16),
+                                   (384, 256, 4096), (130, 520, 136)])
+@pytest.mark.parametrize("dt", ["bf16", "f16"])
+def test_gemm_half(umi, orc, dev, M, N, K, dt):
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(M * 7 + N + K)
+    tdt = torch.bfloat16 if dt == "bf16" else torch.float16
+    A = torch.randn(M, K, generator=g).to(tdt)
+    B = torch.randn(N, K, generator=g).to(tdt)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    C = umi.gemm(A.to(dev), B.to(dev), err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    a, b = A.float().numpy(), B.float().numpy()
+    want = orc.gemm_f64(a, b, b_is_nk=True)
+    scale = orc.gemm_f64(np.abs(a), np.abs(b), b_is_nk=True)
+    _check(C, want, scale, 1e-5)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 256, 1024), (200, 136, 48)])
+def test_gemm_f32_bf16x3(umi, orc, dev, M, N, K):
+    import torch
+    g = np.random.default_rng(M + N + K)
+    a = g.standard_normal((M, K)).astype(np.float32)
+    b = g.standard_normal((N, K)).astype(np.float32)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    C = umi.gemm_f32_bf16x3(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev), err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    want = orc.gemm_f64(a, b, b_is_nk=True)
+    scale = orc.gemm_f64(np.abs(a), np.abs(b), b_is_nk=True)
+    _check(C, want, scale, 1e-4)
+
+
+def test_gemm_rejects(umi, dev):
+    import torch
+    A = torch.zeros(128, 12, dtype=torch.bfloat16, device=dev)
+    with pytest.raises(umi.UmiError):
+        umi.gemm(A, A)  # K = 12 is not a multiple of 8

@@ -59,6 +59,10 @@ SIGNATURES = {
     "umi_bilateral_f32": ([_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp], ctypes.c_int),
     "umi_wfilter3x3_pp_f32": ([_vp, _vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_cost_volume_dot_f32": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
+    "umi_gemm_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_gemm_f16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_gemm_f32_bf16x3_workspace_bytes": ([_i32, _i32, _i32], _sz),
+    "umi_gemm_f32_bf16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _sz, _vp, _vp], ctypes.c_int),
     "umi_batch_variants": ([_i32], _i32),
     "umi_batch_run": ([_i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
     "umi_autotune_batch": ([_i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
@@ -348,3 +352,38 @@ def autotune_batch(op, images, params=None, reps=3, stream=None):
     check(lib().umi_autotune_batch(op, tab, len(images), ctypes.byref(prm), reps, ctypes.byref(v), ctypes.byref(ms),
                                    _stream_ptr(stream)), "umi_autotune_batch")
     return v.value, ms.value
+
+
+# ---- tensor-core GEMM ----
+
+def gemm(A, B, out=None, err=None, stream=None):
+    """C = A @ B.T on the tensor cores: A (M,K), B (N,K) bf16 or f16 CUDA tensors -> fp32 (M,N)."""
+    import torch
+    if A.dtype not in (torch.bfloat16, torch.float16) or B.dtype != A.dtype:
+        raise TypeError("A and B must both be bfloat16 or both float16")
+    _need(A, A.dtype, "A")
+    _need(B, B.dtype, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    if B.shape[1] != K:
+        raise ValueError("B must be (N, K)")
+    out = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    _need(out, torch.float32, "out")
+    fn = lib().umi_gemm_bf16 if A.dtype == torch.bfloat16 else lib().umi_gemm_f16
+    check(fn(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(err), _stream_ptr(stream)), fn.__name__)
+    return out
+
+
+def gemm_f32_bf16x3(A, B, out=None, workspace=None, err=None, stream=None):
+    """C = A @ B.T for fp32 A (M,K), B (N,K) via bf16x3 split precision on the tensor cores."""
+    import torch
+    _need(A, torch.float32, "A")
+    _need(B, torch.float32, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    out = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    nb = int(lib().umi_gemm_f32_bf16x3_workspace_bytes(M, N, K))
+    workspace = torch.empty(max(nb, 256), dtype=torch.uint8, device=A.device) if workspace is None else workspace
+    check(lib().umi_gemm_f32_bf16x3(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(workspace), workspace.numel(),
+                                    _ptr(err), _stream_ptr(stream)), "umi_gemm_f32_bf16x3")
+    return out
