@@ -39,7 +39,8 @@ L2_BYTES = 129 * 2 ** 20
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
 # from the ncu capture summarised under profiles/ (None until captured).
-NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None, "gemm_4096": None}
+NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None, "gemm_4096": None,
+               "fprop_n32": None}
 
 
 def parse():
@@ -48,14 +49,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096"],
+    ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096",
+                                           "fprop_n32"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
-                   "gemm_4096": 3000}[a.workload]
+                   "gemm_4096": 3000, "fprop_n32": 3000}[a.workload]
     return a
 
 
@@ -543,7 +545,85 @@ class Gemm:
         return 2.0 * rows * self.N * self.K / 1e12
 
 
-WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm}
+class Fprop:
+    """Convolution forward pass N=32, C=64, H=W=128, K=128, 3x3, stride 1,
+    pad 1: bf16 NHWC input ~ N(0,1), bf16 KRSC weights ~ N(0, 1/576), fp32
+    accumulation and NCHW fp32 output (implicit GEMM on the tensor cores)."""
+    name = "fprop_n32"
+    metric = "fprop TFLOP/s (N32 C64 128x128 K128 3x3, bf16 in, fp32 accumulate)"
+    unit = "TFLOP/s"
+    dtype = "bf16"
+    N, C, H, W, K, R = 32, 64, 128, 128, 128, 3
+
+    def __init__(self, seed=13, **_):
+        self.seed = seed
+        self.flops = 2.0 * self.N * self.K * self.H * self.W * self.C * self.R * self.R
+
+    def config(self):
+        return {"workload": self.name, "N": self.N, "C": self.C, "H": self.H, "W": self.W, "K": self.K,
+                "filter": "3x3 s1 p1", "layout": "x NHWC bf16, w KRSC bf16, out NCHW fp32",
+                "l2": "4 rotating input/output sets (>= 1 GB)"}
+
+    def units_per_step(self):
+        return self.flops / 1e12
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        self.U = U
+        gen = torch.Generator(device=dev).manual_seed(self.seed)
+        x = torch.randn((self.N, self.H, self.W, self.C), generator=gen, device=dev).to(torch.bfloat16)
+        w = (torch.randn((self.K, self.R, self.R, self.C), generator=gen, device=dev) / 24.0).to(torch.bfloat16)
+        self.n_rot = 4
+        self.x = [x.clone() for _ in range(self.n_rot)]
+        self.w = w
+        self.out = [torch.empty((self.N, self.K, self.H, self.W), device=dev) for _ in range(self.n_rot)]
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.launches_per_step = 1
+        self.hx = x.cpu().pin_memory()
+        self.hout = torch.empty((self.N, self.K, self.H, self.W)).pin_memory()
+
+    def step(self, i):
+        k = i % self.n_rot
+        self.U.conv2d_fprop_bf16(self.x[k], self.w, out=self.out[k], err=self.err)
+
+    def step_e2e(self, i):
+        k = i % self.n_rot
+        self.x[k].copy_(self.hx, non_blocking=True)
+        self.U.conv2d_fprop_bf16(self.x[k], self.w, out=self.out[k], err=self.err)
+        self.hout.copy_(self.out[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return 2 * self.N * self.H * self.W * self.C, 4 * self.N * self.K * self.H * self.W
+
+    def check(self):
+        import torch
+        xd = self.x[0][:2].permute(0, 3, 1, 2).double()
+        wd = self.w.permute(0, 3, 1, 2).double()
+        ref = torch.nn.functional.conv2d(xd, wd, padding=1)
+        scale = torch.nn.functional.conv2d(xd.abs(), wd.abs(), padding=1)
+        d = (self.out[0][:2].double() - ref).abs()
+        return {"max_err_over_scale": float((d / scale.clamp_min(1e-30)).max()), "max_abs": float(d.max()),
+                "rms_abs": float(d.pow(2).mean().sqrt()), "images_checked": 2, "err_word": int(self.err.item())}
+
+    def kernels(self, dev, peaks, n=30):
+        return {"conv2d_fprop_bf16": time_launches(self.step, self.n_rot, n)}, None, None
+
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+        g = np.random.default_rng(1)
+        self.hxn = g.standard_normal((1, self.C, self.H, self.W)).astype(np.float32)
+        self.hwn = (g.standard_normal((self.K, self.C, self.R, self.R)) / 24.0).astype(np.float32)
+
+    def cpu_step(self, rows, threads):
+        """The reference's direct convolution loop (main/fprop.cu:84-108, FP64) on `rows` output rows of one image."""
+        self.orc.conv2d_f64(np.ascontiguousarray(self.hxn[:, :, :rows + 2]), self.hwn, 1, 1, threads=threads)
+        return 2.0 * self.K * (rows + 2) * self.W * self.C * 9 / 1e12
+
+
+WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm,
+             "fprop_n32": Fprop}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -705,6 +785,14 @@ def run_ours(args, wl, dist):
         roof = dict(kernels["gemm_bf16"], bound="tensor", kernel="gemm_tc_kernel (bf16)", peak=pk["bf16_tflops"],
                     traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
                     flops_per_launch=wl.flops)
+    elif isinstance(wl, Fprop):
+        kt = kms["conv2d_fprop_bf16"]
+        ach = wl.flops / (kt * 1e-3) / 1e12
+        kernels["conv2d_fprop_bf16"] = {"ms_per_launch": kt, "achieved": ach, "unit": "TFLOP/s",
+                                        "frac": ach / pk["bf16_tflops"]}
+        roof = dict(kernels["conv2d_fprop_bf16"], bound="tensor", kernel="tc_kernel<conv> (bf16)",
+                    peak=pk["bf16_tflops"], traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
+                    flops_per_launch=wl.flops)
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
             b = wl.BYTES[name] * wl.px
@@ -732,7 +820,8 @@ def run_ours(args, wl, dist):
         "impl": "ours",
     }
     if sanity is not None:
-        key = {IntPair: "sanity_true_mv_recovered", Gemm: "errors_vs_fp64_sampled_rows"}.get(type(wl),
+        key = {IntPair: "sanity_true_mv_recovered", Gemm: "errors_vs_fp64_sampled_rows",
+               Fprop: "errors_vs_fp64"}.get(type(wl),
                                                                                            "sanity_max_rel_err_sampled")
         line[key] = sanity
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -746,6 +835,8 @@ def cpu_baseline(wl, sample_s=10.0):
     wl.cpu_setup()
     if isinstance(wl, IntPair):
         chunk, what = 256, "random blocks of the 1080p pair, +-32 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin, plus the matching rows of iimg (main/iimg.cu:100-111)"
+    elif isinstance(wl, Fprop):
+        chunk, what = 8, "output rows of one 64-channel 128x128 image through the reference's direct convolution loop (main/fprop.cu:84-108), FP64"
     elif isinstance(wl, Gemm):
         chunk, what = 4, "rows of the 4096^3 product, the reference's gemm loop (main/gemm.cu:69-78) with FP64 accumulation"
     elif isinstance(wl, Batched):
@@ -768,7 +859,7 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = {IntPair: 32, Batched: 2, Gemm: 2}.get(type(wl), 16)
+    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2}.get(type(wl), 16)
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()

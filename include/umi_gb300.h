@@ -219,6 +219,16 @@ size_t umi_gemm_f32_bf16x3_workspace_bytes(int32_t M, int32_t N, int32_t K);
 umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float* C, int32_t M, int32_t N, int32_t K,
                                void* workspace, size_t workspace_bytes, int32_t* err, void* stream);
 
+/* Convolution forward pass on the tensor cores (implicit GEMM, tcgen05):
+ * out[n,k,y,x] = sum_{c,dy,dx} w[k,dy,dx,c] * in[n,y+dy-r/2,x+dx-r/2,c], stride
+ * 1, zero padding r/2 (same size output).  in is NHWC bf16, w is KRSC bf16,
+ * out is NCHW fp32 (fp32 accumulation).  c a multiple of 64, r in {1,3,5,7},
+ * 16-byte aligned inputs.  `err` as for umi_gemm_bf16.  The tensor-core form
+ * of the direct convolution of main/fprop.cu:53-82 (Gemm strategy over
+ * (N, K, OH, OW) x (C, R, S); there int32, stride 2, 7x7). */
+umi_status umi_conv2d_fprop_bf16(const void* x_nhwc, const void* w_krsc, float* out_nchw, int32_t n, int32_t c,
+                                 int32_t h, int32_t w, int32_t k, int32_t r, int32_t* err, void* stream);
+
 /* ---- batched launches: many images of uneven sizes in one persistent
  * launch.  The image table is copied into the launch (no device allocation);
  * CTAs walk a prefix-summed queue of tiles across all images.  `variant`

@@ -54,3 +54,42 @@ def test_gemm_rejects(umi, dev):
     A = torch.zeros(128, 12, dtype=torch.bfloat16, device=dev)
     with pytest.raises(umi.UmiError):
         umi.gemm(A, A)  # K = 12 is not a multiple of 8
+
+
+# ---------------------------------------------------------------- conv fprop (implicit GEMM)
+def _conv_case(n, c, h, w, k, r, seed):
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    x = torch.randn(n, c, h, w, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(k, c, r, r, generator=g) / (r * (c ** 0.5))).to(torch.bfloat16)
+    return x, wt
+
+
+@pytest.mark.parametrize("n,c,h,w,k,r", [(2, 64, 16, 16, 128, 3), (1, 128, 5, 130, 64, 3), (1, 64, 7, 9, 128, 1),
+                                         (1, 64, 9, 20, 200, 5), (1, 64, 1, 1, 128, 3), (3, 64, 33, 128, 128, 3)])
+def test_conv2d_fprop_bf16(umi, orc, dev, n, c, h, w, k, r):
+    import torch
+    x, wt = _conv_case(n, c, h, w, k, r, n * 1000 + h * 10 + k)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    got = umi.conv2d_fprop_bf16(x.permute(0, 2, 3, 1).contiguous().to(dev), wt.permute(0, 2, 3, 1).contiguous().to(dev),
+                                err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    xf, wf = x.float().numpy(), wt.float().numpy()
+    want = orc.conv2d_f64(xf, wf, 1, r // 2)
+    scale = orc.conv2d_f64(np.abs(xf), np.abs(wf), 1, r // 2)
+    _check(got, want, scale, 1e-5)
+
+
+def test_conv2d_fprop_bf16_benchmark_shape_sampled(umi, dev):
+    """N32 C64 128x128 K128 3x3: every output checked against an FP64 direct
+    convolution computed on the GPU (torch, float64) of the same bf16 inputs."""
+    import torch
+    x, wt = _conv_case(32, 64, 128, 128, 128, 3, 7)
+    xd, wd = x.to(dev), wt.to(dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    got = umi.conv2d_fprop_bf16(xd.permute(0, 2, 3, 1).contiguous(), wd.permute(0, 2, 3, 1).contiguous(), err=err)
+    assert int(err.item()) == 0
+    want = torch.nn.functional.conv2d(xd.double(), wd.double(), padding=1)
+    scale = torch.nn.functional.conv2d(xd.double().abs(), wd.double().abs(), padding=1)
+    rel = ((got.double() - want).abs() / scale.clamp_min(1e-30)).max().item()
+    assert rel <= 1e-5, rel

@@ -63,6 +63,7 @@ SIGNATURES = {
     "umi_gemm_f16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_gemm_f32_bf16x3_workspace_bytes": ([_i32, _i32, _i32], _sz),
     "umi_gemm_f32_bf16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _sz, _vp, _vp], ctypes.c_int),
+    "umi_conv2d_fprop_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_batch_variants": ([_i32], _i32),
     "umi_batch_run": ([_i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
     "umi_autotune_batch": ([_i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
@@ -386,4 +387,20 @@ def gemm_f32_bf16x3(A, B, out=None, workspace=None, err=None, stream=None):
     workspace = torch.empty(max(nb, 256), dtype=torch.uint8, device=A.device) if workspace is None else workspace
     check(lib().umi_gemm_f32_bf16x3(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(workspace), workspace.numel(),
                                     _ptr(err), _stream_ptr(stream)), "umi_gemm_f32_bf16x3")
+    return out
+
+
+def conv2d_fprop_bf16(x_nhwc, w_krsc, out=None, err=None, stream=None):
+    """Stride-1 'same' convolution on the tensor cores: x (N,H,W,C) bf16, w (K,R,R,C) bf16 -> (N,K,H,W) fp32."""
+    import torch
+    _need(x_nhwc, torch.bfloat16, "x")
+    _need(w_krsc, torch.bfloat16, "w")
+    n, h, w, c = x_nhwc.shape
+    k, r, r2, c2 = w_krsc.shape
+    if r != r2 or c2 != c:
+        raise ValueError("w must be (K, R, R, C) with the input's C")
+    out = torch.empty((n, k, h, w), dtype=torch.float32, device=x_nhwc.device) if out is None else out
+    _need(out, torch.float32, "out")
+    check(lib().umi_conv2d_fprop_bf16(_ptr(x_nhwc), _ptr(w_krsc), _ptr(out), n, c, h, w, k, r, _ptr(err),
+                                      _stream_ptr(stream)), "umi_conv2d_fprop_bf16")
     return out

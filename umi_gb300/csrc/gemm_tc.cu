@@ -28,13 +28,11 @@ namespace {
 
 using namespace umi_tc;
 
-constexpr int BM = 128, BN = 256, BK = 64;
-constexpr int STAGES = 4;
-constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2, STAGE_BYTES = A_TILE + B_TILE;
-constexpr uint32_t TMEM_COLS = 256;
+constexpr int BM = 128, BK = 64;
 constexpr int NTHREADS = 192;
-constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 
+// Tile policies: where the K-slices of A and B come from and where the
+// 128 x BN fp32 tile goes.
 struct GemmArgs {
 	float* C;
 	int M, N, K, ldc;
@@ -42,9 +40,91 @@ struct GemmArgs {
 	int* err;  // optional: error bits of bounded waits that gave up
 };
 
+// C[M,N] = A[M,K] B[N,K]^T: grid (N/BN, M/BM).
+struct GemmPolicy {
+	static constexpr int BN = 256, STAGES = 4;
+	using Args = GemmArgs;
+	struct Tile { int m0, n0; };
+	__device__ static Tile tile(const Args&) { return {(int)blockIdx.y * BM, (int)blockIdx.x * BN}; }
+	__device__ static int nk(const Args& g) { return (g.K + BK - 1) / BK; }
+	__device__ static void load(const CUtensorMap* ta, const CUtensorMap* tb, const Args&, const Tile& t, int ks,
+	                            void* a, void* b, uint64_t* bar) {
+		tma_load_2d(a, ta, bar, ks * BK, t.m0);
+		tma_load_2d(b, tb, bar, ks * BK, t.n0);
+	}
+	// this thread's row of the tile, columns [c, c+32)
+	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
+		const int row = t.m0 + rl;
+		if (row >= g.M) return;
+		float* dst = g.C + (size_t)row * g.ldc + t.n0 + c;
+		if (g.vec && t.n0 + c + 31 < g.N) {
+#pragma unroll
+			for (int i = 0; i < 32; i += 4)
+				*reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+		} else {
+#pragma unroll
+			for (int i = 0; i < 32; ++i)
+				if (t.n0 + c + i < g.N) dst[i] = v[i];
+		}
+	}
+};
+
+// 2-D convolution, stride 1, zero padding r/2, as an implicit GEMM:
+// rows = 128 output pixels of one image row (n, y, x0..x0+127), columns =
+// output channels, K = (tap, input-channel slice of 64).  A slice is one TMA
+// box of the NHWC input at (c0, x0+dx-pad, y+dy-pad, n): the box's
+// out-of-bounds zero fill is the padding.  B slices come from the KRSC
+// weights viewed as (k, r*r*c).  Output NCHW fp32.
+struct ConvArgs {
+	float* out;
+	int n, c, h, w, k, r;
+	int xtiles;
+	int* err;
+};
+struct ConvPolicy {
+	static constexpr int BN = 128, STAGES = 3;
+	using Args = ConvArgs;
+	struct Tile { int n, y, x0, k0; };
+	__device__ static Tile tile(const Args& g) {
+		const int b = blockIdx.x;
+		const int xt = b % g.xtiles, rest = b / g.xtiles;
+		return {rest / g.h, rest % g.h, xt * BM, (int)blockIdx.y * BN};
+	}
+	__device__ static int nk(const Args& g) { return g.r * g.r * (g.c / BK); }
+	__device__ static void load(const CUtensorMap* ta, const CUtensorMap* tb, const Args& g, const Tile& t, int ks,
+	                            void* a, void* b, uint64_t* bar) {
+		const int cs = g.c / BK;
+		const int tap = ks / cs, c0 = (ks - tap * cs) * BK;
+		const int dy = tap / g.r, dx = tap - dy * g.r, pad = g.r / 2;
+		tma_load_4d(a, ta, bar, c0, t.x0 + dx - pad, t.y + dy - pad, t.n);
+		tma_load_2d(b, tb, bar, tap * g.c + c0, t.k0);
+	}
+	// this thread's pixel (row rl of the tile), output channels [k0+c, +32)
+	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
+		const int x = t.x0 + rl;
+		if (x >= g.w) return;
+		const size_t plane = (size_t)g.h * g.w;
+		float* dst = g.out + ((size_t)t.n * g.k) * plane + (size_t)t.y * g.w + x;
+#pragma unroll
+		for (int i = 0; i < 32; ++i) {
+			const int kk = t.k0 + c + i;
+			if (kk < g.k) dst[(size_t)kk * plane] = v[i];
+		}
+	}
+};
+
+// One CTA computes one 128 x BN tile:
+//   warp 0, one lane : TMA producer into a STAGES-deep ring (A 16 KB, B BN*128 B);
+//   warp 1           : allocates BN TMEM columns; one lane issues tcgen05.mma
+//                      (M=128, N=BN, K=16, 4 per slice), commits each slice
+//                      back to the producer;
+//   warps 2..5       : epilogue, tcgen05.ld of their 32 TMEM lanes, stores.
+template <class P>
 __global__ void __launch_bounds__(NTHREADS, 1)
-	gemm_tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmArgs g,
-	               const uint32_t idesc) {
+	tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const typename P::Args g,
+	          const uint32_t idesc) {
+	constexpr int BN = P::BN, STAGES = P::STAGES;
+	constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2, STAGE_BYTES = A_TILE + B_TILE;
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 	uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
@@ -53,8 +133,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
 	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-	const int nk = (g.K + BK - 1) / BK;
+	const typename P::Tile t = P::tile(g);
+	const int nk = P::nk(g);
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < STAGES; ++s) {
@@ -68,7 +148,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		tma_prefetch(&tb);
 	}
 	if (warp == 1) {
-		tmem_alloc(tmem_slot, TMEM_COLS);
+		tmem_alloc(tmem_slot, BN);
 		tmem_relinquish();
 	}
 	tc_fence_before();
@@ -86,8 +166,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 			if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
 			mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
 			armed[s] = (int)round;
-			tma_load_2d(base + s * STAGE_BYTES, &ta, &full[s], ks * BK, m0);
-			tma_load_2d(base + s * STAGE_BYTES + A_TILE, &tb, &full[s], ks * BK, n0);
+			P::load(&ta, &tb, g, t, ks, base + s * STAGE_BYTES, base + s * STAGE_BYTES + A_TILE, &full[s]);
 		}
 		if (*abort_flag) {
 			// let every copy this thread started land before the CTA exits
@@ -118,23 +197,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		tc_fence_after();
 		if (ok && !*abort_flag) {
 			const int q = warp & 3;
-			const int row = m0 + 32 * q + lane;
 #pragma unroll 1
 			for (int c = 0; c < BN; c += 32) {
 				float v[32];
 				tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
-				if (row < g.M) {
-					float* dst = g.C + (size_t)row * g.ldc + n0 + c;
-					if (g.vec && n0 + c + 31 < g.N) {
-#pragma unroll
-						for (int i = 0; i < 32; i += 4)
-							*reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-					} else {
-#pragma unroll
-						for (int i = 0; i < 32; ++i)
-							if (n0 + c + i < g.N) dst[i] = v[i];
-					}
-				}
+				P::store(g, t, 32 * q + lane, c, v);
 			}
 		}
 	}
@@ -142,8 +209,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	__syncthreads();
 	if (warp == 1) {
 		tc_fence_after();
-		tmem_dealloc(tmem, TMEM_COLS);
+		tmem_dealloc(tmem, BN);
 	}
+}
+
+template <class P>
+constexpr size_t smem_bytes() {
+	return (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + 1024 + 256;
 }
 
 // ---- split of fp32 operands into bf16 hi/lo parts, concatenated along K:
@@ -205,13 +277,15 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 	const CUtensorMapDataType dt = ab_type ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 	CUtensorMap ta, tb;
 	UMI_TRY(map_kmajor(&ta, A, dt, M, K, BM));
-	UMI_TRY(map_kmajor(&tb, B, dt, N, K, BN));
+	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
 	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err};
-	UMI_TRY(umi::cuda_status(
-		cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM), "cudaFuncSetAttribute"));
-	const dim3 grid(umi::ceil_div(N, BN), umi::ceil_div(M, BM));
-	gemm_tc_kernel<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16((uint32_t)ab_type, BM, BN));
-	return umi::launch_status("gemm_tc_kernel");
+	constexpr size_t SMEM = smem_bytes<GemmPolicy>();
+	auto kern = tc_kernel<GemmPolicy>;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
+	                         "cudaFuncSetAttribute"));
+	const dim3 grid(umi::ceil_div(N, GemmPolicy::BN), umi::ceil_div(M, BM));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy::BN));
+	return umi::launch_status("tc_kernel<gemm>");
 }
 
 }  // namespace
@@ -251,5 +325,49 @@ extern "C" umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float*
 	split_bf16x3_kernel<<<1024, 256, 0, st>>>(B, Bs, N, K, 2);
 	UMI_TRY(umi::launch_status("split_bf16x3_kernel"));
 	const umi_status s = gemm_launch(As, Bs, C, M, N, 3 * K, 1, err, st);
+	return s == UMI_OK ? umi::ok() : s;
+}
+
+namespace {
+
+umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, int h, int w, int k, int r, int* err,
+                       cudaStream_t st) {
+	if (n < 0 || c < 0 || h < 0 || w < 0 || k < 0) return umi::fail(UMI_ERR_INVALID_ARG, "conv: negative size");
+	if (n == 0 || h == 0 || w == 0 || k == 0) return UMI_OK;
+	if (!x || !wt || !out) return umi::fail(UMI_ERR_INVALID_ARG, "conv: null pointer");
+	if (r != 1 && r != 3 && r != 5 && r != 7) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: filter %dx%d (1, 3, 5, 7)", r, r);
+	if (c % BK != 0) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: %d input channels (a multiple of %d)", c, BK);
+	if (!umi::aligned(x, 16) || !umi::aligned(wt, 16)) return umi::fail(UMI_ERR_INVALID_ARG, "conv: misaligned input");
+	auto enc = encode_fn();
+	if (!enc) return umi::fail(UMI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+	CUtensorMap ta, tb;
+	{
+		const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+		const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)BM, 1, 1};
+		const cuuint32_t es[4] = {1, 1, 1, 1};
+		const CUresult rr = enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
+		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "conv: input tensor map (%d)", (int)rr);
+	}
+	UMI_TRY(map_kmajor(&tb, wt, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, k, r * r * c, ConvPolicy::BN));
+	ConvArgs g{out, n, c, h, w, k, r, umi::ceil_div(w, BM), err};
+	constexpr size_t SMEM = smem_bytes<ConvPolicy>();
+	auto kern = tc_kernel<ConvPolicy>;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
+	                         "cudaFuncSetAttribute"));
+	const int64_t tiles = (int64_t)n * h * g.xtiles;
+	if (tiles > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: too many tiles");
+	const dim3 grid((unsigned)tiles, umi::ceil_div(k, ConvPolicy::BN));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvPolicy::BN));
+	return umi::launch_status("tc_kernel<conv>");
+}
+
+}  // namespace
+
+extern "C" umi_status umi_conv2d_fprop_bf16(const void* x_nhwc, const void* w_krsc, float* out_nchw, int32_t n, int32_t c,
+                                            int32_t h, int32_t w, int32_t k, int32_t r, int32_t* err, void* stream) {
+	const umi_status s = conv_launch(x_nhwc, w_krsc, out_nchw, n, c, h, w, k, r, err, umi::as_stream(stream));
 	return s == UMI_OK ? umi::ok() : s;
 }
