@@ -168,10 +168,63 @@ umi_status umi_iimg_u8_i32_noalloc(const uint8_t* in, int32_t* out, int32_t h, i
  * (dy, dx).  b in {8, 16}; 1 <= r <= 64; pitch = w. */
 umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
                           const int32_t* centers, int32_t* mv, void* stream);
+/* The same search restricted to a device-side list of blocks: searches
+ * blocks[0 .. *n_blocks) (block indices in raster order; *n_blocks is read on
+ * the device, so it may be produced by an earlier kernel on the stream) and
+ * writes their (mv_y, mv_x, sad) at their own positions of `mv`, leaving the
+ * other entries untouched.  max_blocks bounds *n_blocks (grid size). */
+umi_status umi_full_me_u8_list(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
+                               const int32_t* centers, const int32_t* blocks, const int32_t* n_blocks,
+                               int32_t max_blocks, int32_t* mv, void* stream);
 /* The same search without the argmin: writes the whole SAD volume
  * (h/b, w/b, 2r+1, 2r+1) int32, the output layout of main/full_me.cu:55-62. */
 umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
                               int32_t* sad, void* stream);
+
+/* ---- Learned motion proposal for 16x16 block motion estimation.
+ * No counterpart in the reference (its full_me, main/full_me.cu, only does
+ * exhaustive search); the exhaustive search above stays the fallback.
+ * Network: the pair (cur, ref) box-averaged 4x4 -> four 3x3 convolutions
+ * (32 channels, dilations 1, 2, 4, 8, ReLU, bf16 weights, fp32 accumulation)
+ * -> a linear head per 16x16 block over its 4x4 cells x 32 channels -> one
+ * vector (mv_y, mv_x) / 16.  Parameters are one fp32 array of
+ * umi_menet_param_count() floats: per layer the weights [cout][cin][3][3]
+ * then the biases, then the head weights [2][32*4*4] (feature index
+ * channel*16 + cell_row*4 + cell_col) and the head biases [2].
+ * Frames are h x w uint8 with h, w multiples of 16 and pitch w.  All
+ * pointers are device pointers; workspace is device memory of at least
+ * umi_menet_workspace_bytes(h, w) bytes, 256-byte aligned. */
+int32_t umi_menet_param_count(void);
+size_t umi_menet_workspace_bytes(int32_t h, int32_t w);
+/* Forward pass; keeps the activations in the workspace for
+ * umi_menet_backward.  pred (may be NULL) receives (h/16 * w/16, 2) fp32. */
+umi_status umi_menet_forward(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
+                             float* pred, void* workspace, size_t workspace_bytes, void* stream);
+/* Backward pass of the mean smooth-L1 loss between the last forward's
+ * prediction and target/16 (target: int32 vectors (mv_y, mv_x) per block at
+ * target[k*target_stride], target[k*target_stride+1]).  Writes the full
+ * gradient (param_count floats) to grads and, when loss is not NULL, the
+ * loss (one float, device). */
+umi_status umi_menet_backward(const int32_t* target, int32_t target_stride, int32_t h, int32_t w, const float* params,
+                              float* grads, float* loss, void* workspace, size_t workspace_bytes, void* stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8; step counts from 1). */
+umi_status umi_menet_adam(float* params, const float* grads, float* m, float* v, int32_t step, float lr,
+                          void* stream);
+/* Learned motion estimation: forward pass, search centres round(16 * pred)
+ * clamped to +-(full_r - refine_r), exhaustive search in +-refine_r around
+ * them.  Audit: when audit_stride > 0, blocks 0, audit_stride, 2*audit_stride,
+ * ... are also searched exhaustively in +-full_r around (0, 0); they take
+ * that exact result, and audit_sums (device, 2 x uint64, may be NULL)
+ * receives the sum over them of the refined SAD and of the exhaustive SAD
+ * (the sampled SAD regression is their ratio - 1).  Fallback: every other
+ * block whose refined SAD exceeds sad_threshold is searched exhaustively in
+ * +-full_r around (0, 0).  mv receives (mv_y, mv_x, sad) per block as
+ * umi_full_me_u8 with b = 16; n_fallback (device, may be NULL) the number of
+ * fallback blocks.  1 <= refine_r <= full_r <= 64. */
+umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
+                             int32_t refine_r, int32_t full_r, int32_t sad_threshold, int32_t audit_stride,
+                             int32_t* mv, unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,
+                             size_t workspace_bytes, void* stream);
 
 /* Bilateral filter, float32 (h, w), (2*radius+1)^2 window, radius 1..3.
  * out = sum(w*n) / sum(w) with w = exp(-(n-c)^2 / (2 sigma_r^2)) *

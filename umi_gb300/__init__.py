@@ -56,6 +56,14 @@ SIGNATURES = {
     "umi_iimg_u8_i32_noalloc": ([_vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_full_me_u8_list": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp], ctypes.c_int),
+    "umi_menet_param_count": ([], _i32),
+    "umi_menet_workspace_bytes": ([_i32, _i32], _sz),
+    "umi_menet_forward": ([_vp, _vp, _i32, _i32, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "umi_menet_backward": ([_vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "umi_menet_adam": ([_vp, _vp, _vp, _vp, _i32, _f32, _vp], ctypes.c_int),
+    "umi_me_learned_u8": ([_vp, _vp, _i32, _i32, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp],
+                          ctypes.c_int),
     "umi_bilateral_f32": ([_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp], ctypes.c_int),
     "umi_wfilter3x3_pp_f32": ([_vp, _vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_cost_volume_dot_f32": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
@@ -251,6 +259,135 @@ def full_me_u8(cur, ref, block: int = 16, search: int = 32, centers=None, out=No
     check(lib().umi_full_me_u8(_ptr(cur), _ptr(ref), h, w, block, search, _ptr(centers), _ptr(out),
                                _stream_ptr(stream)), "umi_full_me_u8")
     return out
+
+
+def full_me_u8_list(cur, ref, blocks, n_blocks, out, block: int = 16, search: int = 32, centers=None,
+                    stream=None):
+    """Full search of the listed blocks only (umi_full_me_u8_list).
+
+    blocks: int32 CUDA tensor of block indices; n_blocks: int32 CUDA tensor
+    whose first element is how many of them to search; out: the (nblk, 3)
+    int32 tensor whose listed rows are overwritten."""
+    import torch
+    _need(cur, torch.uint8, "cur")
+    _need(ref, torch.uint8, "ref")
+    _need(blocks, torch.int32, "blocks")
+    _need(n_blocks, torch.int32, "n_blocks")
+    _need(out, torch.int32, "out")
+    if centers is not None:
+        _need(centers, torch.int32, "centers")
+    h, w = cur.shape
+    check(lib().umi_full_me_u8_list(_ptr(cur), _ptr(ref), h, w, block, search, _ptr(centers), _ptr(blocks),
+                                    _ptr(n_blocks), blocks.numel(), _ptr(out), _stream_ptr(stream)),
+          "umi_full_me_u8_list")
+    return out
+
+
+class MeNet:
+    """Learned motion proposal network (umi_menet_* / umi_me_learned_u8).
+
+    Holds the fp32 parameters, Adam moments and a workspace for one frame
+    size on one CUDA device."""
+
+    def __init__(self, h: int, w: int, device="cuda", params=None, seed: int = 0):
+        import torch
+        self.h, self.w = h, w
+        self.n = param_count()
+        self.device = torch.device(device)
+        if params is None:
+            params = init_params(seed)
+        self.params = torch.as_tensor(params, dtype=torch.float32).to(self.device).contiguous()
+        if self.params.numel() != self.n:
+            raise ValueError(f"expected {self.n} parameters, got {self.params.numel()}")
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.step = 0
+        nbytes = lib().umi_menet_workspace_bytes(h, w)
+        if nbytes == 0:
+            raise ValueError(f"frame {h}x{w} unsupported (h, w must be multiples of 16)")
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        self.nblk = (h // 16) * (w // 16)
+        self.loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+
+    def forward(self, cur, ref, pred=None, stream=None):
+        import torch
+        _need(cur, torch.uint8, "cur")
+        _need(ref, torch.uint8, "ref")
+        if pred is None:
+            pred = torch.empty((self.nblk, 2), dtype=torch.float32, device=self.device)
+        check(lib().umi_menet_forward(_ptr(cur), _ptr(ref), self.h, self.w, _ptr(self.params), _ptr(pred),
+                                      _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)), "umi_menet_forward")
+        return pred
+
+    def backward(self, target, stride: int = 2, stream=None):
+        import torch
+        _need(target, torch.int32, "target")
+        check(lib().umi_menet_backward(_ptr(target), stride, self.h, self.w, _ptr(self.params), _ptr(self.grads),
+                                       _ptr(self.loss), _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)),
+              "umi_menet_backward")
+        return self.grads
+
+    def adam(self, lr: float, stream=None):
+        self.step += 1
+        check(lib().umi_menet_adam(_ptr(self.params), _ptr(self.grads), _ptr(self.m), _ptr(self.v), self.step,
+                                   lr, _stream_ptr(stream)), "umi_menet_adam")
+
+    def estimate(self, cur, ref, refine_r: int = 4, full_r: int = 64, sad_threshold: int = (1 << 31) - 1,
+                 audit_stride: int = 0, out=None, audit_sums=None, n_fallback=None, stream=None):
+        """Learned proposal + refine + audit + fallback (umi_me_learned_u8).
+
+        Returns (mv (nblk, 3) int32, audit_sums (2,) int64, n_fallback (1,) int32)."""
+        import torch
+        if out is None:
+            out = torch.empty((self.nblk, 3), dtype=torch.int32, device=self.device)
+        if audit_sums is None:
+            audit_sums = torch.zeros(2, dtype=torch.int64, device=self.device)
+        if n_fallback is None:
+            n_fallback = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _need(cur, torch.uint8, "cur")
+        _need(ref, torch.uint8, "ref")
+        check(lib().umi_me_learned_u8(_ptr(cur), _ptr(ref), self.h, self.w, _ptr(self.params), refine_r, full_r,
+                                      sad_threshold, audit_stride, _ptr(out), _ptr(audit_sums), _ptr(n_fallback),
+                                      _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)), "umi_me_learned_u8")
+        return out, audit_sums, n_fallback
+
+
+def param_count() -> int:
+    return int(lib().umi_menet_param_count())
+
+
+MENET_CH = 32
+MENET_CIN = (2, 32, 32, 32)
+MENET_DIL = (1, 2, 4, 8)
+
+
+def param_layout():
+    """Offsets of the parameter array: [(w_off, b_off) per layer], head_w_off, head_b_off, total."""
+    o = 0
+    layers = []
+    for cin in MENET_CIN:
+        wo = o
+        o += MENET_CH * cin * 9
+        layers.append((wo, o))
+        o += MENET_CH
+    wh = o
+    o += 2 * MENET_CH * 16
+    bh = o
+    o += 2
+    return layers, wh, bh, o
+
+
+def init_params(seed: int = 0):
+    """He-normal conv weights, zero biases, small head weights (numpy float32)."""
+    import numpy as np
+    g = np.random.Generator(np.random.PCG64(seed))
+    layers, wh, bh, total = param_layout()
+    p = np.zeros(total, dtype=np.float32)
+    for (wo, bo), cin in zip(layers, MENET_CIN):
+        p[wo:bo] = g.normal(0.0, np.sqrt(2.0 / (cin * 9)), size=bo - wo)
+    p[wh:bh] = g.normal(0.0, 0.01, size=bh - wh)
+    return p
 
 
 def full_me_sad_u8(cur, ref, block: int = 16, search: int = 32, out=None, stream=None):

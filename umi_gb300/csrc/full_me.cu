@@ -47,7 +47,16 @@ struct MeGeom {
 	int tasks_per_mb; // ndx * ng
 	int vec_ok;       // ref is 4-byte aligned and w % 4 == 0: word loads allowed
 	int nx32;         // largest multiple of 32 <= ndx: displacements served by whole warps
+	const int32_t* list;        // optional: search only these blocks (slot i -> block list[i])
+	const int32_t* list_count;  // number of valid slots of `list` (device word)
+	int slots;                  // slots covered by the grid (nblk, or the list's capacity)
 };
+
+// Block searched by slot `slot`, or -1 past the last slot.
+__device__ __forceinline__ int slot_block(const MeGeom& g, int slot) {
+	if (g.list) return slot < *g.list_count ? g.list[slot] : -1;
+	return slot < g.nblk ? slot : -1;
+}
 
 // Register budget per instantiation: the benchmark shape (b = 16, G = 13,
 // 352 threads) is held to 80 registers so that two CTAs (6 warps per SM
@@ -74,8 +83,8 @@ full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
 	const bool stager = row0 < rstep;  // threads past rstep*win_words idle while staging
 	// 1. Stage windows (copy 0) and current blocks.
 	for (int m = 0; m < g.m; ++m) {
-		const int blk = mb0 + m;
-		if (blk >= g.nblk) break;
+		const int blk = slot_block(g, mb0 + m);
+		if (blk < 0) break;
 		const int by = blk / g.nbx, bx = blk - by * g.nbx;
 		const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
 		const int gy0 = by * B + cy - g.r, gx0 = bx * B + cx - g.r;
@@ -114,7 +123,7 @@ full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
 	__syncthreads();
 	// 2. Shifted copies s = 1..3: word k holds bytes [4k+s, 4k+s+4) of the row.
 	for (int m = 0; m < g.m; ++m) {
-		if (mb0 + m >= g.nblk || !stager) break;
+		if (slot_block(g, mb0 + m) < 0 || !stager) break;
 		uint32_t* win = smem + m * g.mb_stride;
 		const bool last = wd0 + 1 == g.win_words;
 		for (int row = row0; row < g.win_rows; row += rstep) {
@@ -145,8 +154,8 @@ full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
 			grp = r2 / rw;
 			ix = g.nx32 + (r2 - grp * rw);
 		}
-		const int blk = mb0 + m;
-		if (blk >= g.nblk) continue;
+		const int blk = slot_block(g, mb0 + m);
+		if (blk < 0) continue;
 		const uint32_t* win = smem + m * g.mb_stride;
 		const uint32_t* cb = win + 4 * g.copy_stride;
 		const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + grp * G * g.win_words;
@@ -198,8 +207,8 @@ full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
 	if (VOLUME) return;
 	__syncthreads();
 	for (int m = tid; m < g.m; m += blockDim.x) {
-		const int blk = mb0 + m;
-		if (blk >= g.nblk) break;
+		const int blk = slot_block(g, mb0 + m);
+		if (blk < 0) break;
 		const uint32_t key = best[m];
 		const int idx = (int)(key & 0x7fffu);
 		const int iy = idx / g.ndx, ix = idx - iy * g.ndx;
@@ -233,7 +242,7 @@ umi_status launch_g(const uint8_t* cur, const uint8_t* ref, const int32_t* cente
 	// allow only one CTA per SM.
 	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
 	                                              (int)cudaSharedmemCarveoutMaxShared), "cudaFuncSetAttribute"));
-	const int grid = (g.nblk + g.m - 1) / g.m;
+	const int grid = (g.slots + g.m - 1) / g.m;
 	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
 	return umi::launch_status("full_me_kernel");
 }
@@ -250,7 +259,8 @@ umi_status launch_b(int G, const uint8_t* cur, const uint8_t* ref, const int32_t
 }
 
 umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
-                          const int32_t* centers, int32_t* out, bool volume, void* stream) {
+                          const int32_t* centers, int32_t* out, bool volume, void* stream,
+                          const int32_t* list = nullptr, const int32_t* list_count = nullptr, int32_t max_slots = 0) {
 	if (!cur || !ref || !out) return umi::fail(UMI_ERR_INVALID_ARG, "full_me: null pointer");
 	if (h < 0 || w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "full_me: negative size %dx%d", h, w);
 	if (b != 8 && b != 16) return umi::fail(UMI_ERR_UNSUPPORTED, "full_me: block size %d (supported: 8, 16)", b);
@@ -260,6 +270,10 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.nbx = w / b;
 	g.nblk = (h / b) * g.nbx;
 	if (g.nblk == 0) return umi::ok();
+	g.list = list;
+	g.list_count = list_count;
+	g.slots = list ? std::min(max_slots, g.nblk) : g.nblk;
+	if (g.slots <= 0) return umi::ok();
 	g.ndx = 2 * r + 1;
 	const int G = pick_g(g.ndx);
 	g.ng = (g.ndx + G - 1) / G;
@@ -309,4 +323,12 @@ extern "C" umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int
 extern "C" umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b,
                                          int32_t r, int32_t* sad, void* stream) {
 	return full_me_common(cur, ref, h, w, b, r, nullptr, sad, true, stream);
+}
+
+extern "C" umi_status umi_full_me_u8_list(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b,
+                                          int32_t r, const int32_t* centers, const int32_t* blocks,
+                                          const int32_t* n_blocks, int32_t max_blocks, int32_t* mv, void* stream) {
+	if (!blocks || !n_blocks) return umi::fail(UMI_ERR_INVALID_ARG, "full_me_list: null block list");
+	if (max_blocks < 0) return umi::fail(UMI_ERR_INVALID_ARG, "full_me_list: negative capacity");
+	return full_me_common(cur, ref, h, w, b, r, centers, mv, false, stream, blocks, n_blocks, max_blocks);
 }

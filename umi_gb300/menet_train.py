@@ -1,0 +1,220 @@
+"""Training, checkpointing and evaluation of the learned motion proposal.
+
+Training data: seeded synthetic 4K pairs (workloads.me_pair_cuda: blurred
+noise reference, per-block shifts round(N(0, 16^2)) clipped to +-64), each
+labelled by the plain exhaustive search (umi_full_me_u8, 16x16 blocks,
++-64) -- the labels are what the plain operator finds, not the generator's
+shifts.  Every step is one pair: umi_menet_forward, umi_menet_backward
+(mean smooth-L1 on vectors / 16), umi_menet_adam.  All arithmetic runs in
+the library's kernels; torch only holds the buffers.
+
+Checkpoint: a little-endian blob
+  magic b"UMIMENET", uint32 version (1), uint32 param_count, uint64 step,
+  float32 params[param_count], float32 adam_m[param_count], float32 adam_v[param_count]
+so that training resumes exactly where it stopped.
+
+Run `python -m umi_gb300.menet_train --pairs 2000 --out weights.bin` on a GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import struct
+import time
+
+import numpy as np
+
+from . import MeNet, full_me_u8, full_me_u8_list, init_params, param_count
+from .workloads import me_pair_cuda
+
+MAGIC = b"UMIMENET"
+VERSION = 1
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "menet_weights.bin")
+TRAIN_SEED0 = 1_000_000   # training pairs use seeds TRAIN_SEED0 + i
+EVAL_SEED0 = 9_000_000    # held-out pairs
+
+
+# ---------------------------------------------------------------- checkpoint
+def save_checkpoint(path: str, params, m=None, v=None, step: int = 0) -> None:
+    p = np.ascontiguousarray(params, dtype="<f4").ravel()
+    n = p.size
+    m = np.zeros(n, "<f4") if m is None else np.ascontiguousarray(m, dtype="<f4").ravel()
+    v = np.zeros(n, "<f4") if v is None else np.ascontiguousarray(v, dtype="<f4").ravel()
+    if m.size != n or v.size != n:
+        raise ValueError("moment arrays differ in size from the parameters")
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(MAGIC + struct.pack("<IIQ", VERSION, n, step))
+        f.write(p.tobytes() + m.tobytes() + v.tobytes())
+    os.replace(tmp, path)
+
+
+def load_checkpoint(path: str) -> dict:
+    with open(path, "rb") as f:
+        raw = f.read()
+    if raw[:8] != MAGIC:
+        raise ValueError(f"{path}: not a motion-proposal checkpoint")
+    version, n, step = struct.unpack_from("<IIQ", raw, 8)
+    if version != VERSION:
+        raise ValueError(f"{path}: checkpoint version {version}, expected {VERSION}")
+    body = np.frombuffer(raw, dtype="<f4", offset=24)
+    if body.size != 3 * n:
+        raise ValueError(f"{path}: truncated ({body.size} floats, expected {3 * n})")
+    return {"params": body[:n].astype(np.float32), "m": body[n:2 * n].astype(np.float32),
+            "v": body[2 * n:].astype(np.float32), "step": int(step)}
+
+
+def to_net(ck: dict, h: int, w: int, device="cuda") -> MeNet:
+    import torch
+    net = MeNet(h, w, device=device, params=ck["params"])
+    net.m.copy_(torch.from_numpy(ck["m"]))
+    net.v.copy_(torch.from_numpy(ck["v"]))
+    net.step = ck["step"]
+    return net
+
+
+def from_net(net: MeNet) -> dict:
+    return {"params": net.params.cpu().numpy(), "m": net.m.cpu().numpy(), "v": net.v.cpu().numpy(),
+            "step": net.step}
+
+
+def default_weights() -> np.ndarray:
+    """The committed trained parameters (init_params(0) if none were committed)."""
+    if os.path.exists(WEIGHTS):
+        return load_checkpoint(WEIGHTS)["params"]
+    return init_params(0)
+
+
+# ---------------------------------------------------------------- training
+def labels_for(cur, ref, full_r: int = 64):
+    return full_me_u8(cur, ref, 16, full_r)
+
+
+def lr_at(step: int, total: int, lr: float, warmup: int = 100) -> float:
+    if step < warmup:
+        return lr * (step + 1) / warmup
+    t = (step - warmup) / max(1, total - warmup)
+    return lr * 0.5 * (1.0 + math.cos(math.pi * min(1.0, t)))
+
+
+def train(pairs: int = 2000, epochs: int = 3, lr: float = 2e-3, h: int = 2160, w: int = 3840, seed: int = 0,
+          resume: str | None = None, log_every: int = 100, full_r: int = 64, ckpt: str | None = None) -> MeNet:
+    import torch
+    net = to_net(load_checkpoint(resume), h, w) if resume else MeNet(h, w, params=init_params(seed))
+    labels = []
+    t0 = time.time()
+    for i in range(pairs):
+        cur, ref, _ = me_pair_cuda(TRAIN_SEED0 + i, h, w)
+        labels.append(labels_for(cur, ref, full_r))
+    torch.cuda.synchronize()
+    print(json.dumps({"labels_s": round(time.time() - t0, 2), "pairs": pairs}), flush=True)
+    total = pairs * epochs
+    order = np.random.Generator(np.random.PCG64(seed)).permutation
+    t0 = time.time()
+    run = 0.0
+    for e in range(epochs):
+        for k, i in enumerate(order(pairs)):
+            step = net.step
+            if step >= total:
+                break
+            cur, ref, _ = me_pair_cuda(TRAIN_SEED0 + int(i), h, w)
+            net.forward(cur, ref)
+            net.backward(labels[int(i)], stride=3)
+            net.adam(lr_at(step, total, lr))
+            if (step + 1) % log_every == 0:
+                run = float(net.loss.item())
+                print(json.dumps({"step": step + 1, "epoch": e, "loss": round(run, 5),
+                                  "s": round(time.time() - t0, 1)}), flush=True)
+        if ckpt:
+            save_checkpoint(ckpt, **from_net(net))
+    torch.cuda.synchronize()
+    return net
+
+
+# ---------------------------------------------------------------- evaluation
+def median_predictor(mv, nby: int, nbx: int):
+    """Component-wise median of the left, top and top-right neighbours' vectors
+    (the H.264 motion-vector predictor), from a first-pass field mv (nblk, >=2)."""
+    import torch
+    f = mv[:, :2].reshape(nby, nbx, 2).float()
+    z = torch.zeros_like(f)
+    left = torch.cat([z[:, :1], f[:, :-1]], dim=1)
+    top = torch.cat([z[:1], f[:-1]], dim=0)
+    tr = torch.cat([z[:1], torch.cat([f[:-1, 1:], z[:-1, :1]], dim=1)], dim=0)
+    med = torch.stack([left, top, tr], dim=0).median(dim=0).values
+    return med.round().to(torch.int32).reshape(-1, 2).contiguous()
+
+
+def evaluate(net: MeNet, seeds, refine_r: int = 4, full_r: int = 64, sad_threshold: int | None = None,
+             audit_stride: int = 64):
+    """Per-method statistics on the given pairs against exhaustive search.
+
+    Methods: learned (proposal + refine, then audit + fallback), zero-MV + refine,
+    neighbour-median + refine (each with the same fallback threshold)."""
+    import torch
+    out = {"learned": [], "zero": [], "median": []}
+    nby, nbx = net.h // 16, net.w // 16
+    for s in seeds:
+        cur, ref, _ = me_pair_cuda(int(s), net.h, net.w)
+        full = full_me_u8(cur, ref, 16, full_r)
+        fsad = full[:, 2].long()
+        thr = sad_threshold if sad_threshold is not None else threshold_from(full)
+        # proposals without fallback: how often the refine window holds the optimum
+        mv_l, sums, nf = net.estimate(cur, ref, refine_r, full_r, sad_threshold=(1 << 31) - 1, audit_stride=0)
+        cand = {"learned": mv_l.clone(), "zero": full_me_u8(cur, ref, 16, refine_r)}
+        cand["median"] = full_me_u8(cur, ref, 16, refine_r, centers=median_predictor(cand["zero"], nby, nbx))
+        for name, mv in cand.items():
+            hit = (mv[:, 2].long() == fsad).float().mean().item()
+            bad = (mv[:, 2] > thr).nonzero().flatten().to(torch.int32)
+            nb = torch.tensor([bad.numel()], dtype=torch.int32, device=mv.device)
+            fixed = mv.clone()
+            if bad.numel():
+                full_me_u8_list(cur, ref, bad, nb, fixed, 16, full_r)
+            reg_before = (mv[:, 2].long().sum() / fsad.sum()).item() - 1.0
+            reg_after = (fixed[:, 2].long().sum() / fsad.sum()).item() - 1.0
+            out[name].append({"hit": hit, "fallback_frac": bad.numel() / mv.shape[0], "sad_reg_no_fallback": reg_before,
+                              "sad_reg": reg_after, "threshold": thr})
+        # the whole learned path through the one entry point, with the audit
+        mv_a, sums, nf = net.estimate(cur, ref, refine_r, full_r, sad_threshold=thr, audit_stride=audit_stride)
+        a = sums.cpu().numpy()
+        out["learned"][-1].update({
+            "entry_sad_reg": (mv_a[:, 2].long().sum() / fsad.sum()).item() - 1.0,
+            "entry_fallback": int(nf.item()),
+            "audit_sad_reg": float(a[0]) / max(float(a[1]), 1.0) - 1.0})
+    return {k: {f: float(np.mean([r[f] for r in v])) for f in v[0]} for k, v in out.items()}
+
+
+def threshold_from(full) -> int:
+    """SAD threshold for the fallback: 1.5 x the 99th percentile of the optimal SADs."""
+    s = full[:, 2].float()
+    return int(1.5 * torch_quantile(s, 0.99))
+
+
+def torch_quantile(x, q: float) -> float:
+    k = max(0, min(x.numel() - 1, int(round(q * (x.numel() - 1)))))
+    return float(x.sort().values[k].item())
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--pairs", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--height", type=int, default=2160)
+    ap.add_argument("--width", type=int, default=3840)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--resume", default=None)
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-pairs", type=int, default=4)
+    a = ap.parse_args(argv)
+    net = train(a.pairs, a.epochs, a.lr, a.height, a.width, a.seed, a.resume, ckpt=a.out)
+    save_checkpoint(a.out, **from_net(net))
+    if a.eval_pairs:
+        r = evaluate(net, range(EVAL_SEED0, EVAL_SEED0 + a.eval_pairs))
+        print(json.dumps({"eval": r}), flush=True)
+
+
+if __name__ == "__main__":
+    main()

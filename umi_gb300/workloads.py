@@ -75,3 +75,43 @@ def me_pair(seed: int = 3, h: int = 1080, w: int = 1920, block: int = 16, shift_
     b = np.clip(np.rint(b), 0, 255).astype(np.uint8)
     true_mv = sh[:nby, :nbx].reshape(-1, 2).astype(np.int32)
     return b, a, true_mv
+
+
+def me_pair_cuda(seed: int, h: int = 2160, w: int = 3840, block: int = 16, shift_sigma: float = 16.0,
+                 max_shift: int = 64, noise_sigma: float = 2.0, blur_sigma: float = 2.0, device="cuda"):
+    """me_pair's distribution drawn on the GPU (torch's Philox generator, seeded).
+
+    Same construction as me_pair (blurred N(128, 40^2) reference, per-block
+    shifts round(N(0, shift_sigma^2)) clipped to +-max_shift, edge-clamped
+    gather, N(0, noise_sigma^2) noise); the random streams differ from
+    numpy's, so the frames are not me_pair's frames.  Used where thousands
+    of 4K pairs are needed (training the motion-proposal network).
+    Returns (cur, ref, true_mv) as CUDA tensors (uint8, uint8, int32 (nblk, 2)).
+    """
+    import torch
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    a = torch.normal(128.0, 40.0, size=(h, w), generator=g, device=dev)
+    r = int(np.ceil(3 * blur_sigma))
+    t = torch.arange(-r, r + 1, dtype=torch.float64, device=dev)
+    k = torch.exp(-t * t / (2 * blur_sigma * blur_sigma))
+    k = (k / k.sum()).float()
+    x = torch.nn.functional.pad(a[None, None], (r, r, 0, 0), mode="replicate")
+    x = torch.nn.functional.conv2d(x, k.view(1, 1, 1, -1))
+    x = torch.nn.functional.pad(x, (0, 0, r, r), mode="replicate")
+    x = torch.nn.functional.conv2d(x, k.view(1, 1, -1, 1))[0, 0]
+    ref = x.round().clamp(0, 255).to(torch.uint8)
+    nby, nbx = max(h // block, 1), max(w // block, 1)
+    sh = torch.normal(0.0, shift_sigma, size=(nby, nbx, 2), generator=g, device=dev)
+    sh = sh.round().clamp(-max_shift, max_shift).to(torch.int64)
+    by = torch.clamp(torch.arange(h, device=dev) // block, max=nby - 1)
+    bx = torch.clamp(torch.arange(w, device=dev) // block, max=nbx - 1)
+    sy = sh[by[:, None], bx[None, :], 0]
+    sx = sh[by[:, None], bx[None, :], 1]
+    yy = torch.clamp(torch.arange(h, device=dev)[:, None] + sy, 0, h - 1)
+    xx = torch.clamp(torch.arange(w, device=dev)[None, :] + sx, 0, w - 1)
+    b = ref[yy, xx].float() + torch.normal(0.0, noise_sigma, size=(h, w), generator=g, device=dev)
+    cur = b.round().clamp(0, 255).to(torch.uint8)
+    true_mv = sh[:h // block, :w // block].reshape(-1, 2).to(torch.int32).contiguous()
+    return cur.contiguous(), ref.contiguous(), true_mv
