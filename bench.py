@@ -40,7 +40,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
 # from the ncu capture summarised under profiles/ (None until captured).
 NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": None, "batched_uneven": None, "gemm_4096": None,
-               "fprop_n32": None}
+               "fprop_n32": None, "learned_me_4k": None}
 
 
 def parse():
@@ -50,14 +50,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096",
-                                           "fprop_n32"],
+                                           "fprop_n32", "learned_me_4k"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
-                   "gemm_4096": 3000, "fprop_n32": 3000}[a.workload]
+                   "gemm_4096": 3000, "fprop_n32": 3000, "learned_me_4k": 200}[a.workload]
     return a
 
 
@@ -622,8 +622,120 @@ class Fprop:
         return 2.0 * self.K * (rows + 2) * self.W * self.C * 9 / 1e12
 
 
+class LearnedMe:
+    """Learned motion proposal on 3840x2160 u8 pairs (per-block shifts
+    round(N(0, 16^2)) clipped to +-64, 16x16 blocks): proposal network,
+    +-4 refine, audit of every 64th block by +-64 exhaustive search,
+    fallback to +-64 exhaustive search above the SAD threshold
+    (umi_me_learned_u8).  The plain +-64 exhaustive search on the same pairs
+    is timed beside it (kernels.full_me_u8_r64)."""
+    name = "learned_me_4k"
+    metric = "learned ME Mblocks/s (4K, +-64 judge, +-4 refine, <= 1% mean SAD regression)"
+    unit = "Mblocks/s"
+    dtype = "u8 (search), bf16 weights / fp32 accumulation (network)"
+    H, W, B, FULL_R, REFINE_R, AUDIT = 2160, 3840, 16, 64, 4, 64
+    data = "synthetic (seeded torch Philox generator on the GPU; the network's weights trained on 2000 such pairs)"
+
+    def __init__(self, seed=0, **_):
+        self.nblk = (self.H // self.B) * (self.W // self.B)
+
+    def config(self):
+        return {"workload": self.name, "frame": f"{self.W}x{self.H} u8", "block": self.B,
+                "shifts": "round(N(0,16^2)) per block, clipped +-64", "judge": f"+-{self.FULL_R} exhaustive",
+                "refine": f"+-{self.REFINE_R}", "audit": f"every {self.AUDIT}th block",
+                "threshold": "1.5 x p99 of the optimal SAD of a calibration pair",
+                "network": "4 x conv3x3 32ch dil 1,2,4,8 + per-block linear head, trained on 2000 pairs",
+                "l2": "16 distinct pairs rotated (265 MB > L2)"}
+
+    def units_per_step(self):
+        return self.nblk / 1e6
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        from umi_gb300 import menet_train as T
+        from umi_gb300.workloads import me_pair_cuda
+        self.U, self.T = U, T
+        self.n_rot = 16
+        pairs = [me_pair_cuda(T.EVAL_SEED0 + k, self.H, self.W, device=dev) for k in range(self.n_rot)]
+        self.d_cur = [p[0] for p in pairs]
+        self.d_ref = [p[1] for p in pairs]
+        self.net = U.MeNet(self.H, self.W, device=dev, params=T.default_weights())
+        self.trained = os.path.exists(T.WEIGHTS)
+        self.full0 = U.full_me_u8(self.d_cur[0], self.d_ref[0], self.B, self.FULL_R)
+        self.thr = T.threshold_from(self.full0)
+        self.d_mv = [torch.empty((self.nblk, 3), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
+        self.d_sums = [torch.zeros(2, dtype=torch.int64, device=dev) for _ in range(self.n_rot)]
+        self.d_nf = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
+        self.h_cur = self.d_cur[0].cpu().pin_memory()
+        self.h_ref = self.d_ref[0].cpu().pin_memory()
+        self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
+        # forward (7) + centres + refine + audit list + audit search + memset x2 + flag + fallback + count copy
+        self.launches_per_step = 15
+
+    def _estimate(self, k):
+        self.net.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
+                          out=self.d_mv[k], audit_sums=self.d_sums[k], n_fallback=self.d_nf[k])
+
+    def step(self, i):
+        self._estimate(i % self.n_rot)
+
+    def step_e2e(self, i):
+        k = i % self.n_rot
+        self.d_cur[k].copy_(self.h_cur, non_blocking=True)
+        self.d_ref[k].copy_(self.h_ref, non_blocking=True)
+        self._estimate(k)
+        self.h_mv.copy_(self.d_mv[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return 2 * self.H * self.W, 12 * self.nblk
+
+    def check(self):
+        """Quality of the timed results against exhaustive search, plus the ablation."""
+        import torch
+        regs, fbs = [], []
+        for k in range(2):
+            full = self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.FULL_R)
+            self._estimate(k)
+            regs.append((self.d_mv[k][:, 2].long().sum() / full[:, 2].long().sum()).item() - 1.0)
+            fbs.append(int(self.d_nf[k].item()) / self.nblk)
+        ab = self.T.evaluate(self.net, [self.T.EVAL_SEED0 + 2], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT)
+        return {"mean_sad_regression": float(np.mean(regs)), "fallback_fraction": float(np.mean(fbs)),
+                "sad_threshold": self.thr, "trained_weights": self.trained,
+                "ablation_hit_rate_within_refine": {m: ab[m]["hit"] for m in ab},
+                "ablation_fallback_fraction": {m: ab[m]["fallback_frac"] for m in ab},
+                "ablation_sad_regression_without_fallback": {m: ab[m]["sad_reg_no_fallback"] for m in ab}}
+
+    def kernels(self, dev, peaks, n=20):
+        R = self.n_rot
+        fns = {
+            "me_learned_u8": self.step,
+            "full_me_u8_r64": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.FULL_R,
+                                                          out=self.d_mv[i % R]),
+            "menet_forward": lambda i: self.net.forward(self.d_cur[i % R], self.d_ref[i % R]),
+            "refine_r4": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.REFINE_R,
+                                                     out=self.d_mv[i % R]),
+        }
+        out = {name: time_launches(fn, R, n) for name, fn in fns.items()}
+        absdiff = self.nblk * (2 * self.FULL_R + 1) ** 2 * self.B * self.B
+        return out, absdiff, None
+
+    def cpu_setup(self):
+        import oracle
+        from umi_gb300.workloads import me_pair
+        self.orc = oracle
+        self.rng = np.random.default_rng(0)
+        # the reference's CPU path is the exhaustive search; a 4K numpy pair of the same distribution
+        self.hc, self.hr, _ = me_pair(seed=5, h=self.H, w=self.W, block=self.B, shift_sigma=16.0, max_shift=64)
+
+    def cpu_step(self, nblocks, threads):
+        blocks = self.rng.choice(self.nblk, size=nblocks, replace=False).astype(np.int32)
+        self.orc.ref_full_me_u8_argmin(self.hc, self.hr, self.B, self.FULL_R, blocks, threads=threads)
+        return nblocks / 1e6
+
+
 WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm,
-             "fprop_n32": Fprop}
+             "fprop_n32": Fprop, "learned_me_4k": LearnedMe}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -793,6 +905,17 @@ def run_ours(args, wl, dist):
         roof = dict(kernels["conv2d_fprop_bf16"], bound="tensor", kernel="tc_kernel<conv> (bf16)",
                     peak=pk["bf16_tflops"], traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
                     flops_per_launch=wl.flops)
+    elif isinstance(wl, LearnedMe):
+        sad_peak = probe_sad4_peak(dev)
+        for name, kt in kms.items():
+            kernels[name] = {"ms_per_launch": kt, "Mblocks_per_s": wl.nblk / (kt * 1e-3) / 1e6}
+        kernels["speedup_learned_vs_full_search"] = kms["full_me_u8_r64"] / kms["me_learned_u8"]
+        ach = absdiff / (kms["full_me_u8_r64"] * 1e-3)
+        roof = {"bound": "int", "kernel": "full_me_u8 +-64 (judge and fallback)", "achieved": ach / 1e9,
+                "peak": sad_peak / 1e9, "unit": "Gabsdiff/s", "frac": ach / sad_peak,
+                "traffic": NCU_TRAFFIC[wl.name],
+                "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
+                "work_per_launch": absdiff, "ms_per_launch": kms["full_me_u8_r64"]}
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
             b = wl.BYTES[name] * wl.px
@@ -811,7 +934,7 @@ def run_ours(args, wl, dist):
     line = {
         "metric": wl.metric, "value": value, "unit": wl.unit, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded numpy generators)",
+        "vs_baseline": None, "dtype": wl.dtype, "data": getattr(wl, "data", "synthetic (seeded numpy generators)"),
         "config": dict(wl.config(), parallelism=f"replicas x{dist.world}"),
         "e2e": {"value": e2e_value, "unit": wl.unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e / e2e_steps, "steps": e2e_steps},
@@ -821,7 +944,7 @@ def run_ours(args, wl, dist):
     }
     if sanity is not None:
         key = {IntPair: "sanity_true_mv_recovered", Gemm: "errors_vs_fp64_sampled_rows",
-               Fprop: "errors_vs_fp64"}.get(type(wl),
+               Fprop: "errors_vs_fp64", LearnedMe: "quality_vs_exhaustive_search"}.get(type(wl),
                                                                                            "sanity_max_rel_err_sampled")
         line[key] = sanity
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -833,7 +956,9 @@ def cpu_baseline(wl, sample_s=10.0):
     """The reference's CPU loop (oracle restatement) on a bounded sample, all host threads."""
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    if isinstance(wl, IntPair):
+    if isinstance(wl, LearnedMe):
+        chunk, what = 8, "random blocks of a 4K pair, +-64 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin (the reference has no learned path)"
+    elif isinstance(wl, IntPair):
         chunk, what = 256, "random blocks of the 1080p pair, +-32 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin, plus the matching rows of iimg (main/iimg.cu:100-111)"
     elif isinstance(wl, Fprop):
         chunk, what = 8, "output rows of one 64-channel 128x128 image through the reference's direct convolution loop (main/fprop.cu:84-108), FP64"
@@ -859,7 +984,7 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2}.get(type(wl), 16)
+    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2, LearnedMe: 8}.get(type(wl), 16)
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()
@@ -874,7 +999,7 @@ def run_reference(args, wl, dist):
         "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded numpy generators)",
         "config": dict(wl.config(), parallelism="host cores"), "impl": "reference",
         "cpu_baseline": {"value": v, "unit": wl.unit, "cores": threads, "kind": "port",
-                         "sample": f"{per_step} {'blocks' if isinstance(wl, IntPair) else 'rows'} per step"},
+                         "sample": f"{per_step} {'blocks' if isinstance(wl, (IntPair, LearnedMe)) else 'rows'} per step"},
         "e2e": {"value": v, "unit": wl.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }

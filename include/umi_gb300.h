@@ -122,6 +122,34 @@ typedef struct {
  * returning UMI_ERR_INVALID_DESC. */
 umi_status umi_plan_build(const umi_desc* desc, umi_plan* plan);
 
+/* The same validation into a plan allocated by the library (host memory,
+ * released by umi_plan_destroy).  Reference: the descriptor half of
+ * Execute, src/UMI_gpu.h:423-609. */
+umi_status umi_plan_create(const umi_desc* desc, umi_plan** plan);
+void umi_plan_destroy(umi_plan* plan);
+
+/* Strategies built into umi_launch: the functors of the reference's example
+ * applications, same arithmetic, element type and constants. */
+typedef enum umi_strategy {
+	UMI_STRATEGY_NEIGHBOUR_SUM_I32 = 0,  /* main/filter3x3.cu:10-17: Pre t = init; Loop(1 in) t += x; Post out = t * mul; constants {int init, mul} */
+	UMI_STRATEGY_WEIGHTED_SUM_I32 = 1,   /* main/wfilter3x3.cu:8-15: Pre t = init; Loop(2 in) t += x * w; Post out = t; constants {int init} */
+	UMI_STRATEGY_RANGE_WEIGHTED_F32 = 2, /* main/bilateral.cu:9-24: Pre(1 in) centre; Loop(3 in) w = expf((x-centre)^2 * norm) * ws_y * ws_x; Post out = sum(w x) / sum(w); constants {float norm} */
+	UMI_STRATEGY_ABS_DIFF_SUM_I32 = 3,   /* main/cost_volume.cu:8-15 and main/full_me.cu: Loop(2 in) s += |a - b|; Post out = s */
+	UMI_STRATEGY_RUNNING_SUM_I32 = 4,    /* main/iimg.cu:11-18: Loop(1 in, 1 out) out = t += x */
+	UMI_STRATEGY_DOT_I32 = 5,            /* main/gemm.cu:8-15 and main/fprop.cu: Loop(2 in) t += a * b; Post out = t */
+	UMI_STRATEGY_DOT_F32 = 6             /* the same on float */
+} umi_strategy;
+
+/* Generic operator through the C ABI: runs `strategy` over the plan's P x A
+ * space (the semantics of Execute, src/UMI_gpu.h:189-358: Pre, Loop over A
+ * in blocked row-major order, Post, per-dimension clamp / PAD).  in[i] and
+ * out[i] are the device pointers of the plan's inputs and outputs (one per
+ * memory); pad (may be NULL = all zero) holds one 4-byte padding value per
+ * input (UnrolledI::padding); user_const / uc_bytes the strategy's
+ * constants.  The memories' count and stages must be the strategy's. */
+umi_status umi_launch(const umi_plan* plan, int32_t strategy, const void* const* in, const void* pad,
+                      void* const* out, const void* user_const, size_t uc_bytes, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* specialised kernels                                                 */
 /* ------------------------------------------------------------------ */
@@ -184,7 +212,7 @@ umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h,
 /* ---- Learned motion proposal for 16x16 block motion estimation.
  * No counterpart in the reference (its full_me, main/full_me.cu, only does
  * exhaustive search); the exhaustive search above stays the fallback.
- * Network: the pair (cur, ref) box-averaged 4x4 -> four 3x3 convolutions
+ * Network: the pair (cur, ref) box-averaged 4x4, (mean - 128) / 32 -> four 3x3 convolutions
  * (32 channels, dilations 1, 2, 4, 8, ReLU, bf16 weights, fp32 accumulation)
  * -> a linear head per 16x16 block over its 4x4 cells x 32 channels -> one
  * vector (mv_y, mv_x) / 16.  Parameters are one fp32 array of
@@ -312,6 +340,21 @@ umi_status umi_batch_run(int32_t op, const umi_batch_image* images, int32_t n_im
 umi_status umi_autotune_batch(int32_t op, const umi_batch_image* images, int32_t n_images,
                               const umi_batch_params* params, int32_t reps, int32_t* best_variant, float* best_ms,
                               void* stream);
+
+/* Batch graphs: a sequence of batched launches recorded once into a CUDA
+ * graph and replayed by one call.  umi_batch_graph_add records
+ * umi_batch_run(op, images, n_images, params, variant) after the previous
+ * ones (the image table is copied at that moment: later replays use the same
+ * buffers); umi_batch_graph_launch replays the whole sequence on `stream`
+ * (instantiating the graph on first use).  The handle owns host-side CUDA
+ * objects only; destroy it when no replay is pending.  The reference has no
+ * batching (one Execute per image). */
+typedef struct umi_batch_graph umi_batch_graph;
+umi_status umi_batch_graph_create(umi_batch_graph** graph);
+umi_status umi_batch_graph_add(umi_batch_graph* graph, int32_t op, const umi_batch_image* images, int32_t n_images,
+                               const umi_batch_params* params, int32_t variant);
+umi_status umi_batch_graph_launch(umi_batch_graph* graph, void* stream);
+void umi_batch_graph_destroy(umi_batch_graph* graph);
 
 #ifdef __cplusplus
 }

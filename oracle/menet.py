@@ -9,7 +9,7 @@ mathematical definition of the network that the CUDA kernels implement.
 The oracle itself is pinned by central finite differences in the tests.
 
 Network (parameters in the flat layout of umi_gb300.param_layout()):
-  x0[0] = boxmean4(cur)/255 - 0.5, x0[1] = boxmean4(ref)/255 - 0.5
+  x0[0] = (boxmean4(cur) - 128)/32, x0[1] = (boxmean4(ref) - 128)/32
   a_l   = ReLU(b_l + sum_{ci,tap} W_l[co, ci, tap] * a_{l-1}[ci, p + dil_l * off(tap)])
           (zero outside the image; off(tap) = (tap // 3 - 1, tap % 3 - 1); dil 1, 2, 4, 8)
   pred[k, j] = bh[j] + sum_f Wh[j, f] * a_4[f // 16, 4 by + (f // 4) % 4, 4 bx + f % 4]
@@ -55,7 +55,7 @@ def downsample(cur, ref):
     out = np.empty((2, H4, W4), np.float64)
     for c, f in enumerate((cur, ref)):
         s = f[:4 * H4, :4 * W4].astype(np.float64).reshape(H4, 4, W4, 4).sum(axis=(1, 3))
-        out[c] = s / (16.0 * 255.0) - 0.5
+        out[c] = s / 512.0 - 4.0
     return out
 
 

@@ -50,6 +50,13 @@ SIGNATURES = {
     "umi_last_error_string": ([], ctypes.c_char_p),
     "umi_version": ([], ctypes.c_int),
     "umi_plan_build": ([_vp, _vp], ctypes.c_int),
+    "umi_plan_create": ([_vp, _vp], ctypes.c_int),
+    "umi_plan_destroy": ([_vp], None),
+    "umi_launch": ([_vp, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "umi_batch_graph_create": ([_vp], ctypes.c_int),
+    "umi_batch_graph_add": ([_vp, _i32, _vp, _i32, _vp, _i32], ctypes.c_int),
+    "umi_batch_graph_launch": ([_vp, _vp], ctypes.c_int),
+    "umi_batch_graph_destroy": ([_vp], None),
     "umi_filter3x3_f32": ([_vp, _vp, _i32, _i32, _vp, _f32, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
     "umi_iimg_u8_i32": ([_vp, _vp, _i32, _i32, _vp, _sz, _vp], ctypes.c_int),
@@ -156,6 +163,73 @@ def plan_build(desc: Desc) -> Plan:
     plan = Plan()
     check(lib().umi_plan_build(ctypes.byref(desc), ctypes.byref(plan)), "umi_plan_build")
     return plan
+
+
+(STRATEGY_NEIGHBOUR_SUM_I32, STRATEGY_WEIGHTED_SUM_I32, STRATEGY_RANGE_WEIGHTED_F32, STRATEGY_ABS_DIFF_SUM_I32,
+ STRATEGY_RUNNING_SUM_I32, STRATEGY_DOT_I32, STRATEGY_DOT_F32) = range(7)
+_STRATEGY_FLOAT = {STRATEGY_RANGE_WEIGHTED_F32, STRATEGY_DOT_F32}
+
+
+def launch(desc: Desc, strategy: int, ins, outs, pads=None, consts=None, stream=None) -> None:
+    """Generic operator with a built-in strategy (umi_plan_create + umi_launch + umi_plan_destroy).
+
+    ins / outs: CUDA tensors (int32 or float32, per the strategy), one per
+    memory in the descriptor's order; pads: one padding value per input;
+    consts: the strategy's constants as a sequence of numbers (int32 or
+    float32 by strategy)."""
+    import numpy as np
+    import torch
+    is_f = strategy in _STRATEGY_FLOAT
+    et = torch.float32 if is_f else torch.int32
+    for i, t in enumerate(list(ins) + list(outs)):
+        _need(t, et, f"memory {i}")
+    plan = ctypes.c_void_p()
+    check(lib().umi_plan_create(ctypes.byref(desc), ctypes.byref(plan)), "umi_plan_create")
+    try:
+        inp = (ctypes.c_void_p * max(1, len(ins)))(*[t.data_ptr() for t in ins])
+        outp = (ctypes.c_void_p * max(1, len(outs)))(*[t.data_ptr() for t in outs])
+        pad = None
+        if pads is not None:
+            pad = np.ascontiguousarray(pads, dtype=np.float32 if is_f else np.int32)
+        uc = None
+        if consts is not None:
+            uc = np.ascontiguousarray(consts, dtype=np.float32 if is_f else np.int32)
+        check(lib().umi_launch(plan, strategy, inp, pad.ctypes.data_as(ctypes.c_void_p) if pad is not None else None,
+                               outp, uc.ctypes.data_as(ctypes.c_void_p) if uc is not None else None,
+                               uc.nbytes if uc is not None else 0, _stream_ptr(stream)), "umi_launch")
+    finally:
+        lib().umi_plan_destroy(plan)
+
+
+class BatchGraph:
+    """A sequence of batched launches recorded once and replayed (umi_batch_graph_*)."""
+
+    def __init__(self):
+        self._h = ctypes.c_void_p()
+        check(lib().umi_batch_graph_create(ctypes.byref(self._h)), "umi_batch_graph_create")
+        self._keep = []
+
+    def add(self, op: int, images, params=None, variant: int = -1):
+        """Record one batched launch: images = [(in, aux_or_None, out), ...] as batch_run."""
+        table = _batch_table(images)
+        prm = params if params is not None else BatchParams()
+        check(lib().umi_batch_graph_add(self._h, op, table, len(images), ctypes.byref(prm), variant),
+              "umi_batch_graph_add")
+        self._keep.append((table, prm))
+
+    def launch(self, stream=None):
+        check(lib().umi_batch_graph_launch(self._h, _stream_ptr(stream)), "umi_batch_graph_launch")
+
+    def close(self):
+        if self._h:
+            lib().umi_batch_graph_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def header_functions() -> list[str]:

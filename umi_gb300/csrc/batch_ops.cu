@@ -15,6 +15,7 @@
 // one Execute per image.
 #include <algorithm>
 #include <cmath>
+#include <new>
 
 #include "common.h"
 
@@ -507,4 +508,73 @@ extern "C" umi_status umi_autotune_batch(int32_t op, const umi_batch_image* imag
 	*best_variant = best;
 	*best_ms = best_t;
 	return umi::ok();
+}
+
+// ---- batch graphs: a sequence of persistent batched launches recorded once
+// into a CUDA graph and replayed with one cudaGraphLaunch.
+struct umi_batch_graph {
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	cudaGraphNode_t last = nullptr;
+	cudaStream_t capture = nullptr;
+	int n_ops = 0;
+};
+
+extern "C" umi_status umi_batch_graph_create(umi_batch_graph** out) {
+	if (!out) return umi::fail(UMI_ERR_INVALID_ARG, "batch graph: null pointer");
+	*out = nullptr;
+	umi_batch_graph* g = new (std::nothrow) umi_batch_graph();
+	if (!g) return umi::fail(UMI_ERR_NO_MEMORY, "batch graph: host allocation failed");
+	umi_status rc = umi::cuda_status(cudaGraphCreate(&g->graph, 0), "cudaGraphCreate");
+	if (rc == UMI_OK)
+		rc = umi::cuda_status(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking), "cudaStreamCreate");
+	if (rc != UMI_OK) {
+		umi_batch_graph_destroy(g);
+		return rc;
+	}
+	*out = g;
+	return umi::ok();
+}
+
+extern "C" umi_status umi_batch_graph_add(umi_batch_graph* g, int32_t op, const umi_batch_image* images,
+                                          int32_t n_images, const umi_batch_params* params, int32_t variant) {
+	if (!g) return umi::fail(UMI_ERR_INVALID_ARG, "batch graph: null graph");
+	UMI_TRY(umi::cuda_status(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal),
+	                         "cudaStreamBeginCapture"));
+	const umi_status rc = run(op, images, n_images, params, variant, g->capture);
+	cudaGraph_t sub = nullptr;
+	const umi_status ec = umi::cuda_status(cudaStreamEndCapture(g->capture, &sub), "cudaStreamEndCapture");
+	if (rc != UMI_OK || ec != UMI_OK) {
+		if (sub) cudaGraphDestroy(sub);
+		return rc != UMI_OK ? rc : ec;
+	}
+	cudaGraphNode_t node = nullptr;
+	const umi_status ac = umi::cuda_status(
+		cudaGraphAddChildGraphNode(&node, g->graph, g->last ? &g->last : nullptr, g->last ? 1 : 0, sub),
+		"cudaGraphAddChildGraphNode");
+	cudaGraphDestroy(sub);  // the child node holds its own copy
+	UMI_TRY(ac);
+	g->last = node;
+	++g->n_ops;
+	if (g->exec) {
+		cudaGraphExecDestroy(g->exec);
+		g->exec = nullptr;
+	}
+	return umi::ok();
+}
+
+extern "C" umi_status umi_batch_graph_launch(umi_batch_graph* g, void* stream) {
+	if (!g) return umi::fail(UMI_ERR_INVALID_ARG, "batch graph: null graph");
+	if (g->n_ops == 0) return umi::ok();
+	if (!g->exec) UMI_TRY(umi::cuda_status(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate"));
+	UMI_TRY(umi::cuda_status(cudaGraphLaunch(g->exec, umi::as_stream(stream)), "cudaGraphLaunch"));
+	return umi::ok();
+}
+
+extern "C" void umi_batch_graph_destroy(umi_batch_graph* g) {
+	if (!g) return;
+	if (g->exec) cudaGraphExecDestroy(g->exec);
+	if (g->graph) cudaGraphDestroy(g->graph);
+	if (g->capture) cudaStreamDestroy(g->capture);
+	delete g;
 }

@@ -7,7 +7,7 @@
 //
 // Network (all hand-written kernels below; fp32 master parameters, bf16
 // weights in the forward/backward arithmetic, fp32 accumulation):
-//   x0  = (cur, ref) box-averaged 4x4, scaled to [-0.5, 0.5)        (2, H4, W4)
+//   x0  = ((cur, ref) box-averaged 4x4 - 128) / 32                  (2, H4, W4)
 //   a_l = ReLU(conv3x3_dil(a_{l-1}; W_l, b_l)), dilations 1, 2, 4, 8 (32, H4, W4)
 //   mv  = Wh . a4[:, 4 cells x 4 cells of the block] + bh          (nblk, 2)
 // The dilations give a receptive field of +-15 cells (+-60 pixels at full
@@ -92,7 +92,7 @@ __global__ void downsample4_kernel(const uint8_t* __restrict__ cur, const uint8_
 		for (int dy = 0; dy < 4; ++dy)
 #pragma unroll
 			for (int dx = 0; dx < 4; ++dx) s += src[(size_t)dy * w + dx];
-		x0[i] = (float)s * (1.0f / (16.0f * 255.0f)) - 0.5f;
+		x0[i] = (float)s * (1.0f / 512.0f) - 4.0f;  // (box mean - 128) / 32, exact in fp32
 	}
 }
 
