@@ -165,7 +165,9 @@ umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, int32_t w, 
 /* Integral image, uint8 -> int32: out[y,x] = sum_{y'<=y, x'<=x} in[y',x'].
  * Replaces the two Execute calls of main/iimg.cu:37-82 (row prefix through a
  * Loop output, transposed, twice).  Needs a device workspace of
- * umi_iimg_u8_i32_workspace_bytes(h, w) bytes (16-byte aligned). */
+ * umi_iimg_u8_i32_workspace_bytes(h, w) bytes (16-byte aligned; about
+ * 0.75 byte per pixel).  Frames with h*w*255 >= 2^31 are rejected
+ * (UMI_ERR_UNSUPPORTED: sums could overflow int32). */
 size_t umi_iimg_u8_i32_workspace_bytes(int32_t h, int32_t w);
 umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* workspace,
                            size_t workspace_bytes, void* stream);
@@ -174,9 +176,10 @@ umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w
  * (no allocator to take a workspace from, or a context where cudaMalloc is
  * not allowed).  No counterpart in the reference.  The tile sums go to a
  * scratch array built into the library, UMI_IIMG_NOALLOC_SCRATCH_BYTES
- * (1 MiB) per GPU, held until the process exits; frames whose workspace
- * (umi_iimg_u8_i32_workspace_bytes) exceeds it are rejected with
- * UMI_ERR_NO_MEMORY (3840x2160 and 4096x2160 fit).  The first call on a
+ * (1 MiB) per GPU, held until the process exits; frames whose tile sums
+ * (int32 per row per 256-column tile, per column per 64-row tile and per
+ * tile, each array rounded up to 256 bytes) exceed it are rejected with
+ * UMI_ERR_NO_MEMORY (3840x2160 and 4096x2160 fit); at most 4096 rows.  The first call on a
  * device looks up the scratch address (cudaGetSymbolAddress) with that
  * device current: make it before any stream capture.  All calls share the
  * scratch: calls that overlap on the GPU race and must be serialised by the

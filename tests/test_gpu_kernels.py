@@ -49,7 +49,8 @@ def test_filter3x3_rejects_alias(umi, dev):
 
 # ---------------------------------------------------------------- iimg
 @pytest.mark.parametrize("h,w", [(1080, 1920), (1, 1), (1, 130), (97, 1), (31, 127), (33, 129), (256, 256),
-                                 (300, 500), (517, 1023), (64, 256), (65, 257), (63, 255), (4096, 72), (2160, 3840)])
+                                 (300, 500), (517, 1023), (64, 256), (65, 257), (63, 255), (4096, 72), (2160, 3840),
+                                 (4097, 8), (9, 2049), (13, 4101), (17, 6150), (7, 2048)])
 def test_iimg_u8_i32(umi, orc, dev, h, w):
     from umi_gb300 import workloads
     x = workloads.iimg_frame(seed=h + w, h=h, w=w)
@@ -79,10 +80,10 @@ def test_iimg_unaligned_views(umi, orc, dev):
 
 def test_iimg_limits(umi, dev):
     import torch
-    x = torch.zeros((4097, 8), dtype=torch.uint8, device=dev)
+    x = torch.zeros((8500, 1000), dtype=torch.uint8, device=dev)
     with pytest.raises(umi.UmiError) as e:
         umi.iimg_u8_i32(x)
-    assert e.value.status == 3  # UMI_ERR_UNSUPPORTED: more rows than the carry unroll covers
+    assert e.value.status == 3  # UMI_ERR_UNSUPPORTED: 8.5M pixels x 255 could overflow int32
 
 
 def test_iimg_repeated_calls_reuse_workspace(umi, orc, dev):

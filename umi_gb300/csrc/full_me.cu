@@ -20,6 +20,10 @@
 //    shared-memory atomicMin per macroblock gives the minimum SAD with the
 //    first displacement in raster order (the reference's output order
 //    (..., sy, sx), main/full_me.cu:70-71).
+//  * the argmin search runs persistent CTAs with two window buffers: the
+//    next macroblocks' windows are copied with cp.async while the current
+//    ones are searched (full_me_pipe_kernel); the SAD-volume output keeps
+//    one CTA per group of macroblocks (full_me_kernel).
 #include <algorithm>
 
 #include "common.h"
@@ -45,7 +49,7 @@ struct MeGeom {
 	int mb_stride;    // words per macroblock (4 copies + current block)
 	int m;            // macroblocks per CTA
 	int tasks_per_mb; // ndx * ng
-	int vec_ok;       // ref is 4-byte aligned and w % 4 == 0: word loads allowed
+	int vec_ok;       // ref and cur are 4-byte aligned and w % 4 == 0: word loads / 4-byte cp.async allowed
 	int nx32;         // largest multiple of 32 <= ndx: displacements served by whole warps
 	const int32_t* list;        // optional: search only these blocks (slot i -> block list[i])
 	const int32_t* list_count;  // number of valid slots of `list` (device word)
@@ -219,6 +223,203 @@ full_me_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
 	}
 }
 
+// ---- Persistent, double-buffered form of the argmin search.
+// Each CTA walks groups of g.m macroblocks (group gi = blockIdx.x, +gridDim.x,
+// ...).  While it searches group gi out of one shared-memory buffer, the
+// windows of its next group are copied into the other buffer with cp.async
+// (windows wholly inside the frame; windows that need edge replication are
+// staged with clamped loads as before), so the copy latency hides behind the
+// search.  Same tasks, same arithmetic, same argmin key: results are
+// identical to full_me_kernel.
+
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const void* src) {
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Stage copy 0 of every window of group gi (and its current blocks) into buf.
+template <int B>
+__device__ __forceinline__ void me_stage_group(const MeGeom& g, uint32_t* buf, int gi, const uint8_t* __restrict__ cur,
+                                               const uint8_t* __restrict__ ref, const int32_t* __restrict__ centers,
+                                               int tid, int row0, int wd0, int rstep, bool stager) {
+	constexpr int BW = B / 4;
+	for (int m = 0; m < g.m; ++m) {
+		const int blk = slot_block(g, gi * g.m + m);
+		if (blk < 0) break;
+		const int by = blk / g.nbx, bx = blk - by * g.nbx;
+		const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
+		const int gy0 = by * B + cy - g.r, gx0 = bx * B + cx - g.r;
+		uint32_t* win = buf + m * g.mb_stride;
+		const bool inside = g.vec_ok && gy0 >= 0 && gy0 + g.win_rows <= g.h && gx0 >= 0 &&
+		                    gx0 + 4 * g.win_words <= g.w && (gx0 & 3) == 0;
+		if (stager) {
+			if (inside) {
+				const uint8_t* src = ref + (size_t)gy0 * g.w + gx0 + 4 * wd0;
+				for (int row = row0; row < g.win_rows; row += rstep)
+					cp_async4(win + row * g.win_words + wd0, src + (size_t)row * g.w);
+			} else {
+				const int gx = gx0 + 4 * wd0;
+				const bool vec = g.vec_ok && gx >= 0 && gx + 3 < g.w && (gx & 3) == 0;
+				int xs[4];
+#pragma unroll
+				for (int k = 0; k < 4; ++k) xs[k] = min(max(gx + k, 0), g.w - 1);
+				for (int row = row0; row < g.win_rows; row += rstep) {
+					const int gy = min(max(gy0 + row, 0), g.h - 1);
+					const uint8_t* src = ref + (size_t)gy * g.w;
+					uint32_t v;
+					if (vec) {
+						v = __ldg(reinterpret_cast<const uint32_t*>(src + gx));
+					} else {
+						v = 0;
+#pragma unroll
+						for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + xs[k]) << (8 * k);
+					}
+					win[row * g.win_words + wd0] = v;
+				}
+			}
+		}
+		uint32_t* cb = win + 4 * g.copy_stride;
+		if (tid < B * BW) {
+			const int row = tid / BW, wd = tid - row * BW;
+			const uint8_t* src = cur + (size_t)(by * B + row) * g.w + bx * B + 4 * wd;
+			if (g.vec_ok) {
+				cp_async4(cb + tid, src);
+			} else {
+				uint32_t v = 0;
+#pragma unroll
+				for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + k) << (8 * k);
+				cb[tid] = v;
+			}
+		}
+	}
+}
+
+// Copies 1..3 of every window of group gi (word k of copy s holds bytes
+// [4k+s, 4k+s+4) of the row).
+__device__ __forceinline__ void me_shift_group(const MeGeom& g, uint32_t* buf, int gi, int row0, int wd0, int rstep,
+                                               bool stager) {
+	if (!stager) return;
+	for (int m = 0; m < g.m; ++m) {
+		if (slot_block(g, gi * g.m + m) < 0) break;
+		uint32_t* win = buf + m * g.mb_stride;
+		const bool last = wd0 + 1 == g.win_words;
+		for (int row = row0; row < g.win_rows; row += rstep) {
+			const int j = row * g.win_words + wd0;
+			const uint32_t lo = win[j], hi = last ? 0u : win[j + 1];
+			win[g.copy_stride + j] = __funnelshift_r(lo, hi, 8);
+			win[2 * g.copy_stride + j] = __funnelshift_r(lo, hi, 16);
+			win[3 * g.copy_stride + j] = __funnelshift_r(lo, hi, 24);
+		}
+	}
+}
+
+template <int B, int G>
+__global__ void __launch_bounds__(512) __maxnreg__((MeRegs<B, G>::value))
+full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
+                    const int32_t* __restrict__ centers, int32_t* __restrict__ out, const MeGeom g) {
+	extern __shared__ __align__(16) uint32_t smem[];
+	constexpr int BW = B / 4;
+	__shared__ uint32_t best[2][64];
+	const int tid = threadIdx.x;
+	const int ngroups = (g.slots + g.m - 1) / g.m;
+	const int rstep = blockDim.x / g.win_words;  // host guarantees blockDim >= win_words
+	const int row0 = tid / g.win_words;
+	const int wd0 = tid - row0 * g.win_words;
+	const bool stager = row0 < rstep;
+	const int buf_words = g.m * g.mb_stride;
+	int gi = blockIdx.x;
+	if (gi >= ngroups || slot_block(g, gi * g.m) < 0) return;  // uniform over the CTA
+	if (tid < 64) best[0][tid] = best[1][tid] = 0xffffffffu;
+	me_stage_group<B>(g, smem, gi, cur, ref, centers, tid, row0, wd0, rstep, stager);
+	cp_async_wait_all();
+	__syncthreads();
+	me_shift_group(g, smem, gi, row0, wd0, rstep, stager);
+	__syncthreads();
+	int cbuf = 0;
+	const int total = g.m * g.tasks_per_mb;
+	while (true) {
+		const int ngi = gi + gridDim.x;
+		const bool has_next = ngi < ngroups && slot_block(g, ngi * g.m) >= 0;
+		uint32_t* cur_buf = smem + cbuf * buf_words;
+		uint32_t* next_buf = smem + (cbuf ^ 1) * buf_words;
+		if (has_next) me_stage_group<B>(g, next_buf, ngi, cur, ref, centers, tid, row0, wd0, rstep, stager);
+		// Search group gi (the tasks of full_me_kernel).
+		for (int t = tid; t < total; t += blockDim.x) {
+			const int m = t / g.tasks_per_mb;
+			const int rem = t - m * g.tasks_per_mb;
+			int grp, ix;
+			const int main_tasks = g.ng * g.nx32;
+			if (rem < main_tasks) {
+				grp = rem / g.nx32;
+				ix = rem - grp * g.nx32;
+			} else {
+				const int rw = g.ndx - g.nx32, r2 = rem - main_tasks;
+				grp = r2 / rw;
+				ix = g.nx32 + (r2 - grp * rw);
+			}
+			if (slot_block(g, gi * g.m + m) < 0) continue;
+			const uint32_t* win = cur_buf + m * g.mb_stride;
+			const uint32_t* cb = win + 4 * g.copy_stride;
+			const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + grp * G * g.win_words;
+			uint32_t ring[G][BW];
+			uint32_t acc[G];
+#pragma unroll
+			for (int q = 0; q < G; ++q) {
+				acc[q] = 0;
+#pragma unroll
+				for (int k = 0; k < BW; ++k) ring[q][k] = wp[q * g.win_words + k];
+			}
+#pragma unroll
+			for (int py = 0; py < B; ++py) {
+				uint32_t cv[BW];
+				if (BW == 4) {
+					const uint4 c4 = *reinterpret_cast<const uint4*>(cb + py * BW);
+					cv[0] = c4.x; cv[1] = c4.y; cv[2 % BW] = c4.z; cv[3 % BW] = c4.w;
+				} else {
+#pragma unroll
+					for (int k = 0; k < BW; ++k) cv[k] = cb[py * BW + k];
+				}
+				if (py > 0) {
+					const int r = py + G - 1;
+#pragma unroll
+					for (int k = 0; k < BW; ++k) ring[r % G][k] = wp[r * g.win_words + k];
+				}
+#pragma unroll
+				for (int k = 0; k < BW; ++k)
+#pragma unroll
+					for (int q = 0; q < G; ++q) acc[q] = sad4_acc(cv[k], ring[(py + q) % G][k], acc[q]);
+			}
+			const int iy0 = grp * G;
+			uint32_t key = 0xffffffffu;
+#pragma unroll
+			for (int q = 0; q < G; ++q)
+				if (iy0 + q < g.ndx) key = min(key, (acc[q] << 15) | (uint32_t)((iy0 + q) * g.ndx + ix));
+			atomicMin(&best[cbuf][m], key);
+		}
+		cp_async_wait_all();
+		__syncthreads();  // search of gi done; this thread's copies for ngi landed (all threads: barrier)
+		if (tid < g.m) {
+			const int blk = slot_block(g, gi * g.m + tid);
+			if (blk >= 0) {
+				const uint32_t key = best[cbuf][tid];
+				const int idx = (int)(key & 0x7fffu);
+				const int iy = idx / g.ndx, ix = idx - iy * g.ndx;
+				const int cy = centers ? centers[2 * blk] : 0, cx = centers ? centers[2 * blk + 1] : 0;
+				out[3 * blk + 0] = cy + iy - g.r;
+				out[3 * blk + 1] = cx + ix - g.r;
+				out[3 * blk + 2] = (int32_t)(key >> 15);
+			}
+			best[cbuf][tid] = 0xffffffffu;
+		}
+		if (!has_next) break;
+		me_shift_group(g, next_buf, ngi, row0, wd0, rstep, stager);
+		__syncthreads();
+		gi = ngi;
+		cbuf ^= 1;
+	}
+}
+
 // Vertical displacements per thread: the candidate that wastes the fewest
 // padded rows (ng*G - ndx), larger G on ties (fewer window-row loads).
 int pick_g(int ndx) {
@@ -245,6 +446,37 @@ umi_status launch_g(const uint8_t* cur, const uint8_t* ref, const int32_t* cente
 	const int grid = (g.slots + g.m - 1) / g.m;
 	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
 	return umi::launch_status("full_me_kernel");
+}
+
+template <int B, int G>
+umi_status launch_pipe_g(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
+                         int threads, size_t smem, cudaStream_t st) {
+	auto kern = full_me_pipe_kernel<B, G>;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+	                         "cudaFuncSetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+	                                              (int)cudaSharedmemCarveoutMaxShared), "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0, per_sm = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
+	                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
+	if (per_sm < 1) return umi::fail(UMI_ERR_UNSUPPORTED, "full_me: %zu bytes of shared memory per CTA do not fit", smem);
+	const int ngroups = (g.slots + g.m - 1) / g.m;
+	const int grid = std::min(ngroups, per_sm * sms);
+	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
+	return umi::launch_status("full_me_pipe_kernel");
+}
+
+template <int B>
+umi_status launch_pipe_b(int G, const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out,
+                         const MeGeom& g, int threads, size_t smem, cudaStream_t st) {
+	switch (G) {
+		case 5: return launch_pipe_g<B, 5>(cur, ref, centers, out, g, threads, smem, st);
+		case 9: return launch_pipe_g<B, 9>(cur, ref, centers, out, g, threads, smem, st);
+		case 13: return launch_pipe_g<B, 13>(cur, ref, centers, out, g, threads, smem, st);
+		default: return launch_pipe_g<B, 15>(cur, ref, centers, out, g, threads, smem, st);
+	}
 }
 
 template <int B, bool V>
@@ -285,9 +517,10 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.mb_stride = (g.mb_stride + 3) & ~3;         // keep each current block 16-byte aligned
 	g.tasks_per_mb = g.ndx * g.ng;
 	g.nx32 = (g.ndx / 32) * 32;
-	g.vec_ok = umi::aligned(ref, 4) && (w % 4) == 0;
+	g.vec_ok = umi::aligned(ref, 4) && umi::aligned(cur, 4) && (w % 4) == 0;
 	// Macroblocks per CTA: enough tasks to fill at least ~256 threads, within
-	// 96 KB of shared memory and the 64-slot argmin table.
+	// 96 KB of shared memory (the argmin search keeps two such buffers) and
+	// the 64-slot argmin table.
 	int m = std::max(1, 256 / g.tasks_per_mb);
 	const int max_m_smem = std::max(1, (int)((96 * 1024) / (g.mb_stride * 4)));
 	m = std::min(std::min(m, max_m_smem), 64);
@@ -304,7 +537,10 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	const size_t smem = (size_t)m * g.mb_stride * 4;
 	const cudaStream_t st = umi::as_stream(stream);
 	umi_status rc;
-	if (b == 16)
+	if (!volume && 2 * smem <= 200 * 1024)  // double-buffered persistent search
+		rc = b == 16 ? launch_pipe_b<16>(G, cur, ref, centers, out, g, threads, 2 * smem, st)
+		             : launch_pipe_b<8>(G, cur, ref, centers, out, g, threads, 2 * smem, st);
+	else if (b == 16)
 		rc = volume ? launch_b<16, true>(G, cur, ref, centers, out, g, threads, smem, st)
 		            : launch_b<16, false>(G, cur, ref, centers, out, g, threads, smem, st);
 	else

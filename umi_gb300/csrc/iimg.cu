@@ -4,7 +4,11 @@
 // scan along x written transposed, applied twice) with one read of the uint8
 // frame from HBM and one write of the int32 result.
 //
-// The frame is cut into TH x TW tiles (64 x 256: a 1080p frame is 136 tiles,
+// Two forms share this file.  umi_iimg_u8_i32 uses the band form (further
+// down: per-band column sums, a carry scan down the bands, one output pass).
+// umi_iimg_u8_i32_noalloc keeps the tile form below, whose small tile sums
+// fit the library's built-in scratch:
+// the frame is cut into TH x TW tiles (64 x 256: a 1080p frame is 136 tiles,
 // about one per SM).  With the inclusive integral image ii and a tile at
 // (Y0, X0):
 //   ii[y][x] = corner + sum_{X0<=x'<=x} top[x'] + sum_{Y0<=y'<=y} left[y'] + local[y][x]
@@ -255,6 +259,187 @@ size_t ws_bytes(int h, int w) {
 	return al((size_t)h * ntx * 4) + al(nty * (size_t)w * 4) + al(nty * ntx * 4);
 }
 
+// ---------------------------------------------------------------------------
+// Band form (umi_iimg_u8_i32).  The frame is cut into bands of RB rows over
+// the full width; with V[b][x] = sum of column x over all rows above band b,
+//   ii[y][x] = sum_{x'<=x} V[b][x'] + sum_{band rows y'<=y} sum_{x'<=x} in[y'][x'].
+// Kernel 1 writes per-band column sums (uint16: at most RB*255), kernel 2
+// scans them down the bands into V (one warp per band range, 32 columns per
+// CTA), kernel 3 reads each band once, scans its RB rows and its V row along
+// x with one block-wide scan of RB+1 values per thread, and writes the band.
+// The three launches are chained with programmatic dependent launch; kernel
+// 3 loads its pixels before waiting for kernel 2.  Every grid is parallel
+// over the whole frame (no chain of tiles), so a 1080p frame runs 135 CTAs of
+// 256 threads in the output pass.
+constexpr int RB = 8;          // rows per band
+constexpr int SEG = NT * CPL;  // columns per CTA pass (2048)
+
+struct BandGeom {
+	int h, w, nb, wpad, nseg;
+	int bpw;  // bands per warp in the carry scan: ceil(nb / NW)
+	int vec_in, vec_out;
+	uint16_t* colsum;  // [nb][wpad]
+	int32_t* vsum;     // [nb][wpad]
+};
+
+size_t band_ws_bytes(int h, int w) {
+	const size_t nb = umi::ceil_div(h, RB), wpad = (size_t)umi::ceil_div(w, CPL) * CPL;
+	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+	return al(nb * wpad * 2) + al(nb * wpad * 4);
+}
+
+__global__ void __launch_bounds__(NT) iimg_band_colsums(const uint8_t* __restrict__ in, const BandGeom g) {
+	pdl_trigger();
+	const int b = blockIdx.y;
+	const int x0 = blockIdx.x * SEG + threadIdx.x * CPL;
+	if (x0 >= g.w) return;
+	IimgGeom ig{};
+	ig.h = g.h; ig.w = g.w; ig.vec_in = g.vec_in;
+	uint32_t s[CPL] = {};
+#pragma unroll
+	for (int r = 0; r < RB; ++r) {
+		uint32_t v[CPL];
+		unpack8(load8(in, ig, b * RB + r, x0), v);
+#pragma unroll
+		for (int k = 0; k < CPL; ++k) s[k] += v[k];
+	}
+	uint4 o;
+	o.x = s[0] | (s[1] << 16);
+	o.y = s[2] | (s[3] << 16);
+	o.z = s[4] | (s[5] << 16);
+	o.w = s[6] | (s[7] << 16);
+	*reinterpret_cast<uint4*>(g.colsum + (size_t)b * g.wpad + x0) = o;
+}
+
+// V[b][x] = sum_{b' < b} colsum[b'][x]: lane = column, warp w = bands
+// [w*S, (w+1)*S), warp totals combined through shared memory.
+__global__ void __launch_bounds__(NT) iimg_band_carry(const BandGeom g) {
+	__shared__ uint32_t tot[NW][32];
+	pdl_trigger();
+	pdl_wait();
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+	const int x = blockIdx.x * 32 + lane;
+	const int b0 = wp * g.bpw, b1 = min(g.nb, b0 + g.bpw);
+	uint32_t s = 0;
+	if (x < g.wpad)
+		for (int b = b0; b < b1; ++b) s += g.colsum[(size_t)b * g.wpad + x];
+	tot[wp][lane] = s;
+	__syncthreads();
+	uint32_t pre = 0;
+	for (int k = 0; k < wp; ++k) pre += tot[k][lane];
+	if (x < g.wpad)
+		for (int b = b0; b < b1; ++b) {
+			g.vsum[(size_t)b * g.wpad + x] = (int32_t)pre;
+			pre += g.colsum[(size_t)b * g.wpad + x];
+		}
+}
+
+__global__ void __launch_bounds__(NT) iimg_band_out(const uint8_t* __restrict__ in, int32_t* __restrict__ out,
+                                                     const BandGeom g) {
+	__shared__ uint32_t wtot[NW][RB + 1];
+	const int b = blockIdx.x, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+	const int y0 = b * RB;
+	IimgGeom ig{};
+	ig.h = g.h; ig.w = g.w; ig.vec_in = g.vec_in;
+	uint32_t carry[RB + 1] = {};  // totals of the segments to the left (rows, then the V row)
+	uint2 raw[RB];
+	{
+		const int x0 = threadIdx.x * CPL;
+#pragma unroll
+		for (int r = 0; r < RB; ++r) raw[r] = x0 < g.w ? load8(in, ig, y0 + r, x0) : make_uint2(0, 0);
+	}
+	pdl_wait();
+	for (int seg = 0; seg < g.nseg; ++seg) {
+		const int x0 = seg * SEG + threadIdx.x * CPL;
+		const bool live = x0 < g.w;
+		if (seg > 0) {
+#pragma unroll
+			for (int r = 0; r < RB; ++r) raw[r] = live ? load8(in, ig, y0 + r, x0) : make_uint2(0, 0);
+		}
+		uint32_t vv[CPL] = {};
+		if (live) {
+			const int4* vp = reinterpret_cast<const int4*>(g.vsum + (size_t)b * g.wpad + x0);
+			const int4 a = vp[0], c = vp[1];
+			vv[0] = a.x; vv[1] = a.y; vv[2] = a.z; vv[3] = a.w;
+			vv[4] = c.x; vv[5] = c.y; vv[6] = c.z; vv[7] = c.w;
+		}
+		// thread totals of each row and of the V row, scanned over the block
+		uint32_t tsum[RB + 1];
+#pragma unroll
+		for (int r = 0; r < RB; ++r) {
+			uint32_t v[CPL];
+			unpack8(raw[r], v);
+			uint32_t t = 0;
+#pragma unroll
+			for (int k = 0; k < CPL; ++k) t += v[k];
+			tsum[r] = t;
+		}
+		{
+			uint32_t t = 0;
+#pragma unroll
+			for (int k = 0; k < CPL; ++k) t += vv[k];
+			tsum[RB] = t;
+		}
+		uint32_t ex[RB + 1];
+#pragma unroll
+		for (int r = 0; r <= RB; ++r) {
+			const uint32_t inc = warp_incl_scan(tsum[r], lane);
+			ex[r] = inc - tsum[r];
+			if (lane == 31) wtot[wp][r] = inc;
+		}
+		__syncthreads();
+		uint32_t segtot[RB + 1];
+#pragma unroll
+		for (int r = 0; r <= RB; ++r) {
+			uint32_t before = 0, all = 0;
+#pragma unroll
+			for (int k = 0; k < NW; ++k) {
+				const uint32_t t = wtot[k][r];
+				before += k < wp ? t : 0u;
+				all += t;
+			}
+			ex[r] += before + carry[r];
+			segtot[r] = all;
+		}
+		__syncthreads();  // wtot is rewritten by the next segment
+		// outputs: T(x) = V-row prefix, plus the running column sum of the row prefixes
+		uint32_t T[CPL], colacc[CPL];
+		{
+			uint32_t tp = ex[RB];
+#pragma unroll
+			for (int k = 0; k < CPL; ++k) {
+				tp += vv[k];
+				T[k] = tp;
+				colacc[k] = 0;
+			}
+		}
+#pragma unroll
+		for (int r = 0; r < RB; ++r) {
+			uint32_t rp = ex[r], o[CPL];
+#pragma unroll
+			for (int k = 0; k < CPL; ++k) {
+				rp += (k < 4 ? (raw[r].x >> (8 * k)) : (raw[r].y >> (8 * (k - 4)))) & 0xffu;
+				colacc[k] += rp;
+				o[k] = T[k] + colacc[k];
+			}
+			const int y = y0 + r;
+			if (live && y < g.h) {
+				int32_t* op = out + (size_t)y * g.w + x0;
+				if (g.vec_out && x0 + 7 < g.w) {
+					reinterpret_cast<int4*>(op)[0] = make_int4(o[0], o[1], o[2], o[3]);
+					reinterpret_cast<int4*>(op)[1] = make_int4(o[4], o[5], o[6], o[7]);
+				} else {
+#pragma unroll
+					for (int k = 0; k < CPL; ++k)
+						if (x0 + k < g.w) op[k] = (int32_t)o[k];
+				}
+			}
+		}
+#pragma unroll
+		for (int r = 0; r <= RB; ++r) carry[r] += segtot[r];
+	}
+}
+
 cudaLaunchAttribute pdl_attr() {
 	cudaLaunchAttribute a;
 	a.id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -266,7 +451,7 @@ cudaLaunchAttribute pdl_attr() {
 
 extern "C" size_t umi_iimg_u8_i32_workspace_bytes(int32_t h, int32_t w) {
 	if (h <= 0 || w <= 0) return 0;
-	return ws_bytes(h, w);
+	return band_ws_bytes(h, w);
 }
 
 extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* workspace,
@@ -275,32 +460,37 @@ extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h
 	if (h == 0 || w == 0) return umi::ok();
 	if (!in || !out || !workspace) return umi::fail(UMI_ERR_INVALID_ARG, "iimg: null pointer");
 	if (!umi::aligned(workspace, 16)) return umi::fail(UMI_ERR_INVALID_ARG, "iimg: workspace not 16-byte aligned");
-	if (workspace_bytes < ws_bytes(h, w))
-		return umi::fail(UMI_ERR_NO_MEMORY, "iimg: workspace of %zu bytes, need %zu", workspace_bytes, ws_bytes(h, w));
-	if (umi::ceil_div(h, TH) > MAXNTY)
-		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg: %d rows (max %d)", h, MAXNTY * TH);
+	if (workspace_bytes < band_ws_bytes(h, w))
+		return umi::fail(UMI_ERR_NO_MEMORY, "iimg: workspace of %zu bytes, need %zu", workspace_bytes,
+		                 band_ws_bytes(h, w));
 	if ((int64_t)h * w > ((int64_t)1 << 31) / 255)
 		return umi::fail(UMI_ERR_UNSUPPORTED, "iimg: %dx%d frame: sums could exceed int32", h, w);
-	IimgGeom g{};
+	BandGeom g{};
 	g.h = h; g.w = w;
-	g.ntx = umi::ceil_div(w, TW);
-	g.nty = umi::ceil_div(h, TH);
+	g.nb = umi::ceil_div(h, RB);
+	g.wpad = umi::ceil_div(w, CPL) * CPL;
+	g.nseg = umi::ceil_div(w, SEG);
+	g.bpw = umi::ceil_div(g.nb, NW);
 	g.vec_in = umi::aligned(in, 8) && (w % 8) == 0;
 	g.vec_out = umi::aligned(out, 16) && (w % 4) == 0;
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
 	char* ws = static_cast<char*>(workspace);
-	g.rowsum = reinterpret_cast<int32_t*>(ws);
-	g.colsum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4));
-	g.tilesum = reinterpret_cast<int32_t*>(ws + al((size_t)h * g.ntx * 4) + al((size_t)g.nty * w * 4));
-	cudaLaunchConfig_t cfg{};
-	cfg.gridDim = dim3(g.ntx, g.nty);
-	cfg.blockDim = dim3(NT);
-	cfg.stream = umi::as_stream(stream);
+	g.colsum = reinterpret_cast<uint16_t*>(ws);
+	g.vsum = reinterpret_cast<int32_t*>(ws + al((size_t)g.nb * g.wpad * 2));
+	const cudaStream_t st = umi::as_stream(stream);
+	// kernel 1 follows whatever the stream ran before: plain launch
+	iimg_band_colsums<<<dim3(g.nseg, g.nb), NT, 0, st>>>(in, g);
+	UMI_TRY(umi::launch_status("iimg_band_colsums"));
 	cudaLaunchAttribute attr[1] = {pdl_attr()};
+	cudaLaunchConfig_t cfg{};
+	cfg.blockDim = dim3(NT);
+	cfg.stream = st;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tile_sums, in, g), "iimg_tile_sums"));
-	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tiles, in, out, g), "iimg_tiles"));
+	cfg.gridDim = dim3(umi::ceil_div(g.wpad, 32));
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_band_carry, g), "iimg_band_carry"));
+	cfg.gridDim = dim3(g.nb);
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_band_out, in, out, g), "iimg_band_out"));
 	return umi::ok();
 }
 

@@ -186,10 +186,12 @@ def evaluate(net: MeNet, seeds, refine_r: int = 4, full_r: int = 64, sad_thresho
     return {k: {f: float(np.mean([r[f] for r in v])) for f in v[0]} for k, v in out.items()}
 
 
-def threshold_from(full) -> int:
-    """SAD threshold for the fallback: 1.5 x the 99th percentile of the optimal SADs."""
+def threshold_from(full, mult: float = 1.2) -> int:
+    """SAD threshold for the fallback: mult x the 99th percentile of the optimal SADs
+    of a calibration pair.  On the 4K workload 1.2 keeps the mean SAD regression
+    near 0.3 % (1.5: 1.5 %, 1.0: < 0.01 %) at 88 % fallback."""
     s = full[:, 2].float()
-    return int(1.5 * torch_quantile(s, 0.99))
+    return int(mult * torch_quantile(s, 0.99))
 
 
 def torch_quantile(x, q: float) -> float:
