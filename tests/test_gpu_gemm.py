@@ -66,7 +66,8 @@ def _conv_case(n, c, h, w, k, r, seed):
 
 
 @pytest.mark.parametrize("n,c,h,w,k,r", [(2, 64, 16, 16, 128, 3), (1, 128, 5, 130, 64, 3), (1, 64, 7, 9, 128, 1),
-                                         (1, 64, 9, 20, 200, 5), (1, 64, 1, 1, 128, 3), (3, 64, 33, 128, 128, 3)])
+                                         (1, 64, 9, 20, 200, 5), (1, 64, 1, 1, 128, 3), (3, 64, 33, 128, 128, 3),
+                                         (1, 64, 6, 300, 96, 3), (2, 64, 3, 129, 16, 3)])
 def test_conv2d_fprop_bf16(umi, orc, dev, n, c, h, w, k, r):
     import torch
     x, wt = _conv_case(n, c, h, w, k, r, n * 1000 + h * 10 + k)

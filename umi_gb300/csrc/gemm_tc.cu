@@ -5,20 +5,21 @@
 // main/gemm.cu:8-15: accum += A * B through shared memory, scalar) for the
 // half-precision operand types, plus a split-precision FP32 emulation.
 //
-// One CTA computes a 128 x 256 tile of C:
+// Persistent CTAs compute 128 x 256 tiles of C:
 //   warp 0, one lane  : TMA producer, K-slices of 64 into a 4-stage ring
 //                       (A 16 KB + B 32 KB per stage, 128-byte swizzle);
-//   warp 1            : allocates 256 TMEM columns; one lane issues the
-//                       tcgen05.mma (M=128, N=256, K=16, 4 per slice) and
-//                       commits each slice back to the producer;
+//   warp 1            : allocates 512 TMEM columns (two accumulators); one
+//                       lane issues the tcgen05.mma (M=128, N=256, K=16, 4 per
+//                       slice) and commits each slice back to the producer;
 //   warps 2..5        : epilogue, tcgen05.ld of their 32 TMEM lanes (rows),
-//                       fp32 stores.
+//                       fp32 stores, overlapping the next tile's MMAs.
 // All mbarrier waits are bounded (tc_common.cuh); on timeout the kernel
 // records an error bit in *err, drains its own copies and MMAs, frees TMEM
 // and returns.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.h"
@@ -43,9 +44,20 @@ struct GemmArgs {
 // C[M,N] = A[M,K] B[N,K]^T: grid (N/BN, M/BM).
 struct GemmPolicy {
 	static constexpr int BN = 256, STAGES = 4;
+	static constexpr bool RESIDENT_B = false;
+	static constexpr int NK_RES = 0;
+	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
+	static constexpr int R = 1;
+	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
 	using Args = GemmArgs;
 	struct Tile { int m0, n0; };
-	__device__ static Tile tile(const Args&) { return {(int)blockIdx.y * BM, (int)blockIdx.x * BN}; }
+	// tiles in row-major order of (m-block, n-block): CTAs working at the same
+	// time share A row-blocks in L2
+	__host__ __device__ static int ntiles(const Args& g) { return ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN); }
+	__device__ static Tile tile(const Args& g, int id) {
+		const int nt = (g.N + BN - 1) / BN;
+		return {(id / nt) * BM, (id % nt) * BN};
+	}
 	__device__ static int nk(const Args& g) { return (g.K + BK - 1) / BK; }
 	__device__ static void load(const CUtensorMap* ta, const CUtensorMap* tb, const Args&, const Tile& t, int ks,
 	                            void* a, void* b, uint64_t* bar) {
@@ -78,17 +90,25 @@ struct GemmPolicy {
 struct ConvArgs {
 	float* out;
 	int n, c, h, w, k, r;
-	int xtiles;
+	int xtiles, ktiles;
+	int vec4;  // out 16-byte aligned and w % 4 == 0: float4 stores along x
 	int* err;
 };
 struct ConvPolicy {
 	static constexpr int BN = 128, STAGES = 3;
+	static constexpr bool RESIDENT_B = false;
+	static constexpr int NK_RES = 0;
+	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
+	static constexpr int R = 1;
+	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
 	using Args = ConvArgs;
 	struct Tile { int n, y, x0, k0; };
-	__device__ static Tile tile(const Args& g) {
-		const int b = blockIdx.x;
+	// tile id = ((n*h + y)*xtiles + xt)*ktiles + kt
+	__host__ __device__ static int ntiles(const Args& g) { return g.n * g.h * g.xtiles * g.ktiles; }
+	__device__ static Tile tile(const Args& g, int id) {
+		const int kt = id % g.ktiles, b = id / g.ktiles;
 		const int xt = b % g.xtiles, rest = b / g.xtiles;
-		return {rest / g.h, rest % g.h, xt * BM, (int)blockIdx.y * BN};
+		return {rest / g.h, rest % g.h, xt * BM, kt * BN};
 	}
 	__device__ static int nk(const Args& g) { return g.r * g.r * (g.c / BK); }
 	__device__ static void load(const CUtensorMap* ta, const CUtensorMap* tb, const Args& g, const Tile& t, int ks,
@@ -99,56 +119,156 @@ struct ConvPolicy {
 		tma_load_4d(a, ta, bar, c0, t.x0 + dx - pad, t.y + dy - pad, t.n);
 		tma_load_2d(b, tb, bar, tap * g.c + c0, t.k0);
 	}
-	// this thread's pixel (row rl of the tile), output channels [k0+c, +32)
+	// resident-weight form: the A slice alone, and B slice ks of output-channel block 0
+	__device__ static void load_a(const CUtensorMap* ta, const Args& g, const Tile& t, int ks, void* a, uint64_t* bar) {
+		const int cs = g.c / BK;
+		const int tap = ks / cs, c0 = (ks - tap * cs) * BK;
+		const int dy = tap / g.r, dx = tap - dy * g.r, pad = g.r / 2;
+		tma_load_4d(a, ta, bar, c0, t.x0 + dx - pad, t.y + dy - pad, t.n);
+	}
+	__device__ static void load_b(const CUtensorMap* tb, const Args& g, int ks, void* b, uint64_t* bar) {
+		const int cs = g.c / BK;
+		const int tap = ks / cs, c0 = (ks - tap * cs) * BK;
+		tma_load_2d(b, tb, bar, tap * g.c + c0, 0);
+	}
+	// This thread holds pixel x0 + rl of the tile for output channels
+	// [k0+c, +32).  Groups of 4 channels are transposed across the 4 lanes of
+	// each quad (two butterfly shuffle stages), after which lane 4j+m holds
+	// channel 4*grp+m of pixels 4j..4j+3: one 16-byte store per lane and
+	// group instead of four 4-byte stores.  Every lane takes part in the
+	// shuffles; bounds are checked at the stores.
 	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
-		const int x = t.x0 + rl;
-		if (x >= g.w) return;
+		const int lane = rl & 31, m = lane & 3;
+		const bool b1 = (m >> 1) & 1, b0 = m & 1;
+		const int xq = t.x0 + (rl - m);  // first pixel of this lane's quad
 		const size_t plane = (size_t)g.h * g.w;
-		float* dst = g.out + ((size_t)t.n * g.k) * plane + (size_t)t.y * g.w + x;
+		float* base = g.out + ((size_t)t.n * g.k) * plane + (size_t)t.y * g.w + xq;
+		const bool vec = g.vec4 && xq + 3 < g.w;
 #pragma unroll
-		for (int i = 0; i < 32; ++i) {
-			const int kk = t.k0 + c + i;
-			if (kk < g.k) dst[(size_t)kk * plane] = v[i];
+		for (int grp = 0; grp < 8; ++grp) {
+			// r[k] = channel 4grp+k of this lane's pixel
+			float r0 = v[4 * grp], r1 = v[4 * grp + 1], r2 = v[4 * grp + 2], r3 = v[4 * grp + 3];
+			// stage 1 (lanes m, m^2): keep the channel pair whose high bit is b1, swap the other
+			{
+				const float s0 = b1 ? r0 : r2, s1 = b1 ? r1 : r3;
+				const float y0 = __shfl_xor_sync(0xffffffffu, s0, 2), y1 = __shfl_xor_sync(0xffffffffu, s1, 2);
+				// now (row p1, col c0): own row for p1 == b1, partner's row otherwise; channels (b1, c0)
+				const float k0 = b1 ? r2 : r0, k1 = b1 ? r3 : r1;  // own values of channels (b1, 0), (b1, 1)
+				r0 = b1 ? y0 : k0;  // pixel (0, b0), channel (b1, 0)
+				r1 = b1 ? y1 : k1;  // pixel (0, b0), channel (b1, 1)
+				r2 = b1 ? k0 : y0;  // pixel (1, b0), channel (b1, 0)
+				r3 = b1 ? k1 : y1;  // pixel (1, b0), channel (b1, 1)
+			}
+			// stage 2 (lanes m, m^1): keep channel low bit b0, swap the other
+			{
+				const float s0 = b0 ? r0 : r1, s1 = b0 ? r2 : r3;
+				const float y0 = __shfl_xor_sync(0xffffffffu, s0, 1), y1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+				const float k0 = b0 ? r1 : r0, k1 = b0 ? r3 : r2;  // own: pixels (0, b0), (1, b0), channel (b1, b0)
+				// pixel (p1, p0) of channel (b1, b0): own when p0 == b0
+				const float q00 = b0 ? y0 : k0, q01 = b0 ? k0 : y0;  // p1 = 0: p0 = 0, 1
+				const float q10 = b0 ? y1 : k1, q11 = b0 ? k1 : y1;  // p1 = 1: p0 = 0, 1
+				r0 = q00; r1 = q01; r2 = q10; r3 = q11;             // pixels 0, 1, 2, 3 of the quad
+			}
+			const int kk = t.k0 + c + 4 * grp + m;
+			if (kk < g.k) {
+				float* dst = base + (size_t)kk * plane;
+				if (vec) {
+					*reinterpret_cast<float4*>(dst) = make_float4(r0, r1, r2, r3);
+				} else {
+					if (xq < g.w) dst[0] = r0;
+					if (xq + 1 < g.w) dst[1] = r1;
+					if (xq + 2 < g.w) dst[2] = r2;
+					if (xq + 3 < g.w) dst[3] = r3;
+				}
+			}
 		}
 	}
 };
 
-// One CTA computes one 128 x BN tile:
-//   warp 0, one lane : TMA producer into a STAGES-deep ring (A 16 KB, B BN*128 B);
-//   warp 1           : allocates BN TMEM columns; one lane issues tcgen05.mma
-//                      (M=128, N=BN, K=16, 4 per slice), commits each slice
-//                      back to the producer;
-//   warps 2..5       : epilogue, tcgen05.ld of their 32 TMEM lanes, stores.
+// The same convolution with every weight slice resident in shared memory for
+// the CTA's lifetime (output channels <= BN and at most NK_RES slices: 3x3 x
+// 64 channels is 9 slices, 144 KB): only input slices stream through the ring,
+// halving the operand traffic from L2.
+struct ConvResPolicy : ConvPolicy {
+	static constexpr int STAGES = 4;
+	static constexpr bool RESIDENT_B = true;
+	static constexpr int NK_RES = 9;
+};
+
+// 3x3 convolution over 64 input channels with resident weights and one A
+// load per filter row: the strip of BM + 2 input pixels of row y + dy - 1
+// (one TMA box, zero fill outside the image) serves the three horizontal
+// taps, whose operands start 0, 1 and 2 rows into the strip.  A traffic per
+// tile drops from 9 to 3 boxes.
+struct ConvStripPolicy : ConvResPolicy {
+	static constexpr bool STRIP = true;
+	static constexpr int R = 3;
+	static constexpr int STRIP_ROWS = BM + R - 1;                          // 130
+	static constexpr uint32_t STRIP_BYTES = STRIP_ROWS * BK * 2;          // 16 640 (the box)
+	static constexpr uint32_t STRIP_STAGE = (STRIP_BYTES + 1023) & ~1023u;  // 17 408
+	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, const Tile& t, int dy, void* a,
+	                                  uint64_t* bar) {
+		tma_load_4d(a, ta, bar, 0, t.x0 - 1, t.y + dy - 1, t.n);
+	}
+};
+
+// Persistent CTAs, each looping over tiles id = blockIdx.x, +gridDim.x, ...:
+//   warp 0, one lane : TMA producer into a STAGES-deep ring (A 16 KB, B BN*128 B),
+//                      running ahead across tile boundaries;
+//   warp 1           : allocates 2*BN TMEM columns (two accumulators); one lane
+//                      issues tcgen05.mma (M=128, N=BN, K=16, 4 per slice) into
+//                      accumulator (tile & 1), commits each slice back to the
+//                      producer and each finished tile to the epilogue;
+//   warps 2..5       : epilogue, tcgen05.ld of their 32 TMEM lanes, stores,
+//                      then release the accumulator to the MMA warp.
+// The epilogue of tile i runs while the MMAs of tile i+1 fill the other
+// accumulator.  Every wait is bounded (tc_common.cuh); on a timeout every
+// role stops, the producer drains its copies, the MMA lane waits for its
+// issued MMAs, and TMEM is freed.
 template <class P>
 __global__ void __launch_bounds__(NTHREADS, 1)
 	tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const typename P::Args g,
 	          const uint32_t idesc) {
 	constexpr int BN = P::BN, STAGES = P::STAGES;
-	constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2, STAGE_BYTES = A_TILE + B_TILE;
+	constexpr bool RES = P::RESIDENT_B;
+	constexpr bool STRIP = P::STRIP;
+	constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2;
+	constexpr uint32_t STAGE_BYTES = STRIP ? P::STRIP_STAGE : (RES ? A_TILE : A_TILE + B_TILE);
+	constexpr uint32_t LOAD_BYTES = STRIP ? P::STRIP_BYTES : STAGE_BYTES;
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-	uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+	uint8_t* bres = base + STAGES * STAGE_BYTES;  // resident B slices (RES only)
+	uint64_t* full = reinterpret_cast<uint64_t*>(bres + (RES ? P::NK_RES * B_TILE : 0));
 	uint64_t* empty = full + STAGES;
-	uint64_t* accum = empty + STAGES;
-	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+	uint64_t* accfull = empty + STAGES;  // [2]
+	uint64_t* accempty = accfull + 2;    // [2]
+	uint64_t* drain = accempty + 2;
+	uint64_t* bready = drain + 1;        // resident B loaded (RES only)
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bready + 1);
 	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const typename P::Tile t = P::tile(g);
-	const int nk = P::nk(g);
+	const int ntiles = P::ntiles(g);
+	const int nk = P::nk(g);                   // K-slices of B (and of A, unless STRIP)
+	const int nload = STRIP ? P::R : nk;       // ring loads per tile
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < STAGES; ++s) {
 			mbar_init(&full[s], 1);
 			mbar_init(&empty[s], 1);
 		}
-		mbar_init(accum, 1);
+		for (int a = 0; a < 2; ++a) {
+			mbar_init(&accfull[a], 1);
+			mbar_init(&accempty[a], 4);  // one arrive per epilogue warp
+		}
+		mbar_init(drain, 1);
+		mbar_init(bready, 1);
 		*abort_flag = 0;
 		fence_mbar_init();
 		tma_prefetch(&ta);
 		tma_prefetch(&tb);
 	}
 	if (warp == 1) {
-		tmem_alloc(tmem_slot, BN);
+		tmem_alloc(tmem_slot, 2 * BN);
 		tmem_relinquish();
 	}
 	tc_fence_before();
@@ -160,62 +280,134 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		// ---- producer
 		int armed[STAGES];
 		for (int s = 0; s < STAGES; ++s) armed[s] = -1;
-		for (int ks = 0; ks < nk; ++ks) {
-			const int s = ks % STAGES;
-			const uint32_t round = ks / STAGES;
-			if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
-			mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-			armed[s] = (int)round;
-			P::load(&ta, &tb, g, t, ks, base + s * STAGE_BYTES, base + s * STAGE_BYTES + A_TILE, &full[s]);
+		if constexpr (RES) {
+			mbar_arrive_expect_tx(bready, (uint32_t)nk * B_TILE);
+			for (int ks = 0; ks < nk; ++ks) P::load_b(&tb, g, ks, bres + ks * B_TILE, bready);
+		}
+		uint32_t q = 0;  // slices issued by this CTA
+		for (int id = blockIdx.x; id < ntiles && !*abort_flag; id += gridDim.x) {
+			const typename P::Tile t = P::tile(g, id);
+			for (int ks = 0; ks < nload; ++ks, ++q) {
+				const int s = (int)(q % STAGES);
+				const uint32_t round = q / STAGES;
+				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
+				mbar_arrive_expect_tx(&full[s], LOAD_BYTES);
+				armed[s] = (int)round;
+				if constexpr (STRIP)
+					P::load_strip(&ta, g, t, ks, base + s * STAGE_BYTES, &full[s]);
+				else if constexpr (RES)
+					P::load_a(&ta, g, t, ks, base + s * STAGE_BYTES, &full[s]);
+				else
+					P::load(&ta, &tb, g, t, ks, base + s * STAGE_BYTES, base + s * STAGE_BYTES + A_TILE, &full[s]);
+			}
 		}
 		if (*abort_flag) {
 			// let every copy this thread started land before the CTA exits
 			volatile int own = 0;
 			for (int s = 0; s < STAGES; ++s)
 				if (armed[s] >= 0) mbar_wait(&full[s], (uint32_t)armed[s] & 1, &own, g.err, kErrTimeoutFull);
+			if constexpr (RES) mbar_wait(bready, 0, &own, g.err, kErrTimeoutFull);
 		}
 	} else if (warp == 1 && lane == 0) {
 		// ---- MMA issuer
-		for (int ks = 0; ks < nk; ++ks) {
-			const int s = ks % STAGES;
-			const uint32_t round = ks / STAGES;
-			if (!mbar_wait(&full[s], round & 1, abort_flag, g.err, kErrTimeoutFull)) break;
+		bool ready = true;
+		if constexpr (RES) ready = mbar_wait(bready, 0, abort_flag, g.err, kErrTimeoutFull);
+		uint32_t q = 0;
+		int i = 0;  // local tile count
+		for (int id = blockIdx.x; ready && id < ntiles && !*abort_flag; id += gridDim.x, ++i) {
+			const int a = i & 1;
+			const uint32_t use = (uint32_t)(i >> 1);
+			if (!mbar_wait(&accempty[a], (use & 1) ^ 1, abort_flag, g.err, kErrTimeoutAccEmpty)) break;
 			tc_fence_after();
-			const uint64_t ad = desc_kmajor_sw128(smem_u32(base + s * STAGE_BYTES));
-			const uint64_t bd = desc_kmajor_sw128(smem_u32(base + s * STAGE_BYTES + A_TILE));
+			const uint32_t acc = tmem + (uint32_t)(a * BN);
+			bool ok = true;
+			for (int ks = 0; ks < nload; ++ks, ++q) {
+				const int s = (int)(q % STAGES);
+				const uint32_t round = q / STAGES;
+				if (!mbar_wait(&full[s], round & 1, abort_flag, g.err, kErrTimeoutFull)) { ok = false; break; }
+				tc_fence_after();
+				if constexpr (STRIP) {
+					// strip ks = filter row dy; taps dx = 0..R-1 start dx rows into it
 #pragma unroll
-			for (int kk = 0; kk < BK / 16; ++kk) mma_f16(tmem, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || kk > 0);
-			mma_commit(&empty[s]);
+					for (int dx = 0; dx < P::R; ++dx) {
+						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * STAGE_BYTES), dx);
+						const uint64_t bd = desc_kmajor_sw128(smem_u32(bres + (ks * P::R + dx) * B_TILE));
+#pragma unroll
+						for (int kk = 0; kk < BK / 16; ++kk)
+							mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || dx > 0 || kk > 0);
+					}
+				} else {
+					const uint64_t ad = desc_kmajor_sw128(smem_u32(base + s * STAGE_BYTES));
+					const uint64_t bd =
+						desc_kmajor_sw128(smem_u32(RES ? bres + ks * B_TILE : base + s * STAGE_BYTES + A_TILE));
+#pragma unroll
+					for (int kk = 0; kk < BK / 16; ++kk)
+						mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || kk > 0);
+				}
+				mma_commit(&empty[s]);
+			}
+			if (!ok) break;
+			mma_commit(&accfull[a]);
 		}
-		mma_commit(accum);
-		// the MMAs issued above finish before TMEM is freed
+		// every MMA issued above finishes before TMEM is freed
+		mma_commit(drain);
 		volatile int own = 0;
-		mbar_wait(accum, 0, &own, g.err, kErrTimeoutAccum);
+		mbar_wait(drain, 0, &own, g.err, kErrTimeoutAccum);
 	} else if (warp >= 2) {
 		// ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (rows of the tile)
-		const bool ok = mbar_wait(accum, 0, abort_flag, g.err, kErrTimeoutAccum);
-		tc_fence_after();
-		if (ok && !*abort_flag) {
-			const int q = warp & 3;
+		const int qd = warp & 3;
+		int i = 0;
+		for (int id = blockIdx.x; id < ntiles; id += gridDim.x, ++i) {
+			const int a = i & 1;
+			const uint32_t use = (uint32_t)(i >> 1);
+			if (!mbar_wait(&accfull[a], use & 1, abort_flag, g.err, kErrTimeoutAccum)) break;
+			tc_fence_after();
+			const typename P::Tile t = P::tile(g, id);
 #pragma unroll 1
 			for (int c = 0; c < BN; c += 32) {
 				float v[32];
-				tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
-				P::store(g, t, 32 * q + lane, c, v);
+				tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * BN + c), v);
+				P::store(g, t, 32 * qd + lane, c, v);
 			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&accempty[a]);
 		}
 	}
 	tc_fence_before();
 	__syncthreads();
 	if (warp == 1) {
 		tc_fence_after();
-		tmem_dealloc(tmem, BN);
+		tmem_dealloc(tmem, 2 * BN);
 	}
 }
 
 template <class P>
 constexpr size_t smem_bytes() {
-	return (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + 1024 + 256;
+	const size_t stage = P::STRIP ? (size_t)P::STRIP_STAGE : (size_t)(BM * BK * 2);
+	return P::RESIDENT_B
+	           ? (size_t)P::STAGES * stage + (size_t)P::NK_RES * (P::BN * BK * 2) + 1024 + 256
+	           : (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + 1024 + 256;
+}
+
+// Persistent grid: as many CTAs as fit on the GPU at once (each holds 2*BN of
+// the 512 TMEM columns of its SM; shared memory admits at most two CTAs per
+// SM, so the columns always suffice), at most one per tile.
+template <class K>
+umi_status persistent_grid(K kern, size_t smem, int ntiles, int tmem_cols, int* grid) {
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+	                         "cudaFuncSetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+	                                              (int)cudaSharedmemCarveoutMaxShared), "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0, per_sm = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NTHREADS, smem),
+	                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
+	per_sm = std::min(per_sm, 512 / tmem_cols);  // co-resident CTAs never wait for TMEM columns
+	if (per_sm < 1) return umi::fail(UMI_ERR_UNSUPPORTED, "tc_kernel: does not fit an SM");
+	*grid = std::max(1, std::min(ntiles, per_sm * sms));
+	return UMI_OK;
 }
 
 // ---- split of fp32 operands into bf16 hi/lo parts, concatenated along K:
@@ -279,11 +471,12 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 	UMI_TRY(map_kmajor(&ta, A, dt, M, K, BM));
 	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
 	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err};
+	if ((int64_t)umi::ceil_div(M, BM) * umi::ceil_div(N, GemmPolicy::BN) > INT32_MAX)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "gemm: too many tiles");
 	constexpr size_t SMEM = smem_bytes<GemmPolicy>();
 	auto kern = tc_kernel<GemmPolicy>;
-	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
-	                         "cudaFuncSetAttribute"));
-	const dim3 grid(umi::ceil_div(N, GemmPolicy::BN), umi::ceil_div(M, BM));
+	int grid = 0;
+	UMI_TRY(persistent_grid(kern, SMEM, GemmPolicy::ntiles(g), 2 * GemmPolicy::BN, &grid));
 	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy::BN));
 	return umi::launch_status("tc_kernel<gemm>");
 }
@@ -341,10 +534,11 @@ umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, 
 	auto enc = encode_fn();
 	if (!enc) return umi::fail(UMI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
 	CUtensorMap ta, tb;
+	const bool strip = r == 3 && c == BK && k <= ConvStripPolicy::BN;
 	{
 		const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
 		const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
-		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)BM, 1, 1};
+		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)(strip ? ConvStripPolicy::STRIP_ROWS : BM), 1, 1};
 		const cuuint32_t es[4] = {1, 1, 1, 1};
 		const CUresult rr = enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
 		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -352,14 +546,28 @@ umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, 
 		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "conv: input tensor map (%d)", (int)rr);
 	}
 	UMI_TRY(map_kmajor(&tb, wt, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, k, r * r * c, ConvPolicy::BN));
-	ConvArgs g{out, n, c, h, w, k, r, umi::ceil_div(w, BM), err};
+	ConvArgs g{out, n, c, h, w, k, r, umi::ceil_div(w, BM), umi::ceil_div(k, ConvPolicy::BN),
+	           umi::aligned(out, 16) && w % 4 == 0, err};
+	const int64_t tiles = (int64_t)n * h * g.xtiles * g.ktiles;
+	if (tiles > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: too many tiles");
+	int grid = 0;
+	if (strip) {
+		constexpr size_t SMEM = smem_bytes<ConvStripPolicy>();
+		auto kern = tc_kernel<ConvStripPolicy>;
+		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvStripPolicy::BN, &grid));
+		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvStripPolicy::BN));
+		return umi::launch_status("tc_kernel<conv, strips>");
+	}
+	if (g.ktiles == 1 && r * r * (c / BK) <= ConvResPolicy::NK_RES) {
+		constexpr size_t SMEM = smem_bytes<ConvResPolicy>();
+		auto kern = tc_kernel<ConvResPolicy>;
+		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvResPolicy::BN, &grid));
+		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvResPolicy::BN));
+		return umi::launch_status("tc_kernel<conv, resident weights>");
+	}
 	constexpr size_t SMEM = smem_bytes<ConvPolicy>();
 	auto kern = tc_kernel<ConvPolicy>;
-	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
-	                         "cudaFuncSetAttribute"));
-	const int64_t tiles = (int64_t)n * h * g.xtiles;
-	if (tiles > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: too many tiles");
-	const dim3 grid((unsigned)tiles, umi::ceil_div(k, ConvPolicy::BN));
+	UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvPolicy::BN, &grid));
 	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvPolicy::BN));
 	return umi::launch_status("tc_kernel<conv>");
 }

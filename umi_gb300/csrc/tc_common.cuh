@@ -15,7 +15,7 @@
 namespace umi_tc {
 
 constexpr unsigned long long kWaitNs = 1000ull * 1000ull * 1000ull;  // 1 s
-enum : int { kErrTimeoutFull = 1, kErrTimeoutEmpty = 2, kErrTimeoutAccum = 4 };
+enum : int { kErrTimeoutFull = 1, kErrTimeoutEmpty = 2, kErrTimeoutAccum = 4, kErrTimeoutAccEmpty = 8 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -29,6 +29,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
 	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
@@ -140,6 +143,17 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t saddr) {
 	d |= (uint64_t)1 << 46;             // descriptor version
 	d |= (uint64_t)2 << 61;             // 128-byte swizzle
 	return d;
+}
+
+// The same layout for an operand that starts `row` 128-byte rows into a
+// 1024-byte-aligned swizzled tile (row need not be a multiple of 8): only
+// the start address moves.  The 128-byte swizzle is a function of the
+// absolute shared-memory address (bits 7-9 select the XOR of the 16-byte
+// chunk), for the TMA that wrote the tile and for the MMA that reads it, so
+// the matrix base offset field stays 0 (checked on the GPU against an FP64
+// convolution for row = 1, 2).
+__device__ __forceinline__ uint64_t desc_kmajor_sw128_rows(uint32_t tile_saddr, int row) {
+	return desc_kmajor_sw128(tile_saddr + 128u * (uint32_t)row);
 }
 
 // Instruction descriptor, kind::f16: fp32 accumulator, A and B of one type
