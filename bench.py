@@ -674,8 +674,9 @@ class LearnedMe:
         self.h_cur = self.d_cur[0].cpu().pin_memory()
         self.h_ref = self.d_ref[0].cpu().pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
-        # forward (7) + centres + refine + audit list + audit search + memset x2 + flag + fallback + count copy
-        self.launches_per_step = 15
+        # inference (downsample, 4 weight packs, layer 1, 3 tensor-core layers, head) + centres + refine
+        # + audit list + audit search + flag + fallback (memsets and the count copy are not kernels)
+        self.launches_per_step = 17
 
     def _estimate(self, k):
         self.net.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
@@ -716,7 +717,8 @@ class LearnedMe:
             "me_learned_u8": self.step,
             "full_me_u8_r64": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.FULL_R,
                                                           out=self.d_mv[i % R]),
-            "menet_forward": lambda i: self.net.forward(self.d_cur[i % R], self.d_ref[i % R]),
+            "menet_forward_fp32_training_pass": lambda i: self.net.forward(self.d_cur[i % R], self.d_ref[i % R]),
+            "menet_infer_tensor_cores": lambda i: self.net.infer(self.d_cur[i % R], self.d_ref[i % R]),
             "refine_r4": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.REFINE_R,
                                                      out=self.d_mv[i % R]),
         }

@@ -238,10 +238,17 @@ umi_status umi_menet_forward(const uint8_t* cur, const uint8_t* ref, int32_t h, 
  * loss (one float, device). */
 umi_status umi_menet_backward(const int32_t* target, int32_t target_stride, int32_t h, int32_t w, const float* params,
                               float* grads, float* loss, void* workspace, size_t workspace_bytes, void* stream);
+/* Inference forward pass (the one umi_me_learned_u8 runs): layer 1 on the
+ * FP32 pipe, layers 2-4 on the tensor cores (tcgen05, bf16 activations,
+ * fp32 accumulation), activations rounded to bf16 after each ReLU; pred (may
+ * be NULL) as umi_menet_forward.  err (device, may be NULL) receives error
+ * bits of bounded waits that gave up (0 when all is well). */
+umi_status umi_menet_infer(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
+                           float* pred, int32_t* err, void* workspace, size_t workspace_bytes, void* stream);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8; step counts from 1). */
 umi_status umi_menet_adam(float* params, const float* grads, float* m, float* v, int32_t step, float lr,
                           void* stream);
-/* Learned motion estimation: forward pass, search centres round(16 * pred)
+/* Learned motion estimation: inference pass (umi_menet_infer), search centres round(16 * pred)
  * clamped to +-(full_r - refine_r), exhaustive search in +-refine_r around
  * them.  Audit: when audit_stride > 0, blocks 0, audit_stride, 2*audit_stride,
  * ... are also searched exhaustively in +-full_r around (0, 0); they take

@@ -115,12 +115,16 @@ def head_features(a4, nby, nbx):
     return t.transpose(1, 3, 0, 2, 4).reshape(nby * nbx, C * 16)
 
 
-def forward(params, cur, ref, bf16=True):
-    """Returns (pred (nblk, 2), activations [x0, a1..a4])."""
+def forward(params, cur, ref, bf16=True, act_bf16=False):
+    """Returns (pred (nblk, 2), activations [x0, a1..a4]).
+
+    act_bf16: round each layer's output (after ReLU) to bfloat16, as the
+    tensor-core inference pass stores its activations."""
     ws, bs, whm, bhv = _weights(params, bf16)
     acts = [downsample(cur, ref)]
     for l in range(4):
-        acts.append(np.maximum(conv(acts[-1], ws[l], bs[l], DIL[l]), 0.0))
+        a = np.maximum(conv(acts[-1], ws[l], bs[l], DIL[l]), 0.0)
+        acts.append(to_bf16(a.astype(np.float32)) if act_bf16 else a)
     h, w = cur.shape
     feat = head_features(acts[-1], h // 16, w // 16)
     return feat @ whm.T + bhv, acts

@@ -65,6 +65,33 @@ def test_menet_forward_matches_oracle(umi, dev, shape):
     assert np.abs(got - want).max() <= 2e-5 * scale + 1e-6, np.abs(got - want).max()
 
 
+@pytest.mark.parametrize("shape", [(64, 96), (144, 528), (272, 1040)])
+def test_menet_infer_matches_oracle(umi, dev, shape):
+    """Tensor-core inference pass vs the FP64 oracle with bf16 activations.
+    Shapes cover partial 128-pixel tiles, several tiles per row, and rows
+    where the dilation-8 taps fall outside the image."""
+    import torch
+    h, w = shape
+    g = np.random.default_rng(h * w)
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = g.integers(0, 256, (h, w), dtype=np.uint8)
+    p = _params(5)
+    net = umi.MeNet(h, w, device=dev, params=p)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    got = net.infer(_t(cur, dev), _t(ref, dev), err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    want, _ = menet.forward(p, cur, ref, bf16=True, act_bf16=True)
+    scale = np.abs(want).max() + 1e-3
+    d = np.abs(got - want)
+    # fp32 accumulation vs fp64 can move an activation across a bf16 rounding
+    # boundary (2^-8 relative); such flips stay far below this bound
+    assert d.max() <= 5e-3 * scale, (d.max(), scale)
+    assert np.median(d) <= 1e-4 * scale
+    # and the tensor-core pass agrees with the fp32 training pass to bf16 precision
+    fp32 = net.forward(_t(cur, dev), _t(ref, dev)).cpu().numpy()
+    assert np.abs(fp32 - got).max() <= 0.05 * scale
+
+
 def test_menet_backward_matches_oracle(umi, dev):
     import torch
     h, w = 64, 96
@@ -112,7 +139,7 @@ def test_learned_entry_refine_audit_fallback(umi, dev):
     c, r = _t(cur, dev), _t(ref, dev)
     nblk = (h // 16) * (w // 16)
     net = umi.MeNet(h, w, device=dev, params=_params(9))
-    pred = net.forward(c, r)
+    pred = net.infer(c, r)  # the pass umi_me_learned_u8 runs
     full_r, refine_r = 24, 4
     centers = torch.clamp(torch.round(pred * 16), -(full_r - refine_r), full_r - refine_r).to(torch.int32).contiguous()
     refined = umi.full_me_u8(c, r, 16, refine_r, centers=centers)

@@ -69,6 +69,7 @@ SIGNATURES = {
     "umi_menet_forward": ([_vp, _vp, _i32, _i32, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "umi_menet_backward": ([_vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "umi_menet_adam": ([_vp, _vp, _vp, _vp, _i32, _f32, _vp], ctypes.c_int),
+    "umi_menet_infer": ([_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "umi_me_learned_u8": ([_vp, _vp, _i32, _i32, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp],
                           ctypes.c_int),
     "umi_bilateral_f32": ([_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp], ctypes.c_int),
@@ -392,6 +393,17 @@ class MeNet:
             pred = torch.empty((self.nblk, 2), dtype=torch.float32, device=self.device)
         check(lib().umi_menet_forward(_ptr(cur), _ptr(ref), self.h, self.w, _ptr(self.params), _ptr(pred),
                                       _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)), "umi_menet_forward")
+        return pred
+
+    def infer(self, cur, ref, pred=None, err=None, stream=None):
+        """Inference forward pass, layers 2-4 on the tensor cores (umi_menet_infer)."""
+        import torch
+        _need(cur, torch.uint8, "cur")
+        _need(ref, torch.uint8, "ref")
+        if pred is None:
+            pred = torch.empty((self.nblk, 2), dtype=torch.float32, device=self.device)
+        check(lib().umi_menet_infer(_ptr(cur), _ptr(ref), self.h, self.w, _ptr(self.params), _ptr(pred), _ptr(err),
+                                    _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)), "umi_menet_infer")
         return pred
 
     def backward(self, target, stride: int = 2, stream=None):

@@ -51,6 +51,8 @@ struct MeGeom {
 	int tasks_per_mb; // ndx * ng
 	int vec_ok;       // ref and cur are 4-byte aligned and w % 4 == 0: word loads / 4-byte cp.async allowed
 	int nx32;         // largest multiple of 32 <= ndx: displacements served by whole warps
+	int ng2;          // argmin search: groups of G2 vertical displacements for the ndx - nx32 leftover columns (0: none)
+	int tasks_pipe;   // argmin search tasks per macroblock: ng*nx32 + ng2*(ndx - nx32), or ndx*ng when ng2 == 0
 	const int32_t* list;        // optional: search only these blocks (slot i -> block list[i])
 	const int32_t* list_count;  // number of valid slots of `list` (device word)
 	int slots;                  // slots covered by the grid (nblk, or the list's capacity)
@@ -314,6 +316,53 @@ __device__ __forceinline__ void me_shift_group(const MeGeom& g, uint32_t* buf, i
 	}
 }
 
+// One search task: horizontal displacement ix, vertical displacements
+// iy0 .. iy0+GG-1 (those < ndx) of the window at `win`; returns the argmin key.
+template <int B, int GG>
+__device__ __forceinline__ uint32_t me_task(const MeGeom& g, const uint32_t* win, int ix, int iy0) {
+	constexpr int BW = B / 4;
+	const uint32_t* cb = win + 4 * g.copy_stride;
+	const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + iy0 * g.win_words;
+	uint32_t ring[GG][BW];
+	uint32_t acc[GG];
+#pragma unroll
+	for (int q = 0; q < GG; ++q) {
+		acc[q] = 0;
+#pragma unroll
+		for (int k = 0; k < BW; ++k) ring[q][k] = wp[q * g.win_words + k];
+	}
+#pragma unroll
+	for (int py = 0; py < B; ++py) {
+		uint32_t cv[BW];
+		if (BW == 4) {
+			const uint4 c4 = *reinterpret_cast<const uint4*>(cb + py * BW);
+			cv[0] = c4.x; cv[1] = c4.y; cv[2 % BW] = c4.z; cv[3 % BW] = c4.w;
+		} else {
+#pragma unroll
+			for (int k = 0; k < BW; ++k) cv[k] = cb[py * BW + k];
+		}
+		if (py > 0) {
+			const int r = py + GG - 1;
+#pragma unroll
+			for (int k = 0; k < BW; ++k) ring[r % GG][k] = wp[r * g.win_words + k];
+		}
+#pragma unroll
+		for (int k = 0; k < BW; ++k)
+#pragma unroll
+			for (int q = 0; q < GG; ++q) acc[q] = sad4_acc(cv[k], ring[(py + q) % GG][k], acc[q]);
+	}
+	uint32_t key = 0xffffffffu;
+#pragma unroll
+	for (int q = 0; q < GG; ++q)
+		if (iy0 + q < g.ndx) key = min(key, (acc[q] << 15) | (uint32_t)((iy0 + q) * g.ndx + ix));
+	return key;
+}
+
+// Vertical displacements per task of the leftover columns (ix >= nx32): at
+// most one warp of short tasks instead of a warp of full-length tasks with
+// few lanes active.
+constexpr int G2 = 5;
+
 template <int B, int G>
 __global__ void __launch_bounds__(512) __maxnreg__((MeRegs<B, G>::value))
 full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
@@ -337,64 +386,32 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 	me_shift_group(g, smem, gi, row0, wd0, rstep, stager);
 	__syncthreads();
 	int cbuf = 0;
-	const int total = g.m * g.tasks_per_mb;
+	const int total = g.m * g.tasks_pipe;
 	while (true) {
 		const int ngi = gi + gridDim.x;
 		const bool has_next = ngi < ngroups && slot_block(g, ngi * g.m) >= 0;
 		uint32_t* cur_buf = smem + cbuf * buf_words;
 		uint32_t* next_buf = smem + (cbuf ^ 1) * buf_words;
 		if (has_next) me_stage_group<B>(g, next_buf, ngi, cur, ref, centers, tid, row0, wd0, rstep, stager);
-		// Search group gi (the tasks of full_me_kernel).
+		// Search group gi: tasks [0, ng*nx32) are whole-warp columns with G
+		// vertical displacements each; the leftover columns follow in tasks of G2.
 		for (int t = tid; t < total; t += blockDim.x) {
-			const int m = t / g.tasks_per_mb;
-			const int rem = t - m * g.tasks_per_mb;
-			int grp, ix;
-			const int main_tasks = g.ng * g.nx32;
-			if (rem < main_tasks) {
-				grp = rem / g.nx32;
-				ix = rem - grp * g.nx32;
-			} else {
-				const int rw = g.ndx - g.nx32, r2 = rem - main_tasks;
-				grp = r2 / rw;
-				ix = g.nx32 + (r2 - grp * rw);
-			}
+			const int m = t / g.tasks_pipe;
+			const int rem = t - m * g.tasks_pipe;
 			if (slot_block(g, gi * g.m + m) < 0) continue;
 			const uint32_t* win = cur_buf + m * g.mb_stride;
-			const uint32_t* cb = win + 4 * g.copy_stride;
-			const uint32_t* wp = win + (ix & 3) * g.copy_stride + (ix >> 2) + grp * G * g.win_words;
-			uint32_t ring[G][BW];
-			uint32_t acc[G];
-#pragma unroll
-			for (int q = 0; q < G; ++q) {
-				acc[q] = 0;
-#pragma unroll
-				for (int k = 0; k < BW; ++k) ring[q][k] = wp[q * g.win_words + k];
+			const int main_tasks = g.ng * g.nx32;
+			uint32_t key;
+			if (rem < main_tasks) {
+				const int grp = rem / g.nx32;
+				const int ix = rem - grp * g.nx32;
+				key = me_task<B, G>(g, win, ix, grp * G);
+			} else {
+				const int rw = g.ndx - g.nx32, r2 = rem - main_tasks;
+				const int grp = r2 / rw;
+				const int ix = g.nx32 + (r2 - grp * rw);
+				key = g.ng2 ? me_task<B, G2>(g, win, ix, grp * G2) : me_task<B, G>(g, win, ix, grp * G);
 			}
-#pragma unroll
-			for (int py = 0; py < B; ++py) {
-				uint32_t cv[BW];
-				if (BW == 4) {
-					const uint4 c4 = *reinterpret_cast<const uint4*>(cb + py * BW);
-					cv[0] = c4.x; cv[1] = c4.y; cv[2 % BW] = c4.z; cv[3 % BW] = c4.w;
-				} else {
-#pragma unroll
-					for (int k = 0; k < BW; ++k) cv[k] = cb[py * BW + k];
-				}
-				if (py > 0) {
-					const int r = py + G - 1;
-#pragma unroll
-					for (int k = 0; k < BW; ++k) ring[r % G][k] = wp[r * g.win_words + k];
-				}
-#pragma unroll
-				for (int k = 0; k < BW; ++k)
-#pragma unroll
-					for (int q = 0; q < G; ++q) acc[q] = sad4_acc(cv[k], ring[(py + q) % G][k], acc[q]);
-			}
-			const int iy0 = grp * G;
-			uint32_t key = 0xffffffffu;
-#pragma unroll
-			for (int q = 0; q < G; ++q)
-				if (iy0 + q < g.ndx) key = min(key, (acc[q] << 15) | (uint32_t)((iy0 + q) * g.ndx + ix));
 			atomicMin(&best[cbuf][m], key);
 		}
 		cp_async_wait_all();
@@ -517,6 +534,8 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.mb_stride = (g.mb_stride + 3) & ~3;         // keep each current block 16-byte aligned
 	g.tasks_per_mb = g.ndx * g.ng;
 	g.nx32 = (g.ndx / 32) * 32;
+	g.ng2 = (g.nx32 > 0 && g.ndx > g.nx32) ? (g.ndx + G2 - 1) / G2 : 0;
+	g.tasks_pipe = g.ng2 ? g.ng * g.nx32 + g.ng2 * (g.ndx - g.nx32) : g.tasks_per_mb;
 	g.vec_ok = umi::aligned(ref, 4) && umi::aligned(cur, 4) && (w % 4) == 0;
 	// Macroblocks per CTA: enough tasks to fill at least ~256 threads, within
 	// 96 KB of shared memory (the argmin search keeps two such buffers) and
@@ -525,22 +544,26 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	const int max_m_smem = std::max(1, (int)((96 * 1024) / (g.mb_stride * 4)));
 	m = std::min(std::min(m, max_m_smem), 64);
 	g.m = m;
-	const int total = m * g.tasks_per_mb;
-	int threads = ((total + 31) / 32) * 32;
-	if (threads > 512) {
-		const int iters = (total + 511) / 512;
-		threads = (((total + iters - 1) / iters) + 31) / 32 * 32;
-	}
+	// Threads: one task each when they fit 512, else as few rounds as possible.
 	// Staging needs one thread per current-block word (b*b/4 <= 64) and per
 	// window word of a row (<= 37).
-	threads = std::max(threads, 64);
+	auto threads_for = [](int total) {
+		int t = ((total + 31) / 32) * 32;
+		if (t > 512) {
+			const int iters = (total + 511) / 512;
+			t = (((total + iters - 1) / iters) + 31) / 32 * 32;
+		}
+		return std::max(t, 64);
+	};
+	const int threads = threads_for(m * g.tasks_per_mb);
 	const size_t smem = (size_t)m * g.mb_stride * 4;
 	const cudaStream_t st = umi::as_stream(stream);
 	umi_status rc;
-	if (!volume && 2 * smem <= 200 * 1024)  // double-buffered persistent search
-		rc = b == 16 ? launch_pipe_b<16>(G, cur, ref, centers, out, g, threads, 2 * smem, st)
-		             : launch_pipe_b<8>(G, cur, ref, centers, out, g, threads, 2 * smem, st);
-	else if (b == 16)
+	if (!volume && 2 * smem <= 200 * 1024) {  // double-buffered persistent search
+		const int tp = threads_for(m * g.tasks_pipe);
+		rc = b == 16 ? launch_pipe_b<16>(G, cur, ref, centers, out, g, tp, 2 * smem, st)
+		             : launch_pipe_b<8>(G, cur, ref, centers, out, g, tp, 2 * smem, st);
+	} else if (b == 16)
 		rc = volume ? launch_b<16, true>(G, cur, ref, centers, out, g, threads, smem, st)
 		            : launch_b<16, false>(G, cur, ref, centers, out, g, threads, smem, st);
 	else

@@ -49,6 +49,8 @@ struct GemmPolicy {
 	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
 	static constexpr int R = 1;
 	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
+	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
+	template <class A> __device__ static int dil(const A&) { return 1; }
 	using Args = GemmArgs;
 	struct Tile { int m0, n0; };
 	// tiles in row-major order of (m-block, n-block): CTAs working at the same
@@ -101,6 +103,8 @@ struct ConvPolicy {
 	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
 	static constexpr int R = 1;
 	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
+	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
+	template <class A> __device__ static int dil(const A&) { return 1; }
 	using Args = ConvArgs;
 	struct Tile { int n, y, x0, k0; };
 	// tile id = ((n*h + y)*xtiles + xt)*ktiles + kt
@@ -206,9 +210,65 @@ struct ConvStripPolicy : ConvResPolicy {
 	static constexpr int STRIP_ROWS = BM + R - 1;                          // 130
 	static constexpr uint32_t STRIP_BYTES = STRIP_ROWS * BK * 2;          // 16 640 (the box)
 	static constexpr uint32_t STRIP_STAGE = (STRIP_BYTES + 1023) & ~1023u;  // 17 408
+	// (defined here: the inherited hook would read ConvPolicy::STRIP_BYTES)
+	__device__ static uint32_t strip_bytes(const Args&) { return STRIP_BYTES; }
 	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, const Tile& t, int dy, void* a,
 	                                  uint64_t* bar) {
 		tma_load_4d(a, ta, bar, 0, t.x0 - 1, t.y + dy - 1, t.n);
+	}
+};
+
+// One 3x3 layer of the motion-proposal network (32 -> 32 channels, dilation
+// d <= 8) on the tensor cores.  Activations are bf16 NHWC with 64-channel
+// pixels (channels 32..63 are zero, so one 128-byte row per pixel feeds
+// K = 64 per tap; the weights of those channels are zero too).  A tile is
+// 128 pixels of one row x 32 output channels (MMA M=128, N=32); the strip of
+// filter row dy holds the 128 + 2d input pixels of row y + (dy-1)d and the
+// three taps start 0, d, 2d rows into it.  Epilogue: + bias, ReLU, bf16, one
+// 128-byte NHWC pixel per thread (upper 64 bytes written as zeros).
+struct MenetArgs {
+	__nv_bfloat16* out;  // (h, w, 64) bf16
+	const float* bias;   // 32
+	int h, w, dil, xtiles;
+	int* err;
+};
+struct MenetConvPolicy {
+	static constexpr int BN = 32, STAGES = 8;
+	static constexpr bool RESIDENT_B = true;
+	static constexpr int NK_RES = 9;
+	static constexpr bool STRIP = true;
+	static constexpr int R = 3, MAXD = 8;
+	static constexpr uint32_t STRIP_BYTES = 0;  // per layer: strip_bytes()
+	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * BK * 2 + 1023) & ~1023u;  // 18 432
+	using Args = MenetArgs;
+	struct Tile { int y, x0; };
+	__host__ __device__ static int ntiles(const Args& g) { return g.h * g.xtiles; }
+	__device__ static Tile tile(const Args& g, int id) { return {id / g.xtiles, (id % g.xtiles) * BM}; }
+	__device__ static int nk(const Args&) { return 9; }
+	__device__ static uint32_t strip_bytes(const Args& g) { return (uint32_t)(BM + 2 * g.dil) * BK * 2; }
+	__device__ static int dil(const Args& g) { return g.dil; }
+	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, const Tile& t, int dy, void* a,
+	                                  uint64_t* bar) {
+		tma_load_4d(a, ta, bar, 0, t.x0 - g.dil, t.y + (dy - 1) * g.dil, 0);
+	}
+	__device__ static void load_b(const CUtensorMap* tb, const Args&, int ks, void* b, uint64_t* bar) {
+		tma_load_2d(b, tb, bar, ks * BK, 0);
+	}
+	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
+		const int x = t.x0 + rl;
+		if (c != 0 || x >= g.w) return;
+		uint32_t q[16];
+#pragma unroll
+		for (int i = 0; i < 16; ++i) {
+			const float a0 = fmaxf(v[2 * i] + g.bias[2 * i], 0.0f), a1 = fmaxf(v[2 * i + 1] + g.bias[2 * i + 1], 0.0f);
+			const __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
+			q[i] = *reinterpret_cast<const uint32_t*>(&b2);
+		}
+		uint4* dst = reinterpret_cast<uint4*>(g.out + ((size_t)t.y * g.w + x) * 64);
+#pragma unroll
+		for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+#pragma unroll
+		for (int i = 4; i < 8; ++i) dst[i] = make_uint4(0u, 0u, 0u, 0u);
 	}
 };
 
@@ -234,7 +294,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	constexpr bool STRIP = P::STRIP;
 	constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2;
 	constexpr uint32_t STAGE_BYTES = STRIP ? P::STRIP_STAGE : (RES ? A_TILE : A_TILE + B_TILE);
-	constexpr uint32_t LOAD_BYTES = STRIP ? P::STRIP_BYTES : STAGE_BYTES;
+	const uint32_t load_bytes = STRIP ? P::strip_bytes(g) : STAGE_BYTES;  // bytes one ring load brings
+	static_assert(!STRIP || P::STRIP_STAGE > 0, "strip policies define their stage size");
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 	uint8_t* bres = base + STAGES * STAGE_BYTES;  // resident B slices (RES only)
@@ -291,7 +352,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 				const int s = (int)(q % STAGES);
 				const uint32_t round = q / STAGES;
 				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
-				mbar_arrive_expect_tx(&full[s], LOAD_BYTES);
+				mbar_arrive_expect_tx(&full[s], load_bytes);
 				armed[s] = (int)round;
 				if constexpr (STRIP)
 					P::load_strip(&ta, g, t, ks, base + s * STAGE_BYTES, &full[s]);
@@ -330,7 +391,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 					// strip ks = filter row dy; taps dx = 0..R-1 start dx rows into it
 #pragma unroll
 					for (int dx = 0; dx < P::R; ++dx) {
-						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * STAGE_BYTES), dx);
+						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * STAGE_BYTES), dx * P::dil(g));
 						const uint64_t bd = desc_kmajor_sw128(smem_u32(bres + (ks * P::R + dx) * B_TILE));
 #pragma unroll
 						for (int kk = 0; kk < BK / 16; ++kk)
@@ -579,3 +640,38 @@ extern "C" umi_status umi_conv2d_fprop_bf16(const void* x_nhwc, const void* w_kr
 	const umi_status s = conv_launch(x_nhwc, w_krsc, out_nchw, n, c, h, w, k, r, err, umi::as_stream(stream));
 	return s == UMI_OK ? umi::ok() : s;
 }
+
+namespace umi {
+
+// One tensor-core layer of the motion-proposal network (see MenetConvPolicy):
+// in/out (h, w, 64) bf16 NHWC, wpack (32, 9*64) bf16 K-major (tap-major, then
+// input channel; channels >= 32 zero), bias 32 fp32.  Used by learned_me.cu.
+umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const float* bias, int h, int w, int dil,
+                         int* err, cudaStream_t st) {
+	if (dil < 1 || dil > MenetConvPolicy::MAXD) return umi::fail(UMI_ERR_UNSUPPORTED, "menet conv: dilation %d", dil);
+	if (!umi::aligned(in, 16) || !umi::aligned(out, 16) || !umi::aligned(wpack, 16))
+		return umi::fail(UMI_ERR_INVALID_ARG, "menet conv: misaligned buffer");
+	auto enc = encode_fn();
+	if (!enc) return umi::fail(UMI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+	CUtensorMap ta, tb;
+	{
+		const cuuint64_t dims[4] = {64, (cuuint64_t)w, (cuuint64_t)h, 1};
+		const cuuint64_t strides[3] = {128, (cuuint64_t)w * 128, (cuuint64_t)h * w * 128};
+		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)(BM + 2 * dil), 1, 1};
+		const cuuint32_t es[4] = {1, 1, 1, 1};
+		const CUresult rr = enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(in), dims, strides, box, es,
+		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "menet conv: activation tensor map (%d)", (int)rr);
+	}
+	UMI_TRY(map_kmajor(&tb, wpack, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 32, 9 * BK, 32));
+	MenetArgs g{static_cast<__nv_bfloat16*>(out), bias, h, w, dil, umi::ceil_div(w, BM), err};
+	constexpr size_t SMEM = smem_bytes<MenetConvPolicy>();
+	auto kern = tc_kernel<MenetConvPolicy>;
+	int grid = 0;
+	UMI_TRY(persistent_grid(kern, SMEM, MenetConvPolicy::ntiles(g), 2 * MenetConvPolicy::BN, &grid));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, MenetConvPolicy::BN));
+	return umi::launch_status("tc_kernel<menet conv>");
+}
+
+}  // namespace umi

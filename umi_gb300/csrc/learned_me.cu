@@ -26,6 +26,11 @@ extern "C" umi_status umi_full_me_u8_list(const uint8_t* cur, const uint8_t* ref
                                           int32_t r, const int32_t* centers, const int32_t* blocks,
                                           const int32_t* n_blocks, int32_t max_blocks, int32_t* mv, void* stream);
 
+namespace umi {
+umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const float* bias, int h, int w, int dil,
+                         int* err, cudaStream_t st);
+}
+
 namespace {
 
 constexpr int CH = 32;       // channels of every hidden layer
@@ -54,6 +59,7 @@ struct Layout {
 struct Work {
 	int H4, W4, P, nbx, nby, nblk, tiles_wg;
 	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, amv, alist, wpart, hpart, lpart;
+	size_t nhwc[2], wtc[NL], err;  // tensor-core inference: bf16 (H4, W4, 64) activations, packed weights
 	size_t bytes;
 	Work(int h, int w) {
 		H4 = h / 4; W4 = w / 4; P = H4 * W4;
@@ -75,6 +81,9 @@ struct Work {
 		wpart = take(sizeof(float) * (size_t)tiles_wg * (CH * CH * 9 + CH));
 		hpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8) * (2 * HEADF + 2));
 		lpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8));
+		for (int i = 0; i < 2; ++i) nhwc[i] = take((size_t)P * 128);
+		for (int l = 0; l < NL; ++l) wtc[l] = take(2 * CH * 9 * 64);
+		err = take(sizeof(int32_t));
 		bytes = o;
 	}
 	template <class T> T* at(void* ws, size_t off) const { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
@@ -385,6 +394,86 @@ __global__ void flag_kernel(int32_t* __restrict__ mv, const int32_t* __restrict_
 	}
 }
 
+// ---- tensor-core inference path: bf16 NHWC activations, 64 channels per
+// pixel (32 used, 32 zero), layers 2-4 on tcgen05 (umi::menet_conv_tc).
+
+// Weights of layer l >= 1 as a (32, 9*64) bf16 K-major matrix: column
+// tap*64 + ci, zero for ci >= 32.
+__global__ void pack_tc_weights_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ out) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < CH * 9 * 64; i += gridDim.x * blockDim.x) {
+		const int co = i / (9 * 64), r = i - co * 9 * 64, tap = r >> 6, ci = r & 63;
+		out[i] = ci < CH ? __float2bfloat16_rn(w[(co * CH + ci) * 9 + tap]) : __float2bfloat16_rn(0.0f);
+	}
+}
+
+// Layer 1 (2 -> 32 channels, dilation 1) on the FP32 pipe, one pixel per
+// thread: + bias, ReLU, bf16, one 128-byte NHWC pixel.
+__global__ void __launch_bounds__(NT) conv1_nhwc_kernel(const float* __restrict__ x0, const __nv_bfloat16* __restrict__ w,
+                                                        const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
+                                                        int H, int W) {
+	__shared__ float ws[2 * 9 * CH];  // [ci][tap][co]
+	for (int i = threadIdx.x; i < CH * 2 * 9; i += NT) {
+		const int co = i / 18, r = i - co * 18;
+		ws[r * CH + co] = __bfloat162float(w[i]);
+	}
+	__syncthreads();
+	const int P = H * W;
+	const int p = blockIdx.x * NT + threadIdx.x;
+	if (p >= P) return;
+	const int y = p / W, x = p - y * W;
+	float in[18];
+#pragma unroll
+	for (int ci = 0; ci < 2; ++ci)
+#pragma unroll
+		for (int tap = 0; tap < 9; ++tap) {
+			const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+			in[ci * 9 + tap] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? x0[(size_t)ci * P + (size_t)yy * W + xx] : 0.0f;
+		}
+	uint32_t q[16];
+#pragma unroll
+	for (int c2 = 0; c2 < CH / 2; ++c2) {
+		float a0 = bias[2 * c2], a1 = bias[2 * c2 + 1];
+#pragma unroll
+		for (int k = 0; k < 18; ++k) {
+			a0 = fmaf(ws[k * CH + 2 * c2], in[k], a0);
+			a1 = fmaf(ws[k * CH + 2 * c2 + 1], in[k], a1);
+		}
+		const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(a0, 0.0f), fmaxf(a1, 0.0f));
+		q[c2] = *reinterpret_cast<const uint32_t*>(&b2);
+	}
+	uint4* dst = reinterpret_cast<uint4*>(out + (size_t)p * 64);
+#pragma unroll
+	for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+#pragma unroll
+	for (int i = 4; i < 8; ++i) dst[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Head on the bf16 NHWC layer-4 activations: one warp per block, lane = channel.
+__global__ void head_nhwc_kernel(const __nv_bfloat16* __restrict__ a4, const float* __restrict__ params, int wh_off,
+                                 int bh_off, float* __restrict__ pred, int W4, int nbx, int nblk) {
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, c = threadIdx.x & 31;
+	if (warp >= nblk) return;
+	const int by = warp / nbx, bx = warp - by * nbx;
+	float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+	for (int cell = 0; cell < 16; ++cell) {
+		const int i = cell >> 2, k = cell & 3;
+		const float v = __bfloat162float(a4[((size_t)(4 * by + i) * W4 + 4 * bx + k) * 64 + c]);
+		const int f = c * 16 + cell;
+		s0 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + f])), v, s0);
+		s1 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + HEADF + f])), v, s1);
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+		s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+	}
+	if (c == 0) {
+		pred[2 * warp] = s0 + params[bh_off];
+		pred[2 * warp + 1] = s1 + params[bh_off + 1];
+	}
+}
+
 // ------------------------------------------------------------------ host side
 const Layout& layout() {
 	static const Layout L;
@@ -428,7 +517,51 @@ umi_status forward(const uint8_t* cur, const uint8_t* ref, int h, int w, const f
 	return umi::launch_status("head_fwd_kernel");
 }
 
+// Inference forward pass with layers 2-4 on the tensor cores; prediction to K.pred.
+umi_status infer(const uint8_t* cur, const uint8_t* ref, int h, int w, const float* params, void* ws, int32_t* err,
+                 cudaStream_t st) {
+	const Layout& L = layout();
+	const Work K(h, w);
+	downsample4_kernel<<<grid_for(2 * (size_t)K.P), NT, 0, st>>>(cur, ref, K.at<float>(ws, K.x0), w, K.H4, K.W4);
+	UMI_TRY(umi::launch_status("downsample4_kernel"));
+	pack_weights_kernel<<<grid_for(CH * 2 * 9), NT, 0, st>>>(params + L.w[0], K.at<__nv_bfloat16>(ws, K.wb[0]), nullptr,
+	                                                          2);
+	UMI_TRY(umi::launch_status("pack_weights_kernel"));
+	for (int l = 1; l < NL; ++l) {
+		pack_tc_weights_kernel<<<grid_for(CH * 9 * 64), NT, 0, st>>>(params + L.w[l], K.at<__nv_bfloat16>(ws, K.wtc[l]));
+		UMI_TRY(umi::launch_status("pack_tc_weights_kernel"));
+	}
+	__nv_bfloat16* a = K.at<__nv_bfloat16>(ws, K.nhwc[0]);
+	__nv_bfloat16* b = K.at<__nv_bfloat16>(ws, K.nhwc[1]);
+	conv1_nhwc_kernel<<<umi::ceil_div(K.P, NT), NT, 0, st>>>(K.at<float>(ws, K.x0), K.at<__nv_bfloat16>(ws, K.wb[0]),
+	                                                         params + L.b[0], a, K.H4, K.W4);
+	UMI_TRY(umi::launch_status("conv1_nhwc_kernel"));
+	for (int l = 1; l < NL; ++l) {
+		UMI_TRY(umi::menet_conv_tc(a, b, K.at<__nv_bfloat16>(ws, K.wtc[l]), params + L.b[l], K.H4, K.W4, DIL[l], err, st));
+		std::swap(a, b);
+	}
+	head_nhwc_kernel<<<umi::ceil_div(K.nblk * 32, NT), NT, 0, st>>>(a, params, L.wh, L.bh, K.at<float>(ws, K.pred),
+	                                                                K.W4, K.nbx, K.nblk);
+	return umi::launch_status("head_nhwc_kernel");
+}
+
 }  // namespace
+
+extern "C" umi_status umi_menet_infer(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
+                                      float* pred, int32_t* err, void* workspace, size_t workspace_bytes, void* stream) {
+	UMI_TRY(check_frame(h, w));
+	if (!cur || !ref || !params || !workspace) return umi::fail(UMI_ERR_INVALID_ARG, "menet_infer: null pointer");
+	const Work K(h, w);
+	if (workspace_bytes < K.bytes) return umi::fail(UMI_ERR_NO_MEMORY, "menet_infer: workspace too small");
+	if (!umi::aligned(workspace, 256)) return umi::fail(UMI_ERR_INVALID_ARG, "menet_infer: workspace alignment");
+	const cudaStream_t st = umi::as_stream(stream);
+	UMI_TRY(infer(cur, ref, h, w, params, workspace, err, st));
+	if (pred)
+		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(pred, K.at<float>(workspace, K.pred), sizeof(float) * 2 * K.nblk,
+		                                         cudaMemcpyDeviceToDevice, st),
+		                         "cudaMemcpyAsync"));
+	return umi::ok();
+}
 
 extern "C" int32_t umi_menet_param_count(void) { return layout().total; }
 
@@ -524,7 +657,7 @@ extern "C" umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, 
 	if (audit_stride < 0) return umi::fail(UMI_ERR_INVALID_ARG, "me_learned: negative audit stride");
 	const cudaStream_t st = umi::as_stream(stream);
 	void* ws = workspace;
-	UMI_TRY(forward(cur, ref, h, w, params, ws, st));
+	UMI_TRY(infer(cur, ref, h, w, params, ws, K.at<int32_t>(ws, K.err), st));
 	int32_t* centers = K.at<int32_t>(ws, K.centers);
 	centers_kernel<<<grid_for(2 * (size_t)K.nblk), NT, 0, st>>>(K.at<float>(ws, K.pred), centers, K.nblk,
 	                                                             full_r - refine_r);
