@@ -676,7 +676,7 @@ class LearnedMe:
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
         # inference (downsample, 4 weight packs, layer 1, 3 tensor-core layers, head) + centres + refine
         # + audit list + audit search + flag + fallback (memsets and the count copy are not kernels)
-        self.launches_per_step = 17
+        self.launches_per_step = 16
 
     def _estimate(self, k):
         self.net.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,

@@ -20,6 +20,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "common.h"
@@ -37,7 +38,7 @@ constexpr int NTHREADS = 192;
 struct GemmArgs {
 	float* C;
 	int M, N, K, ldc;
-	int vec;   // C 16-byte aligned and ldc % 4 == 0
+	int vec;   // C 16-byte aligned and ldc % 4 == 0: stores through the C tensor map
 	int* err;  // optional: error bits of bounded waits that gave up
 };
 
@@ -49,6 +50,7 @@ struct GemmPolicy {
 	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
 	static constexpr int R = 1;
 	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
+	static constexpr bool EPI_TMA = true;  // epilogue through shared memory + TMA tile stores
 	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
 	template <class A> __device__ static int dil(const A&) { return 1; }
 	using Args = GemmArgs;
@@ -103,6 +105,7 @@ struct ConvPolicy {
 	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
 	static constexpr int R = 1;
 	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
+	static constexpr bool EPI_TMA = false;
 	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
 	template <class A> __device__ static int dil(const A&) { return 1; }
 	using Args = ConvArgs;
@@ -234,6 +237,7 @@ struct MenetArgs {
 };
 struct MenetConvPolicy {
 	static constexpr int BN = 32, STAGES = 8;
+	static constexpr bool EPI_TMA = false;
 	static constexpr bool RESIDENT_B = true;
 	static constexpr int NK_RES = 9;
 	static constexpr bool STRIP = true;
@@ -287,8 +291,8 @@ struct MenetConvPolicy {
 // issued MMAs, and TMEM is freed.
 template <class P>
 __global__ void __launch_bounds__(NTHREADS, 1)
-	tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const typename P::Args g,
-	          const uint32_t idesc) {
+	tc_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+	          const __grid_constant__ CUtensorMap tcm, const typename P::Args g, const uint32_t idesc) {
 	constexpr int BN = P::BN, STAGES = P::STAGES;
 	constexpr bool RES = P::RESIDENT_B;
 	constexpr bool STRIP = P::STRIP;
@@ -299,7 +303,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 	uint8_t* bres = base + STAGES * STAGE_BYTES;  // resident B slices (RES only)
-	uint64_t* full = reinterpret_cast<uint64_t*>(bres + (RES ? P::NK_RES * B_TILE : 0));
+	uint8_t* ebuf = bres + (RES ? P::NK_RES * B_TILE : 0);  // epilogue staging, 2 x 4 KB per epilogue warp (EPI_TMA)
+	uint64_t* full = reinterpret_cast<uint64_t*>(ebuf + (P::EPI_TMA ? 8 * 4096 : 0));
 	uint64_t* empty = full + STAGES;
 	uint64_t* accfull = empty + STAGES;  // [2]
 	uint64_t* accempty = accfull + 2;    // [2]
@@ -418,6 +423,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		// ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (rows of the tile)
 		const int qd = warp & 3;
 		int i = 0;
+		uint32_t nst = 0;  // TMA stores issued by this warp
 		for (int id = blockIdx.x; id < ntiles; id += gridDim.x, ++i) {
 			const int a = i & 1;
 			const uint32_t use = (uint32_t)(i >> 1);
@@ -428,11 +434,41 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 			for (int c = 0; c < BN; c += 32) {
 				float v[32];
 				tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * BN + c), v);
+				if constexpr (P::EPI_TMA) {
+					if (g.vec) {
+						// 32 rows x 32 columns through a 4 KB buffer with the 128-byte
+						// swizzle of the C tensor map (chunk j of row r at j ^ (r & 7):
+						// conflict-free), then one TMA store; out-of-range rows and
+						// columns are clipped by the TMA.
+						const int row0 = t.m0 + 32 * qd, col0 = t.n0 + c;
+						if (row0 < g.M && col0 < g.N) {
+							uint8_t* sb = ebuf + (qd * 2 + (nst & 1)) * 4096;
+							if (lane == 0) bulk_wait_read_1();  // the store that last used sb has read it
+							__syncwarp();
+#pragma unroll
+							for (int j = 0; j < 8; ++j)
+								*reinterpret_cast<float4*>(sb + lane * 128 + ((j ^ (lane & 7)) << 4)) =
+									make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+							fence_proxy_async_smem();
+							__syncwarp();
+							if (lane == 0) {
+								tma_store_2d(&tcm, sb, col0, row0);
+								bulk_commit();
+							}
+							++nst;
+						}
+						continue;
+					}
+				}
 				P::store(g, t, 32 * qd + lane, c, v);
 			}
 			tc_fence_before();
 			__syncwarp();
 			if (lane == 0) mbar_arrive(&accempty[a]);
+		}
+		if constexpr (P::EPI_TMA) {
+			if (lane == 0) bulk_wait_all();  // stores done before the CTA exits
+			__syncwarp();
 		}
 	}
 	tc_fence_before();
@@ -446,9 +482,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 template <class P>
 constexpr size_t smem_bytes() {
 	const size_t stage = P::STRIP ? (size_t)P::STRIP_STAGE : (size_t)(BM * BK * 2);
+	const size_t epi = P::EPI_TMA ? 8 * 4096 : 0;
 	return P::RESIDENT_B
-	           ? (size_t)P::STAGES * stage + (size_t)P::NK_RES * (P::BN * BK * 2) + 1024 + 256
-	           : (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + 1024 + 256;
+	           ? (size_t)P::STAGES * stage + (size_t)P::NK_RES * (P::BN * BK * 2) + epi + 1024 + 256
+	           : (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + epi + 1024 + 256;
 }
 
 // Persistent grid: as many CTAs as fit on the GPU at once (each holds 2*BN of
@@ -532,13 +569,26 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 	UMI_TRY(map_kmajor(&ta, A, dt, M, K, BM));
 	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
 	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err};
+	CUtensorMap tc;
+	std::memset(&tc, 0, sizeof(tc));
+	if (g.vec) {
+		auto enc = encode_fn();
+		const cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)M};
+		const cuuint64_t strides[1] = {(cuuint64_t)N * 4};
+		const cuuint32_t box[2] = {32, 32};
+		const cuuint32_t es[2] = {1, 1};
+		const CUresult r = enc(&tc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, es,
+		                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                       CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "gemm: C tensor map (%d)", (int)r);
+	}
 	if ((int64_t)umi::ceil_div(M, BM) * umi::ceil_div(N, GemmPolicy::BN) > INT32_MAX)
 		return umi::fail(UMI_ERR_UNSUPPORTED, "gemm: too many tiles");
 	constexpr size_t SMEM = smem_bytes<GemmPolicy>();
 	auto kern = tc_kernel<GemmPolicy>;
 	int grid = 0;
 	UMI_TRY(persistent_grid(kern, SMEM, GemmPolicy::ntiles(g), 2 * GemmPolicy::BN, &grid));
-	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy::BN));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tc, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy::BN));
 	return umi::launch_status("tc_kernel<gemm>");
 }
 
@@ -616,20 +666,20 @@ umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, 
 		constexpr size_t SMEM = smem_bytes<ConvStripPolicy>();
 		auto kern = tc_kernel<ConvStripPolicy>;
 		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvStripPolicy::BN, &grid));
-		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvStripPolicy::BN));
+		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvStripPolicy::BN));
 		return umi::launch_status("tc_kernel<conv, strips>");
 	}
 	if (g.ktiles == 1 && r * r * (c / BK) <= ConvResPolicy::NK_RES) {
 		constexpr size_t SMEM = smem_bytes<ConvResPolicy>();
 		auto kern = tc_kernel<ConvResPolicy>;
 		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvResPolicy::BN, &grid));
-		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvResPolicy::BN));
+		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvResPolicy::BN));
 		return umi::launch_status("tc_kernel<conv, resident weights>");
 	}
 	constexpr size_t SMEM = smem_bytes<ConvPolicy>();
 	auto kern = tc_kernel<ConvPolicy>;
 	UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvPolicy::BN, &grid));
-	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvPolicy::BN));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvPolicy::BN));
 	return umi::launch_status("tc_kernel<conv>");
 }
 
@@ -670,7 +720,7 @@ umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const flo
 	auto kern = tc_kernel<MenetConvPolicy>;
 	int grid = 0;
 	UMI_TRY(persistent_grid(kern, SMEM, MenetConvPolicy::ntiles(g), 2 * MenetConvPolicy::BN, &grid));
-	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, MenetConvPolicy::BN));
+	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, MenetConvPolicy::BN));
 	return umi::launch_status("tc_kernel<menet conv>");
 }
 
