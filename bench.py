@@ -42,8 +42,8 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # batched_uneven was captured on its 8-image case (12 896 910 px): the cost
 # volume's traffic grows with the pixel count, so it is kept per pixel and
 # scaled to the configured batch.
-NCU_TRAFFIC = {"int_pair_1080p": None, "filter3x3_1024": 4204544 + 0, "gemm_4096": 73273088 + 34650624,
-               "fprop_n32": 67312896 + 206273024, "learned_me_4k": None}
+NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
+               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None}
 NCU_TRAFFIC_PER_PX = {"batched_uneven": (3605180000 + 3255675000) / 12896910}
 
 
