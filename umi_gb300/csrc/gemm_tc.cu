@@ -693,6 +693,9 @@ extern "C" umi_status umi_conv2d_fprop_bf16(const void* x_nhwc, const void* w_kr
 
 namespace umi {
 
+// cuTensorMapEncodeTiled for the other translation units (full_me.cu).
+void* tma_encode_fn() { return reinterpret_cast<void*>(encode_fn()); }
+
 // One tensor-core layer of the motion-proposal network (see MenetConvPolicy):
 // in/out (h, w, 64) bf16 NHWC, wpack (32, 9*64) bf16 K-major (tap-major, then
 // input channel; channels >= 32 zero), bias 32 fp32.  Used by learned_me.cu.
