@@ -19,6 +19,12 @@
 //    clamp/pad rule instead of a 64-thread shared-memory fill; ZeroStrideOpt
 //    is accepted and has no effect on results (the cache deduplicates the
 //    loads it would have saved).
+//
+// Checked builds: compiled with -DUMI_CHECKED, every output write whose
+// physical coordinate falls outside [0, size) of its dimension (size 0 counts
+// as 1) is skipped and sets bit 0 of a device flag word instead (no trap);
+// UMI::checked_flags() synchronises the device and returns (and clears) it.
+// Inputs need no check: their coordinates are clamped into the extent.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -29,6 +35,10 @@
 
 namespace UMI {
 namespace gpu_detail {
+
+#ifdef UMI_CHECKED
+static __device__ unsigned int checked_flags_word = 0;
+#endif
 
 template <class EType, int NI, int NO>
 struct Pointers {
@@ -58,6 +68,9 @@ __device__ __forceinline__ int64_t address(const umi_mem_plan& m, const int (&p)
 			outside |= (cl != c) && ((m.pad_mask >> k) & 1);
 			c = cl;
 		}
+#ifdef UMI_CHECKED
+		if (!CLAMP) outside |= c < 0 || c >= (m.size[k] > 0 ? m.size[k] : 1);  // output outside its extent
+#endif
 		addr += c * m.rowstride[k];
 	}
 	return addr;
@@ -88,6 +101,12 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, con
 		const int mem = OFS + i;
 		bool outside;
 		const int64_t addr = address<false>(plan.mem[Umi::TOTAL_IN + mem], p, a, with_a, outside);
+#ifdef UMI_CHECKED
+		if (outside) {
+			atomicOr(&checked_flags_word, 1u);
+			continue;
+		}
+#endif
 #pragma unroll
 		for (int j = 0; j < MAX_PTR; ++j) {
 			if (j < (int)Slice(PtrNum, 4, Umi::TOTAL_IN + mem)) ptrs.out[mem * MAX_PTR + j][addr] = out[i * MAX_PTR + j];
@@ -203,6 +222,21 @@ inline umi_vdim lower(const ViewDim& v) { return umi_vdim{v.physical_dim_id, v.o
 inline umi_phydim lower(const PhysicalDim& p) { return umi_phydim{p.size, (int32_t)p.mode}; }
 
 }  // namespace gpu_detail
+
+#ifdef UMI_CHECKED
+// Flags raised by checked kernels of this translation unit since the last call
+// (bit 0: an output write outside its extent was skipped); synchronises the device.
+inline unsigned int checked_flags(bool reset = true) {
+	unsigned int v = 0;
+	cudaDeviceSynchronize();
+	cudaMemcpyFromSymbol(&v, gpu_detail::checked_flags_word, sizeof(v));
+	if (reset) {
+		const unsigned int z = 0;
+		cudaMemcpyToSymbol(gpu_detail::checked_flags_word, &z, sizeof(z));
+	}
+	return v;
+}
+#endif
 
 // Generic UMI operator (reference interface: src/UMI_gpu.h:409-422).
 template <

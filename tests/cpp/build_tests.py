@@ -12,7 +12,8 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 BIN = os.path.join(HERE, "_bin")
-PROGRAMS = ["dropin_apps", "generic_fuzz"]
+PROGRAMS = ["dropin_apps", "generic_fuzz", "checked_oob"]
+EXTRA_FLAGS = {"checked_oob": ["-DUMI_CHECKED"]}
 
 sys.path.insert(0, ROOT)
 
@@ -29,7 +30,8 @@ def _build_one(name: str) -> str:
         os.path.join(ROOT, "include", "umi_gb300.h"), os.path.join(ROOT, "oracle", "umi_interp.hpp")]
     if os.path.exists(out) and all(os.path.getmtime(d) <= os.path.getmtime(out) for d in deps if os.path.exists(d)):
         return out
-    cmd = [B.nvcc()] + B.ARCH + ["-std=c++17", "-O2", "-lineinfo", "-I", os.path.join(ROOT, "include"), src, "-o", out,
+    cmd = [B.nvcc()] + B.ARCH + EXTRA_FLAGS.get(name, []) + ["-std=c++17", "-O2", "-lineinfo", "-I",
+                                                            os.path.join(ROOT, "include"), src, "-o", out,
                                  "-L", os.path.dirname(B.LIB), "-lumi_gb300", "-Xlinker",
                                  "-rpath," + os.path.dirname(B.LIB)]
     r = subprocess.run(cmd, capture_output=True, text=True)
