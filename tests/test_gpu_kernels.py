@@ -66,6 +66,20 @@ def test_iimg_all_255_max_value(umi, orc, dev):
     assert np.array_equal(got, orc.iimg_u8_i32(x))
 
 
+def test_iimg_4k_all_255_near_int32_max(umi, dev):
+    # 3840 x 2160 x 255 = 2 115 072 000: the largest 4K integral, 1.5 % below 2^31
+    import torch
+    x = torch.full((2160, 3840), 255, dtype=torch.uint8, device=dev)
+    got = umi.iimg_u8_i32(x)
+    y = torch.arange(1, 2161, device=dev, dtype=torch.int64)[:, None]
+    xx = torch.arange(1, 3841, device=dev, dtype=torch.int64)[None, :]
+    assert int(got[-1, -1].item()) == 2160 * 3840 * 255
+    assert torch.equal(got.to(torch.int64), y * xx * 255)
+    got2 = torch.empty_like(got)
+    assert umi.lib().umi_iimg_u8_i32_noalloc(umi._ptr(x), umi._ptr(got2), 2160, 3840, umi._stream_ptr()) == 0
+    assert torch.equal(got2, got)
+
+
 def test_iimg_unaligned_views(umi, orc, dev):
     import torch
     x = np.random.default_rng(7).integers(0, 256, (50, 61), dtype=np.uint8)
