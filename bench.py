@@ -44,7 +44,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # volume's traffic grows with the pixel count, so it is kept per pixel and
 # scaled to the configured batch.
 NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
-               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None}
+               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None, "coarse_me_4k": None}
 NCU_TRAFFIC_PER_PX = {"batched_uneven": (3605180000 + 3255675000) / 12896910}
 
 
@@ -55,14 +55,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096",
-                                           "fprop_n32", "learned_me_4k"],
+                                           "fprop_n32", "learned_me_4k", "coarse_me_4k"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
-                   "gemm_4096": 3000, "fprop_n32": 3000, "learned_me_4k": 200}[a.workload]
+                   "gemm_4096": 3000, "fprop_n32": 3000, "learned_me_4k": 200, "coarse_me_4k": 2000}[a.workload]
     return a
 
 
@@ -705,7 +705,8 @@ class LearnedMe:
             self._estimate(k)
             regs.append((self.d_mv[k][:, 2].long().sum() / full[:, 2].long().sum()).item() - 1.0)
             fbs.append(int(self.d_nf[k].item()) / self.nblk)
-        ab = self.T.evaluate(self.net, [self.T.EVAL_SEED0 + 2], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT)
+        ab = self.T.evaluate(self.net, [self.T.EVAL_SEED0 + 2], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
+                             coarse=getattr(self, "cme", None))
         return {"mean_sad_regression": float(np.mean(regs)), "fallback_fraction": float(np.mean(fbs)),
                 "sad_threshold": self.thr, "trained_weights": self.trained,
                 "ablation_hit_rate_within_refine": {m: ab[m]["hit"] for m in ab},
@@ -741,8 +742,51 @@ class LearnedMe:
         return nblocks / 1e6
 
 
+class CoarseMe4k(LearnedMe):
+    """Coarse-to-fine motion estimation on the same 4K pairs: 4x4-mean cells
+    searched on a 2-pixel grid within +-60, then the same +-4 refine, audit
+    and fallback (umi_me_coarse_u8).  The learned pipeline and the plain
+    +-64 exhaustive search are timed beside it."""
+    name = "coarse_me_4k"
+    metric = "coarse-to-fine ME Mblocks/s (4K, +-64 judge, +-4 refine, <= 1% mean SAD regression)"
+    dtype = "u8 (search)"
+    step_kernel = "me_coarse_u8"
+
+    def config(self):
+        c = super().config()
+        c.pop("network")
+        c["proposal"] = "rounded 4x4-mean cells, even displacements within +-60 (2-pixel grid), packed SAD, first-min"
+        return c
+
+    def setup(self, dev):
+        super().setup(dev)
+        self.cme = self.U.CoarseMe(self.H, self.W, device=dev)
+        # cells + search + refine + audit list + audit search + flag + fallback
+        self.launches_per_step = 7
+
+    def _estimate(self, k):
+        self.cme.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
+                          out=self.d_mv[k], audit_sums=self.d_sums[k], n_fallback=self.d_nf[k])
+
+    def kernels(self, dev, peaks, n=20):
+        R = self.n_rot
+        rng = (self.FULL_R - self.REFINE_R) & ~1
+        fns = {
+            "me_coarse_u8": self.step,
+            "coarse_centers": lambda i: self.cme.centers(self.d_cur[i % R], self.d_ref[i % R], rng),
+            "full_me_u8_r64": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.FULL_R,
+                                                          out=self.d_mv[i % R]),
+            "me_learned_u8": lambda i: LearnedMe._estimate(self, i % R),
+            "refine_r4": lambda i: self.U.full_me_u8(self.d_cur[i % R], self.d_ref[i % R], self.B, self.REFINE_R,
+                                                     out=self.d_mv[i % R]),
+        }
+        out = {name: time_launches(fn, R, n) for name, fn in fns.items()}
+        absdiff = self.nblk * (rng + 1) ** 2 * 16  # the coarse search: 16 cells per candidate
+        return out, absdiff, None
+
+
 WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm,
-             "fprop_n32": Fprop, "learned_me_4k": LearnedMe}
+             "fprop_n32": Fprop, "learned_me_4k": LearnedMe, "coarse_me_4k": CoarseMe4k}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -979,12 +1023,17 @@ def run_ours(args, wl, dist):
         for name, kt in kms.items():
             kernels[name] = {"ms_per_launch": kt, "Mblocks_per_s": wl.nblk / (kt * 1e-3) / 1e6}
         kernels["speedup_learned_vs_full_search"] = kms["full_me_u8_r64"] / kms["me_learned_u8"]
-        ach = absdiff / (kms["full_me_u8_r64"] * 1e-3)
-        roof = {"bound": "int", "kernel": "full_me_u8 +-64 (judge and fallback)", "achieved": ach / 1e9,
+        if isinstance(wl, CoarseMe4k):
+            kernels["speedup_coarse_vs_full_search"] = kms["full_me_u8_r64"] / kms["me_coarse_u8"]
+            roof_k, roof_name = "coarse_centers", "coarse_cells + coarse_search (the proposal)"
+        else:
+            roof_k, roof_name = "full_me_u8_r64", "full_me_u8 +-64 (judge and fallback)"
+        ach = absdiff / (kms[roof_k] * 1e-3)
+        roof = {"bound": "int", "kernel": roof_name, "achieved": ach / 1e9,
                 "peak": sad_peak / 1e9, "unit": "Gabsdiff/s", "frac": ach / sad_peak,
                 "traffic": NCU_TRAFFIC[wl.name],
                 "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
-                "work_per_launch": absdiff, "ms_per_launch": kms["full_me_u8_r64"]}
+                "work_per_launch": absdiff, "ms_per_launch": kms[roof_k]}
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
             b = wl.BYTES[name] * wl.px
@@ -1017,8 +1066,8 @@ def run_ours(args, wl, dist):
     }
     if sanity is not None:
         key = {IntPair: "sanity_true_mv_recovered", Gemm: "errors_vs_fp64_sampled_rows",
-               Fprop: "errors_vs_fp64", LearnedMe: "quality_vs_exhaustive_search"}.get(type(wl),
-                                                                                           "sanity_max_rel_err_sampled")
+               Fprop: "errors_vs_fp64", LearnedMe: "quality_vs_exhaustive_search",
+               CoarseMe4k: "quality_vs_exhaustive_search"}.get(type(wl), "sanity_max_rel_err_sampled")
         line[key] = sanity
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, sample_s=10.0)
@@ -1057,7 +1106,7 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2, LearnedMe: 8}.get(type(wl), 16)
+    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2, LearnedMe: 8, CoarseMe4k: 8}.get(type(wl), 16)
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()

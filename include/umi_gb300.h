@@ -264,6 +264,27 @@ umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, 
                              int32_t* mv, unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,
                              size_t workspace_bytes, void* stream);
 
+/* Coarse-to-fine motion proposal (no reference counterpart; the fast
+ * proposal beside the learned one).  Cells are rounded 4x4 means
+ * q(img, y, x) = (sum_{u,v<4} img[clamp(y+u)][clamp(x+v)] + 8) >> 4.  For
+ * every 16x16 block, centers (device, nblk x 2 int32) receives the even
+ * displacement (dy, dx) in [-range, range]^2 minimising
+ * sum_{i,j<4} |q(cur, 16by+4i, 16bx+4j) - q(ref, 16by+4i+dy, 16bx+4j+dx)|,
+ * ties to the first in raster order of (dy, dx).  range even, 0..62; h, w
+ * multiples of 16.  workspace: device, 256-byte aligned,
+ * umi_me_coarse_workspace_bytes(h, w) bytes (0: frame unsupported). */
+size_t umi_me_coarse_workspace_bytes(int32_t h, int32_t w);
+umi_status umi_me_coarse_centers_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t range,
+                                    int32_t* centers, void* workspace, size_t workspace_bytes, void* stream);
+/* Motion estimation from the coarse proposal: centres as
+ * umi_me_coarse_centers_u8 with range = (full_r - refine_r) rounded down to
+ * even, then the refine, audit and fallback of umi_me_learned_u8 with the
+ * same arguments and outputs. */
+umi_status umi_me_coarse_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t refine_r,
+                            int32_t full_r, int32_t sad_threshold, int32_t audit_stride, int32_t* mv,
+                            unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
 /* Bilateral filter, float32 (h, w), (2*radius+1)^2 window, radius 1..3.
  * out = sum(w*n) / sum(w) with w = exp(-(n-c)^2 / (2 sigma_r^2)) *
  * ws[dy] * ws[dx], ws[i] = exp(-(i-radius)^2 / (2 sigma_s^2)), c the centre

@@ -50,6 +50,7 @@ def lib():
             "oracle_iimg_u8_i32": [_u8p, _i32p, _I, _I, _I],
             "oracle_full_me_u8": [_u8p, _u8p, _I, _I, _I, _I, ctypes.c_void_p, _I, _i32p, ctypes.c_void_p, _I],
             "oracle_block_sad_u8": [_u8p, _u8p, _I, _I, _I, _I, _I, _I, _I],
+            "oracle_coarse_centers_u8": [_u8p, _u8p, _I, _I, _I, _i32p, _I],
             "oracle_ref_full_me_u8_argmin": [_u8p, _u8p, _I, _I, _I, _I, _i32p, _I, _i32p, _I],
             "oracle_ref_iimg_u8": [_u8p, _i32p, _I, _I],
             "oracle_bilateral_f64": [_f32p, _f64p, _I, _I, _I, ctypes.c_double, ctypes.c_double, _I],
@@ -178,6 +179,15 @@ def ref_iimg_u8(img):
     """The reference's iimg check loop (main/iimg.cu:100-111) on a uint8 frame."""
     img = _c(img, np.uint8); out = np.empty(img.shape, np.int32)
     lib().oracle_ref_iimg_u8(img, out, img.shape[0], img.shape[1])
+    return out
+
+
+def coarse_centers_u8(cur, ref, rng, threads=0):
+    """Coarse proposal centres (nblk, 2) int32: the even displacement within
+    +-rng minimising the SAD of 4x4-mean cells (umi_oracle.h)."""
+    cur = _c(cur, np.uint8); ref = _c(ref, np.uint8); h, w = cur.shape
+    out = np.empty(((h // 16) * (w // 16), 2), np.int32)
+    lib().oracle_coarse_centers_u8(cur, ref, h, w, rng, out, threads)
     return out
 
 

@@ -227,6 +227,46 @@ void oracle_full_me_u8(const uint8_t* cur, const uint8_t* ref, int h, int w, int
 	}
 }
 
+static int box_q(const uint8_t* img, int h, int w, int y, int x) {
+	int s = 0;
+	for (int u = 0; u < 4; ++u) {
+		const uint8_t* row = img + (size_t)clampi(y + u, 0, h - 1) * w;
+		for (int v = 0; v < 4; ++v) s += row[clampi(x + v, 0, w - 1)];
+	}
+	return (s + 8) >> 4;
+}
+
+void oracle_coarse_centers_u8(const uint8_t* cur, const uint8_t* ref, int h, int w, int range, int32_t* centers,
+                              int threads) {
+	const int nby = h / 16, nbx = w / 16, m = range / 2;
+	/* q(ref) at every even position (2 y2, 2 x2) a block's candidates reach:
+	 * y2 = 8 by + 2 i + dy/2 in [-m, 8 nby + m) */
+	const int qh = 8 * nby + 2 * m, qw = 8 * nbx + 2 * m;
+	int* q = (int*)malloc(sizeof(int) * (size_t)qh * qw);
+#pragma omp parallel for num_threads(nthreads(threads)) schedule(static)
+	for (int y2 = 0; y2 < qh; ++y2)
+		for (int x2 = 0; x2 < qw; ++x2) q[(size_t)y2 * qw + x2] = box_q(ref, h, w, 2 * (y2 - m), 2 * (x2 - m));
+#pragma omp parallel for num_threads(nthreads(threads)) schedule(dynamic, 4)
+	for (int blk = 0; blk < nby * nbx; ++blk) {
+		const int by = blk / nbx, bx = blk % nbx;
+		int c[16];
+		for (int i = 0; i < 4; ++i)
+			for (int j = 0; j < 4; ++j) c[4 * i + j] = box_q(cur, h, w, 16 * by + 4 * i, 16 * bx + 4 * j);
+		int best = 0x7fffffff, bdy = 0, bdx = 0;
+		for (int dy2 = -m; dy2 <= m; ++dy2)
+			for (int dx2 = -m; dx2 <= m; ++dx2) {
+				int s = 0;
+				for (int i = 0; i < 4; ++i)
+					for (int j = 0; j < 4; ++j)
+						s += abs(c[4 * i + j] - q[(size_t)(8 * by + 2 * i + dy2 + m) * qw + (8 * bx + 2 * j + dx2 + m)]);
+				if (s < best) { best = s; bdy = 2 * dy2; bdx = 2 * dx2; }
+			}
+		centers[2 * (size_t)blk] = bdy;
+		centers[2 * (size_t)blk + 1] = bdx;
+	}
+	free(q);
+}
+
 void oracle_ref_full_me_u8_argmin(const uint8_t* cur, const uint8_t* ref, int h, int w, int b, int r,
                                   const int32_t* blocks, int n_blocks, int32_t* mv, int threads) {
 	const int nbx = w / b;

@@ -69,6 +69,14 @@ void oracle_ref_full_me_u8_argmin(const uint8_t* cur, const uint8_t* ref, int h,
 /* The reference's iimg loop (main/iimg.cu:100-111) on a uint8 frame:
  * row prefix into out, then column prefix in place (timed CPU baseline). */
 void oracle_ref_iimg_u8(const uint8_t* in, int32_t* out, int h, int w);
+/* Coarse motion proposal (no reference counterpart).  Cells are rounded 4x4
+ * means q(img, y, x) = (sum_{u,v<4} img[clamp(y+u)][clamp(x+v)] + 8) >> 4.
+ * For every 16x16 block (h/16 x w/16, row-major) writes centers[2 blk ..] =
+ * the even displacement (dy, dx) in [-range, range]^2 minimising
+ * sum_{i,j<4} |q(cur, 16by+4i, 16bx+4j) - q(ref, 16by+4i+dy, 16bx+4j+dx)|,
+ * ties to the first in raster order of (dy, dx).  range is even. */
+void oracle_coarse_centers_u8(const uint8_t* cur, const uint8_t* ref, int h, int w, int range, int32_t* centers,
+                              int threads);
 /* SAD of one block at one displacement (same clamping rule). */
 int32_t oracle_block_sad_u8(const uint8_t* cur, const uint8_t* ref, int h, int w, int b, int by, int bx, int dy, int dx);
 /* Bilateral filter, (2r+1)^2 window, spatial weight exp(-d^2/(2 s_s^2)) per

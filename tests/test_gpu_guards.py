@@ -142,3 +142,22 @@ def test_checked_build_flags_out_of_extent_writes(umi):
     assert d["valid"] == {"status": 0, "flags": 0, "guard_ok": 1, "written": 64}
     assert d["oob"]["status"] == 0 and d["oob"]["flags"] == 1 and d["oob"]["guard_ok"] == 1
     assert d["oob"]["written"] == 22  # points 0..21 land at 0, 3, ..., 63; the rest are skipped
+
+
+def test_guards_coarse_me(umi, dev):
+    import torch
+    h, w = 144, 528
+    g = torch.Generator(device=dev).manual_seed(5)
+    cur = torch.randint(0, 256, (h, w), generator=g, device=dev, dtype=torch.uint8)
+    ref = torch.randint(0, 256, (h, w), generator=g, device=dev, dtype=torch.uint8)
+    cme = umi.CoarseMe(h, w, device=dev)
+    nblk = (h // 16) * (w // 16)
+    for rng in (0, 30, 62):
+        full, cen = _guarded((nblk, 2), torch.int32, dev)
+        cme.centers(cur, ref, rng, out=cen)
+        torch.cuda.synchronize()
+        assert _guards_ok(full), rng
+    full, mv = _guarded((nblk, 3), torch.int32, dev)
+    cme.estimate(cur, ref, 4, 24, sad_threshold=500, audit_stride=7, out=mv)
+    torch.cuda.synchronize()
+    assert _guards_ok(full)

@@ -157,6 +157,35 @@ def test_full_me_u8_centers(umi, orc, dev):
         assert tuple(got[i]) == (best[1], best[2], best[0])
 
 
+@pytest.mark.parametrize("r", [1, 2, 3, 4, 5, 6, 7])
+def test_full_me_small_range_centers(umi, orc, dev, r):
+    # the register-only small-range search: centres that push windows past every frame edge
+    import torch
+    g = np.random.default_rng(40 + r)
+    h, w = 80, 112
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = g.integers(0, 256, (h, w), dtype=np.uint8)
+    n = (h // 16) * (w // 16)
+    centers = g.integers(-30, 31, (n, 2)).astype(np.int32)
+    centers[:4] = [[-40, -40], [40, 40], [0, -3], [5, 0]]
+    got = umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, r, centers=_t(centers, dev)).cpu().numpy()
+    for i in range(n):
+        by, bx = divmod(i, w // 16)
+        best = None
+        for dy in range(centers[i, 0] - r, centers[i, 0] + r + 1):
+            for dx in range(centers[i, 1] - r, centers[i, 1] + r + 1):
+                s = orc.block_sad_u8(cur, ref, 16, by, bx, dy, dx)
+                if best is None or s < best[0]:
+                    best = (s, dy, dx)
+        assert tuple(got[i]) == (best[1], best[2], best[0]), i
+    # without centres: identical to the oracle's search around (0, 0); flat frames tie to the first
+    assert np.array_equal(umi.full_me_u8(_t(cur, dev), _t(ref, dev), 16, r).cpu().numpy(),
+                          orc.full_me_u8(cur, ref, 16, r))
+    flat = umi.full_me_u8(torch.full((32, 48), 3, dtype=torch.uint8, device=dev),
+                          torch.full((32, 48), 5, dtype=torch.uint8, device=dev), 16, r).cpu().numpy()
+    assert np.all(flat[:, :2] == -r) and np.all(flat[:, 2] == 512)
+
+
 def test_full_me_sad_volume(umi, orc, dev):
     g = np.random.default_rng(12)
     cur = g.integers(0, 256, (48, 64), dtype=np.uint8)

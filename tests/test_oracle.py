@@ -138,3 +138,50 @@ def test_me_pair_true_motion_is_found(orc):
     inner = [by * nbx + bx for by in range(1, nby - 1) for bx in range(1, nbx - 1)]
     hit = np.mean([(mv[i, 0], mv[i, 1]) == tuple(true_mv[i]) for i in inner])
     assert hit > 0.9
+
+
+def _coarse_numpy(cur, ref, rng):
+    """The coarse proposal restated from its definition with numpy (independent of the C oracle)."""
+    h, w = cur.shape
+    def q(img, y, x):  # (n,) y, (n,) x -> rounded 4x4 means, coordinates clamped
+        yy = np.clip(y[:, None, None] + np.arange(4)[None, :, None], 0, h - 1)
+        xx = np.clip(x[:, None, None] + np.arange(4)[None, None, :], 0, w - 1)
+        return (img[yy, xx].astype(np.int64).sum(axis=(1, 2)) + 8) >> 4
+    nby, nbx = h // 16, w // 16
+    out = np.zeros((nby * nbx, 2), np.int32)
+    ii, jj = np.meshgrid(np.arange(4), np.arange(4), indexing="ij")
+    for blk in range(nby * nbx):
+        by, bx = divmod(blk, nbx)
+        ys, xs = (16 * by + 4 * ii).ravel(), (16 * bx + 4 * jj).ravel()
+        c = q(cur, ys, xs)
+        best = None
+        for dy in range(-rng, rng + 1, 2):
+            for dx in range(-rng, rng + 1, 2):
+                s = int(np.abs(c - q(ref, ys + dy, xs + dx)).sum())
+                if best is None or s < best[0]:
+                    best = (s, dy, dx)
+        out[blk] = best[1:]
+    return out
+
+
+@pytest.mark.parametrize("h,w,rng", [(32, 48, 6), (48, 32, 10), (16, 16, 0), (16, 64, 2), (48, 64, 8)])
+def test_coarse_centers_match_numpy(orc, h, w, rng):
+    g = np.random.default_rng(h + w + rng)
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = g.integers(0, 256, (h, w), dtype=np.uint8)
+    assert np.array_equal(orc.coarse_centers_u8(cur, ref, rng), _coarse_numpy(cur, ref, rng))
+    if h >= 48 and w >= 48:
+        # a planted displacement is found exactly: block (1, 1) of moved = ref at (+6, -4)
+        moved = np.roll(ref, (-6, 4), axis=(0, 1))
+        assert (orc.coarse_centers_u8(moved, ref, rng)[w // 16 + 1] == [6, -4]).all()
+
+
+def test_coarse_proposal_lands_near_true_motion(orc):
+    # the property the proposal exists for: on the 4K-style pairs (per-block shifts
+    # N(0, 16^2) clipped to +-64) almost every block's centre lies within +-4 of the
+    # planted motion, so a +-4 refine around it holds the optimum
+    from umi_gb300 import workloads
+    cur, ref, true_mv = workloads.me_pair(seed=21, h=544, w=960, shift_sigma=16.0, max_shift=64)
+    c = orc.coarse_centers_u8(cur, ref, 60)
+    near = np.all(np.abs(c - np.clip(true_mv, -60, 60)) <= 4, axis=1)
+    assert near.mean() > 0.95, near.mean()

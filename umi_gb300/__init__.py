@@ -72,6 +72,9 @@ SIGNATURES = {
     "umi_menet_infer": ([_vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "umi_me_learned_u8": ([_vp, _vp, _i32, _i32, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp],
                           ctypes.c_int),
+    "umi_me_coarse_workspace_bytes": ([_i32, _i32], _sz),
+    "umi_me_coarse_centers_u8": ([_vp, _vp, _i32, _i32, _i32, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "umi_me_coarse_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "umi_bilateral_f32": ([_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp], ctypes.c_int),
     "umi_wfilter3x3_pp_f32": ([_vp, _vp, _vp, _i32, _i32, _vp], ctypes.c_int),
     "umi_cost_volume_dot_f32": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
@@ -436,6 +439,54 @@ class MeNet:
         check(lib().umi_me_learned_u8(_ptr(cur), _ptr(ref), self.h, self.w, _ptr(self.params), refine_r, full_r,
                                       sad_threshold, audit_stride, _ptr(out), _ptr(audit_sums), _ptr(n_fallback),
                                       _ptr(self.ws), self.ws.numel(), _stream_ptr(stream)), "umi_me_learned_u8")
+        return out, audit_sums, n_fallback
+
+
+class CoarseMe:
+    """Coarse-to-fine motion proposal (umi_me_coarse_centers_u8 / umi_me_coarse_u8):
+    the even displacement minimising the SAD of 4x4-mean cells, then the same
+    refine / audit / fallback stage as the learned proposal.  Holds a workspace
+    for one frame size on one CUDA device."""
+
+    def __init__(self, h: int, w: int, device="cuda"):
+        import torch
+        self.h, self.w = h, w
+        self.device = torch.device(device)
+        nbytes = lib().umi_me_coarse_workspace_bytes(h, w)
+        if nbytes == 0:
+            raise ValueError(f"frame {h}x{w} unsupported (h, w must be multiples of 16)")
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        self.nblk = (h // 16) * (w // 16)
+
+    def centers(self, cur, ref, rng: int = 60, out=None, stream=None):
+        """Proposal centres (nblk, 2) int32, even, within +-rng."""
+        import torch
+        _need(cur, torch.uint8, "cur")
+        _need(ref, torch.uint8, "ref")
+        if out is None:
+            out = torch.empty((self.nblk, 2), dtype=torch.int32, device=self.device)
+        check(lib().umi_me_coarse_centers_u8(_ptr(cur), _ptr(ref), self.h, self.w, rng, _ptr(out), _ptr(self.ws),
+                                             self.ws.numel(), _stream_ptr(stream)), "umi_me_coarse_centers_u8")
+        return out
+
+    def estimate(self, cur, ref, refine_r: int = 4, full_r: int = 64, sad_threshold: int = (1 << 31) - 1,
+                 audit_stride: int = 0, out=None, audit_sums=None, n_fallback=None, stream=None):
+        """Coarse proposal + refine + audit + fallback (umi_me_coarse_u8); the
+        proposal range is (full_r - refine_r) rounded down to even.
+
+        Returns (mv (nblk, 3) int32, audit_sums (2,) int64, n_fallback (1,) int32)."""
+        import torch
+        if out is None:
+            out = torch.empty((self.nblk, 3), dtype=torch.int32, device=self.device)
+        if audit_sums is None:
+            audit_sums = torch.zeros(2, dtype=torch.int64, device=self.device)
+        if n_fallback is None:
+            n_fallback = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _need(cur, torch.uint8, "cur")
+        _need(ref, torch.uint8, "ref")
+        check(lib().umi_me_coarse_u8(_ptr(cur), _ptr(ref), self.h, self.w, refine_r, full_r, sad_threshold,
+                                     audit_stride, _ptr(out), _ptr(audit_sums), _ptr(n_fallback), _ptr(self.ws),
+                                     self.ws.numel(), _stream_ptr(stream)), "umi_me_coarse_u8")
         return out, audit_sums, n_fallback
 
 

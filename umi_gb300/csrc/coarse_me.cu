@@ -1,0 +1,251 @@
+// Coarse-to-fine motion proposal for block motion estimation (sm_103a).
+//
+// No counterpart in the reference.  Every 16x16 block of `cur` is reduced to
+// 4 x 4 cells, each the rounded mean of a 4x4 pixel patch, and `ref` is
+// reduced the same way at every even pixel position:
+//   q(img, y, x) = (sum_{u,v < 4} img[clamp(y + u)][clamp(x + v)] + 8) >> 4
+// (coordinates clamped to the frame: edge replication, the boundary rule of
+// the exhaustive search).  The proposal for block (by, bx) is the
+// displacement (dy, dx), both even and within +-range, that minimises
+//   sum_{i,j < 4} | q(cur, 16by + 4i, 16bx + 4j) - q(ref, 16by + 4i + dy, 16bx + 4j + dx) |,
+// ties to the first displacement in raster order of (dy, dx).  A search on a
+// 2-pixel grid over box-filtered frames: 1/64 of the absolute differences of
+// the exhaustive search over the same range.  The refine, audit and fallback
+// stage (me_pipeline.h) then turns it into the final vectors.
+//
+// Layout.  The reference cells at even positions (2 y2, 2 x2) are split by the
+// parities (py, px) of (y2, x2) into four u8 planes with 16-cell margins,
+//   plane[2 py + px][16 + a][16 + b] = q(ref, 4a + 2py, 4b + 2px),
+//   a in [-16, 4 nby + 16), b in [-16, 4 nbx + 16),
+// so that candidate (dy, dx) = (2 (2A + py), 2 (2B + px)) reads row
+// 16 + 4by + i + A, bytes 16 + 4bx + B .. +3 of plane 2py + px for cell row i:
+// the four cells of a row are one unaligned word, one vabsdiff4 per cell row.
+// cur's cells are four words per block.
+//
+// Search kernel: one CTA per block, one warp per plane, one lane per
+// candidate row A holding 32 candidate columns in registers; the argmin key
+// (sad << 12) | raster index is reduced per warp, then over the four warps.
+#include <algorithm>
+#include <climits>
+
+#include "common.h"
+#include "me_pipeline.h"
+
+namespace {
+
+constexpr int NT = 256;
+constexpr int MARGIN = 16;  // cells on each side of a plane
+constexpr int WIN_ROWS = 35;  // plane rows a block's candidates touch: 4 cell rows + A in [-16, 15]
+constexpr int WIN_WORDS = 9;  // words of a plane row a block's candidates touch: 4 cells + B in [-16, 15]
+
+__device__ __forceinline__ uint32_t sad4_acc(uint32_t a, uint32_t b, uint32_t c) {
+	uint32_t d;
+	asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+	return d;
+}
+
+// Four cells q(img, y0, x0 + 4 j), j = 0..3, packed little-endian.
+__device__ uint32_t box_word(const uint8_t* __restrict__ img, int h, int w, int y0, int x0, bool words) {
+	uint32_t s[4] = {0, 0, 0, 0};
+	if (words && x0 >= 0 && x0 + 16 <= w) {
+		// the 16 columns lie inside the row: aligned word loads, realigned by prmt
+		const int xa = x0 & ~3, sh = x0 & 3;
+		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const uint32_t* row = reinterpret_cast<const uint32_t*>(img + (size_t)min(max(y0 + u, 0), h - 1) * w + xa);
+			uint32_t v[5];
+#pragma unroll
+			for (int k = 0; k < 4; ++k) v[k] = __ldg(row + k);
+			v[4] = sh ? __ldg(row + 4) : 0u;  // in the row: xa + 20 <= w when sh != 0 (w % 4 == 0)
+#pragma unroll
+			for (int j = 0; j < 4; ++j) s[j] = sad4_acc(__byte_perm(v[j], v[j + 1], sel), 0u, s[j]);
+		}
+	} else {
+#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			const uint8_t* row = img + (size_t)min(max(y0 + u, 0), h - 1) * w;
+#pragma unroll
+			for (int j = 0; j < 4; ++j)
+#pragma unroll
+				for (int v = 0; v < 4; ++v) s[j] += __ldg(row + min(max(x0 + 4 * j + v, 0), w - 1));
+		}
+	}
+	return ((s[0] + 8) >> 4) | (((s[1] + 8) >> 4) << 8) | (((s[2] + 8) >> 4) << 16) | (((s[3] + 8) >> 4) << 24);
+}
+
+struct CoarseGeom {
+	int h, w, nby, nbx, nblk, pr, pw;  // pr x pw: rows x bytes of one plane
+	size_t plane_bytes;
+	CoarseGeom(int h_, int w_) : h(h_), w(w_) {
+		nby = h / 16; nbx = w / 16; nblk = nby * nbx;
+		pr = 4 * nby + 2 * MARGIN; pw = 4 * nbx + 2 * MARGIN;
+		plane_bytes = (size_t)pr * pw;
+	}
+};
+
+// cells[4 blk + i] = cells of cur's block row i; planes as described above.
+// One thread per output word.
+__global__ void __launch_bounds__(NT) coarse_cells_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
+                                                          CoarseGeom g, bool words, uint32_t* __restrict__ cells,
+                                                          uint32_t* __restrict__ planes) {
+	const int pww = g.pw / 4;
+	const size_t nplane = 4 * (size_t)g.pr * pww, n = nplane + 4 * (size_t)g.nblk;
+	for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+		if (e < nplane) {
+			const int p = (int)(e / ((size_t)g.pr * pww));
+			const int r = (int)(e - (size_t)p * g.pr * pww);
+			const int row = r / pww, k = r - row * pww;
+			const int py = p >> 1, px = p & 1;
+			// cells b = 4k - 16 + j, j = 0..3: pixels x = 4b + 2px = 16k - 64 + 2px + 4j
+			planes[e] = box_word(ref, g.h, g.w, 4 * (row - MARGIN) + 2 * py, 16 * k - 4 * MARGIN + 2 * px, words);
+		} else {
+			const int c = (int)(e - nplane), blk = c >> 2, i = c & 3;
+			const int by = blk / g.nbx, bx = blk - by * g.nbx;
+			cells[c] = box_word(cur, g.h, g.w, 16 * by + 4 * i, 16 * bx, words);
+		}
+	}
+}
+
+__global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __restrict__ cells,
+                                                            const uint32_t* __restrict__ planes, CoarseGeom g, int m,
+                                                            int32_t* __restrict__ centers) {
+	__shared__ uint32_t win[4][WIN_ROWS][WIN_WORDS];  // row stride 9 words: lanes on distinct rows hit distinct banks
+	__shared__ int best[4];
+	const int blk = blockIdx.x, by = blk / g.nbx, bx = blk - by * g.nbx;
+	const int pww = g.pw / 4;
+	const size_t plane_words = (size_t)g.pr * pww;
+	for (int e = threadIdx.x; e < 4 * WIN_ROWS * WIN_WORDS; e += blockDim.x) {
+		const int p = e / (WIN_ROWS * WIN_WORDS), r = (e - p * WIN_ROWS * WIN_WORDS) / WIN_WORDS;
+		const int k = e - p * WIN_ROWS * WIN_WORDS - r * WIN_WORDS;
+		// plane row 4 by + r < 4 nby + 31 < pr; word bx + k <= nbx + 7 < pww
+		win[p][r][k] = __ldg(planes + p * plane_words + (size_t)(4 * by + r) * pww + bx + k);
+	}
+	uint32_t c[4];
+#pragma unroll
+	for (int i = 0; i < 4; ++i) c[i] = __ldg(cells + 4 * (size_t)blk + i);
+	__syncthreads();
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
+	const int A = -((m + py) >> 1) + lane;  // first row: ceil((-m - py) / 2)
+	const int dy2 = 2 * A + py;
+	int key = INT_MAX;
+	if (dy2 <= m) {  // A <= 15, window rows 16 + A + i in [0, 34]
+		uint32_t cost[32];
+#pragma unroll
+		for (int t = 0; t < 32; ++t) cost[t] = 0;
+#pragma unroll
+		for (int i = 0; i < 4; ++i) {
+			const uint32_t* row = win[warp][16 + A + i];
+			uint32_t v[WIN_WORDS];
+#pragma unroll
+			for (int k = 0; k < WIN_WORDS; ++k) v[k] = row[k];
+#pragma unroll
+			for (int t = 0; t < 32; ++t) {
+				// candidate column B = t - 16: bytes t .. t + 3 of the window row
+				const uint32_t r4 = (t & 3) ? __byte_perm(v[t >> 2], v[(t >> 2) + 1], 0x3210u + 0x1111u * (t & 3))
+				                            : v[t >> 2];
+				cost[t] = sad4_acc(c[i], r4, cost[t]);
+			}
+		}
+		const int nd = 2 * m + 1;
+#pragma unroll
+		for (int t = 0; t < 32; ++t) {
+			const int dx2 = 2 * (t - 16) + px;
+			if (dx2 >= -m && dx2 <= m) key = min(key, (int)(cost[t] << 12) | ((dy2 + m) * nd + dx2 + m));
+		}
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+	if (lane == 0) best[warp] = key;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		const int k = min(min(best[0], best[1]), min(best[2], best[3]));
+		const int idx = k & 4095, nd = 2 * m + 1;
+		centers[2 * blk] = 2 * (idx / nd - m);
+		centers[2 * blk + 1] = 2 * (idx % nd - m);
+	}
+}
+
+// ---- workspace
+struct CoarseWork {
+	size_t cells, planes, centers, list, count, amv, alist, bytes;
+	explicit CoarseWork(const CoarseGeom& g) {
+		size_t o = 0;
+		auto take = [&](size_t n) { size_t r = o; o += (n + 255) & ~size_t(255); return r; };
+		cells = take(16 * (size_t)g.nblk);
+		planes = take(4 * g.plane_bytes);
+		centers = take(sizeof(int32_t) * 2 * g.nblk);
+		list = take(sizeof(int32_t) * g.nblk);
+		count = take(sizeof(int32_t) * 4);
+		amv = take(sizeof(int32_t) * 3 * g.nblk);
+		alist = take(sizeof(int32_t) * g.nblk);
+		bytes = o;
+	}
+	template <class T> T* at(void* ws, size_t off) const { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+};
+
+umi_status check_frame(int h, int w) {
+	if (h < 16 || w < 16) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: frame %dx%d smaller than one block", h, w);
+	if (h % 16 || w % 16) return umi::fail(UMI_ERR_UNSUPPORTED, "coarse ME: frame %dx%d not a multiple of 16", h, w);
+	if ((size_t)h * w > (size_t)1 << 30) return umi::fail(UMI_ERR_UNSUPPORTED, "coarse ME: frame %dx%d too large", h, w);
+	return UMI_OK;
+}
+
+umi_status centers_impl(const uint8_t* cur, const uint8_t* ref, int h, int w, int range, int32_t* centers, void* ws,
+                        cudaStream_t st) {
+	const CoarseGeom g(h, w);
+	const CoarseWork K(g);
+	const bool words = umi::aligned(cur, 4) && umi::aligned(ref, 4);
+	const size_t items = 4 * g.plane_bytes / 4 + 4 * (size_t)g.nblk;
+	const int grid = (int)std::min<size_t>((items + NT - 1) / NT, 152 * 16);
+	coarse_cells_kernel<<<grid, NT, 0, st>>>(cur, ref, g, words, K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes));
+	UMI_TRY(umi::launch_status("coarse_cells_kernel"));
+	coarse_search_kernel<<<g.nblk, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2,
+	                                             centers);
+	return umi::launch_status("coarse_search_kernel");
+}
+
+umi_status check_common(const uint8_t* cur, const uint8_t* ref, int h, int w, void* ws, size_t bytes) {
+	UMI_TRY(check_frame(h, w));
+	if (!cur || !ref || !ws) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: null pointer");
+	if (bytes < CoarseWork(CoarseGeom(h, w)).bytes) return umi::fail(UMI_ERR_NO_MEMORY, "coarse ME: workspace too small");
+	if (!umi::aligned(ws, 256)) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: workspace alignment");
+	return UMI_OK;
+}
+
+}  // namespace
+
+extern "C" size_t umi_me_coarse_workspace_bytes(int32_t h, int32_t w) {
+	if (check_frame(h, w) != UMI_OK) return 0;
+	return CoarseWork(CoarseGeom(h, w)).bytes;
+}
+
+extern "C" umi_status umi_me_coarse_centers_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w,
+                                               int32_t range, int32_t* centers, void* workspace,
+                                               size_t workspace_bytes, void* stream) {
+	UMI_TRY(check_common(cur, ref, h, w, workspace, workspace_bytes));
+	if (!centers) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: null pointer");
+	if (range < 0 || range > 62 || range % 2)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "coarse ME: range %d (even, 0..62)", range);
+	UMI_TRY(centers_impl(cur, ref, h, w, range, centers, workspace, umi::as_stream(stream)));
+	return umi::ok();
+}
+
+extern "C" umi_status umi_me_coarse_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t refine_r,
+                                       int32_t full_r, int32_t sad_threshold, int32_t audit_stride, int32_t* mv,
+                                       unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,
+                                       size_t workspace_bytes, void* stream) {
+	UMI_TRY(check_common(cur, ref, h, w, workspace, workspace_bytes));
+	if (!mv) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: null pointer");
+	if (refine_r < 1 || full_r < refine_r || full_r > 64)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "coarse ME: refine %d / full %d ranges", refine_r, full_r);
+	if (audit_stride < 0) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: negative audit stride");
+	const cudaStream_t st = umi::as_stream(stream);
+	const CoarseWork K{CoarseGeom(h, w)};
+	int32_t* centers = K.at<int32_t>(workspace, K.centers);
+	UMI_TRY(centers_impl(cur, ref, h, w, (full_r - refine_r) & ~1, centers, workspace, st));
+	const umi::MeFinishBuffers fb{K.at<int32_t>(workspace, K.list), K.at<int32_t>(workspace, K.count),
+	                              K.at<int32_t>(workspace, K.amv), K.at<int32_t>(workspace, K.alist)};
+	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
+	                                     audit_sums, n_fallback, fb, st);
+}

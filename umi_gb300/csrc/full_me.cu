@@ -572,6 +572,120 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 	}
 }
 
+// ---- Small-range argmin search (16x16 blocks, r <= 7): the refine around
+// proposal centres.  A lane owns one horizontal displacement of one block and
+// keeps the block's 16 rows (64 words) in registers; each row of the
+// (16 + 2r)-row window is loaded once (four words realigned by prmt from five
+// aligned ones, or clamped bytes at the frame edge) and added to every
+// vertical displacement it meets: 16 (2r + 1) x 4 vabsdiff4 per lane, no
+// shared memory.  floor(32 / (2r + 1)) blocks per warp; the argmin key
+// (sad << 8) | raster index is reduced over each block's lanes by shuffles.
+// Same candidates, clamping and tie-break as full_me_kernel.
+template <int R>
+__global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
+                                                       const int32_t* __restrict__ centers, int32_t* __restrict__ out,
+                                                       int h, int w, int nbx, int nblk, bool cur16) {
+	constexpr int ND = 2 * R + 1, BPW = 32 / ND, WR = 16 + 2 * R;
+	static_assert(ND <= 16 && ND * ND <= 256, "key layout and segment reduction");
+	const int lane = threadIdx.x & 31;
+	const int seg = lane / ND, dx = lane - seg * ND;
+	const int blk = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * BPW + seg;
+	const bool active = seg < BPW && blk < nblk;
+	uint32_t key = 0xffffffffu;
+	int cy = 0, cx = 0;
+	if (active) {
+		const int by = blk / nbx, bx = blk - by * nbx;
+		const int y0 = 16 * by, x0 = 16 * bx;
+		if (centers) { cy = __ldg(centers + 2 * blk); cx = __ldg(centers + 2 * blk + 1); }
+		uint32_t c[16][4];
+#pragma unroll
+		for (int r = 0; r < 16; ++r) {
+			const uint8_t* p = cur + (size_t)(y0 + r) * w + x0;
+			if (cur16) {
+				const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+				c[r][0] = v.x; c[r][1] = v.y; c[r][2] = v.z; c[r][3] = v.w;
+			} else {
+#pragma unroll
+				for (int k = 0; k < 4; ++k) c[r][k] = __ldg(reinterpret_cast<const uint32_t*>(p) + k);
+			}
+		}
+		uint32_t cost[ND];
+#pragma unroll
+		for (int d = 0; d < ND; ++d) cost[d] = 0;
+		const int ys = y0 + cy - R, xs = x0 + cx - R + dx;
+		// the 16 columns inside the row: five aligned words cover them (xa + 20 <= w when sh != 0, w % 4 == 0)
+		const bool inside = xs >= 0 && xs + 16 <= w;
+		const int xa = xs & ~3, sh = xs & 3;
+		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
+#pragma unroll
+		for (int wr = 0; wr < WR; ++wr) {
+			const uint8_t* row = ref + (size_t)min(max(ys + wr, 0), h - 1) * w;
+			uint32_t v[4];
+			if (inside) {
+				const uint32_t* rw = reinterpret_cast<const uint32_t*>(row + xa);
+				uint32_t u[5];
+#pragma unroll
+				for (int k = 0; k < 4; ++k) u[k] = __ldg(rw + k);
+				u[4] = sh ? __ldg(rw + 4) : 0u;
+#pragma unroll
+				for (int k = 0; k < 4; ++k) v[k] = __byte_perm(u[k], u[k + 1], sel);
+			} else {
+#pragma unroll
+				for (int k = 0; k < 4; ++k) {
+					uint32_t t = 0;
+#pragma unroll
+					for (int j = 0; j < 4; ++j) t |= (uint32_t)__ldg(row + min(max(xs + 4 * k + j, 0), w - 1)) << (8 * j);
+					v[k] = t;
+				}
+			}
+#pragma unroll
+			for (int d = 0; d < ND; ++d) {
+				const int br = wr - d;  // block row meeting this window row at vertical displacement d - R
+				if (br >= 0 && br < 16) {
+#pragma unroll
+					for (int k = 0; k < 4; ++k) cost[d] = sad4_acc(c[br][k], v[k], cost[d]);
+				}
+			}
+		}
+#pragma unroll
+		for (int d = 0; d < ND; ++d) key = min(key, (cost[d] << 8) | (uint32_t)(d * ND + dx));
+	}
+#pragma unroll
+	for (int off = 1; off < 16; off <<= 1) {  // segmented min over the block's ND <= 16 lanes
+		const uint32_t o = __shfl_down_sync(0xffffffffu, key, off);
+		if (dx + off < ND) key = min(key, o);
+	}
+	if (active && dx == 0) {
+		const int idx = (int)(key & 0xffu), iy = idx / ND, ix = idx - iy * ND;
+		out[3 * blk + 0] = cy + iy - R;
+		out[3 * blk + 1] = cx + ix - R;
+		out[3 * blk + 2] = (int32_t)(key >> 8);
+	}
+}
+
+template <int R>
+umi_status launch_small_r(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
+                          bool cur16, cudaStream_t st) {
+	constexpr int BPW = 32 / (2 * R + 1);
+	const int warps = (g.nblk + BPW - 1) / BPW;
+	me_small_kernel<R><<<(warps + 3) / 4, 128, 0, st>>>(cur, ref, centers, out, g.h, g.w, g.nbx, g.nblk, cur16);
+	return umi::launch_status("me_small_kernel");
+}
+
+umi_status launch_small(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
+                        cudaStream_t st) {
+	const bool cur16 = umi::aligned(cur, 16) && g.w % 16 == 0;
+	switch (g.r) {
+		case 1: return launch_small_r<1>(cur, ref, centers, out, g, cur16, st);
+		case 2: return launch_small_r<2>(cur, ref, centers, out, g, cur16, st);
+		case 3: return launch_small_r<3>(cur, ref, centers, out, g, cur16, st);
+		case 4: return launch_small_r<4>(cur, ref, centers, out, g, cur16, st);
+		case 5: return launch_small_r<5>(cur, ref, centers, out, g, cur16, st);
+		case 6: return launch_small_r<6>(cur, ref, centers, out, g, cur16, st);
+		default: return launch_small_r<7>(cur, ref, centers, out, g, cur16, st);
+	}
+}
+
 // Vertical displacements per thread: the candidate that wastes the fewest
 // padded rows (ng*G - ndx), larger G on ties (fewer window-row loads).
 int pick_g(int ndx) {
@@ -664,6 +778,10 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.win_rows = g.ng * G + b - 1;
 	g.win_need = (2 * r + b + 3) / 4 + 1;
 	g.vec_ok = umi::aligned(ref, 4) && umi::aligned(cur, 4) && (w % 4) == 0;
+	if (!volume && !list && b == 16 && r <= 7 && g.vec_ok) {  // small windows: registers only
+		const umi_status rc = launch_small(cur, ref, centers, out, g, umi::as_stream(stream));
+		return rc == UMI_OK ? umi::ok() : rc;
+	}
 	// TMA windows (argmin search, 16x16 blocks, r >= 48): 16-byte-aligned frame rows and box rows.
 	// Measured on GB300: at +-64 one TMA box per window beats the thread-staged
 	// copies (2.76 vs 2.81 ms at 4K); at +-32 the row padding to 16 bytes costs

@@ -19,12 +19,7 @@
 #include <cmath>
 
 #include "common.h"
-
-extern "C" umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
-                                     const int32_t* centers, int32_t* mv, void* stream);
-extern "C" umi_status umi_full_me_u8_list(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b,
-                                          int32_t r, const int32_t* centers, const int32_t* blocks,
-                                          const int32_t* n_blocks, int32_t max_blocks, int32_t* mv, void* stream);
+#include "me_pipeline.h"
 
 namespace umi {
 umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const float* bias, int h, int w, int dil,
@@ -662,24 +657,41 @@ extern "C" umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, 
 	centers_kernel<<<grid_for(2 * (size_t)K.nblk), NT, 0, st>>>(K.at<float>(ws, K.pred), centers, K.nblk,
 	                                                             full_r - refine_r);
 	UMI_TRY(umi::launch_status("centers_kernel"));
+	const umi::MeFinishBuffers fb{K.at<int32_t>(ws, K.list), K.at<int32_t>(ws, K.count), K.at<int32_t>(ws, K.amv),
+	                              K.at<int32_t>(ws, K.alist)};
+	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
+	                                     audit_sums, n_fallback, fb, st);
+}
+
+namespace umi {
+
+// Refine around the proposal's centres, audit every audit_stride-th block by
+// exhaustive search (its result replaces the refined one, both SADs go to
+// audit_sums), then exhaustive search for every other block whose refined
+// SAD exceeds sad_threshold.  Shared by the learned and the coarse proposal.
+umi_status me_refine_audit_fallback(const uint8_t* cur, const uint8_t* ref, int h, int w, const int32_t* centers,
+                                    int refine_r, int full_r, int32_t sad_threshold, int audit_stride, int32_t* mv,
+                                    unsigned long long* audit_sums, int32_t* n_fallback, const MeFinishBuffers& b,
+                                    cudaStream_t st) {
+	const int nblk = (h / 16) * (w / 16);
+	void* stream = st;
 	UMI_TRY(umi_full_me_u8(cur, ref, h, w, 16, refine_r, centers, mv, stream));
-	int32_t* count = K.at<int32_t>(ws, K.count);
-	int32_t* amv = K.at<int32_t>(ws, K.amv);
 	if (audit_stride > 0) {
-		audit_list_kernel<<<grid_for(K.nblk), NT, 0, st>>>(K.at<int32_t>(ws, K.alist), count + 1, K.nblk, audit_stride);
+		audit_list_kernel<<<grid_for(nblk), NT, 0, st>>>(b.alist, b.count + 1, nblk, audit_stride);
 		UMI_TRY(umi::launch_status("audit_list_kernel"));
-		UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, K.at<int32_t>(ws, K.alist), count + 1,
-		                            umi::ceil_div(K.nblk, audit_stride), amv, stream));
+		UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 1,
+		                            umi::ceil_div(nblk, audit_stride), b.amv, stream));
 	}
-	UMI_TRY(umi::cuda_status(cudaMemsetAsync(count, 0, sizeof(int32_t), st), "cudaMemsetAsync"));
+	UMI_TRY(umi::cuda_status(cudaMemsetAsync(b.count, 0, sizeof(int32_t), st), "cudaMemsetAsync"));
 	if (audit_sums)
 		UMI_TRY(umi::cuda_status(cudaMemsetAsync(audit_sums, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync"));
-	flag_kernel<<<grid_for(K.nblk), NT, 0, st>>>(mv, amv, K.nblk, audit_stride, sad_threshold, K.at<int32_t>(ws, K.list),
-	                                              count, audit_sums);
+	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, b.amv, nblk, audit_stride, sad_threshold, b.list, b.count, audit_sums);
 	UMI_TRY(umi::launch_status("flag_kernel"));
-	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, K.at<int32_t>(ws, K.list), count, K.nblk, mv, stream));
+	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.list, b.count, nblk, mv, stream));
 	if (n_fallback)
-		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(n_fallback, count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
+		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(n_fallback, b.count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
 		                         "cudaMemcpyAsync"));
 	return umi::ok();
 }
+
+}  // namespace umi

@@ -148,13 +148,17 @@ def median_predictor(mv, nby: int, nbx: int):
 
 
 def evaluate(net: MeNet, seeds, refine_r: int = 4, full_r: int = 64, sad_threshold: int | None = None,
-             audit_stride: int = 64):
+             audit_stride: int = 64, coarse=None):
     """Per-method statistics on the given pairs against exhaustive search.
 
     Methods: learned (proposal + refine, then audit + fallback), zero-MV + refine,
-    neighbour-median + refine (each with the same fallback threshold)."""
+    neighbour-median + refine, and, when `coarse` (a CoarseMe for the frame
+    size) is given, the coarse 4x4-mean proposal + refine (each with the same
+    fallback threshold)."""
     import torch
     out = {"learned": [], "zero": [], "median": []}
+    if coarse is not None:
+        out["coarse"] = []
     nby, nbx = net.h // 16, net.w // 16
     for s in seeds:
         cur, ref, _ = me_pair_cuda(int(s), net.h, net.w)
@@ -165,6 +169,8 @@ def evaluate(net: MeNet, seeds, refine_r: int = 4, full_r: int = 64, sad_thresho
         mv_l, sums, nf = net.estimate(cur, ref, refine_r, full_r, sad_threshold=(1 << 31) - 1, audit_stride=0)
         cand = {"learned": mv_l.clone(), "zero": full_me_u8(cur, ref, 16, refine_r)}
         cand["median"] = full_me_u8(cur, ref, 16, refine_r, centers=median_predictor(cand["zero"], nby, nbx))
+        if coarse is not None:
+            cand["coarse"] = coarse.estimate(cur, ref, refine_r, full_r, sad_threshold=(1 << 31) - 1)[0].clone()
         for name, mv in cand.items():
             hit = (mv[:, 2].long() == fsad).float().mean().item()
             bad = (mv[:, 2] > thr).nonzero().flatten().to(torch.int32)
