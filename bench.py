@@ -676,8 +676,8 @@ class LearnedMe:
         self.h_ref = self.d_ref[0].cpu().pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
         # inference (downsample, 4 weight packs, layer 1, 3 tensor-core layers, head) + centres + refine
-        # + audit list + audit search + flag + fallback (memsets and the count copy are not kernels)
-        self.launches_per_step = 16
+        # + flag + one list search (audit and fallback) + audit sum (memsets and the count copy are not kernels)
+        self.launches_per_step = 15
 
     def _estimate(self, k):
         self.net.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
@@ -761,8 +761,8 @@ class CoarseMe4k(LearnedMe):
     def setup(self, dev):
         super().setup(dev)
         self.cme = self.U.CoarseMe(self.H, self.W, device=dev)
-        # cells + search + refine + audit list + audit search + flag + fallback
-        self.launches_per_step = 7
+        # cells + search + refine + flag + one list search (audit and fallback) + audit sum
+        self.launches_per_step = 6
 
     def _estimate(self, k):
         self.cme.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,

@@ -23,7 +23,7 @@
 // cur's cells are four words per block.
 //
 // Search kernel: one CTA per block, one warp per plane, one lane per
-// candidate row A holding 32 candidate columns in registers; the argmin key
+// candidate column B holding 32 candidate rows in registers; the argmin key
 // (sad << 12) | raster index is reduced per warp, then over the four warps.
 #include <algorithm>
 #include <climits>
@@ -107,11 +107,32 @@ __global__ void __launch_bounds__(NT) coarse_cells_kernel(const uint8_t* __restr
 	}
 }
 
+// Minimum of cost[a] * 32 + a over the candidate rows a whose vertical
+// displacement 2 (a - 16) + PY lies in [-m, m]: the first row wins ties.
+template <int M, int PY>
+__device__ __forceinline__ uint32_t first_min_row(const uint32_t (&cost)[32], int m) {
+	uint32_t mn = 0xffffffffu;
+#pragma unroll
+	for (int a = 0; a < 32; ++a) {
+		const int dy2 = 2 * (a - 16) + PY;
+		if (M >= 0 ? (dy2 >= -M && dy2 <= M) : (dy2 >= -m && dy2 <= m)) mn = min(mn, cost[a] * 32u + (uint32_t)a);
+	}
+	return mn;
+}
+
+// One CTA per block, one warp per plane (py, px), one lane per candidate
+// column B = lane - 16.  The lane streams the plane's 35 window rows once:
+// one realigned word per row (two shared loads and a prmt) meets the four cell
+// rows i at the candidate rows A = row - 16 - i, so a candidate costs four
+// vabsdiff4 and about a quarter of a prmt.  M = range / 2 at compile time
+// (the default range 60), or M < 0 for any range (runtime masks).
+template <int M>
 __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __restrict__ cells,
-                                                            const uint32_t* __restrict__ planes, CoarseGeom g, int m,
+                                                            const uint32_t* __restrict__ planes, CoarseGeom g, int m_rt,
                                                             int32_t* __restrict__ centers) {
-	__shared__ uint32_t win[4][WIN_ROWS][WIN_WORDS];  // row stride 9 words: lanes on distinct rows hit distinct banks
-	__shared__ int best[4];
+	const int m = M >= 0 ? M : m_rt;
+	__shared__ uint32_t win[4][WIN_ROWS][WIN_WORDS];
+	__shared__ uint32_t best[4];
 	const int blk = blockIdx.x, by = blk / g.nbx, bx = blk - by * g.nbx;
 	const int pww = g.pw / 4;
 	const size_t plane_words = (size_t)g.pr * pww;
@@ -126,32 +147,27 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 	for (int i = 0; i < 4; ++i) c[i] = __ldg(cells + 4 * (size_t)blk + i);
 	__syncthreads();
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
-	const int A = -((m + py) >> 1) + lane;  // first row: ceil((-m - py) / 2)
-	const int dy2 = 2 * A + py;
-	int key = INT_MAX;
-	if (dy2 <= m) {  // A <= 15, window rows 16 + A + i in [0, 34]
-		uint32_t cost[32];
+	const int dx2 = 2 * (lane - 16) + px;
+	uint32_t key = 0xffffffffu;
+	if (dx2 >= -m && dx2 <= m) {
+		uint32_t cost[32];  // candidate rows A = a - 16
 #pragma unroll
-		for (int t = 0; t < 32; ++t) cost[t] = 0;
+		for (int a = 0; a < 32; ++a) cost[a] = 0;
+		const uint32_t* wrow = &win[warp][0][lane >> 2];  // bytes lane .. lane + 3 of each row
+		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(lane & 3);
 #pragma unroll
-		for (int i = 0; i < 4; ++i) {
-			const uint32_t* row = win[warp][16 + A + i];
-			uint32_t v[WIN_WORDS];
+		for (int r = 0; r < WIN_ROWS; ++r) {
+			const uint32_t v = __byte_perm(wrow[r * WIN_WORDS], wrow[r * WIN_WORDS + 1], sel);
 #pragma unroll
-			for (int k = 0; k < WIN_WORDS; ++k) v[k] = row[k];
-#pragma unroll
-			for (int t = 0; t < 32; ++t) {
-				// candidate column B = t - 16: bytes t .. t + 3 of the window row
-				const uint32_t r4 = (t & 3) ? __byte_perm(v[t >> 2], v[(t >> 2) + 1], 0x3210u + 0x1111u * (t & 3))
-				                            : v[t >> 2];
-				cost[t] = sad4_acc(c[i], r4, cost[t]);
+			for (int i = 0; i < 4; ++i) {
+				const int a = r - i;  // window row r = 16 + A + i
+				if (a >= 0 && a < 32) cost[a] = sad4_acc(c[i], v, cost[a]);
 			}
 		}
-		const int nd = 2 * m + 1;
-#pragma unroll
-		for (int t = 0; t < 32; ++t) {
-			const int dx2 = 2 * (t - 16) + px;
-			if (dx2 >= -m && dx2 <= m) key = min(key, (int)(cost[t] << 12) | ((dy2 + m) * nd + dx2 + m));
+		const uint32_t mn = py ? first_min_row<M, 1>(cost, m) : first_min_row<M, 0>(cost, m);
+		if (mn != 0xffffffffu) {
+			const int a = (int)(mn & 31u), dy2 = 2 * (a - 16) + py, nd = 2 * m + 1;
+			key = ((mn >> 5) << 12) | (uint32_t)((dy2 + m) * nd + dx2 + m);
 		}
 	}
 #pragma unroll
@@ -159,8 +175,8 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 	if (lane == 0) best[warp] = key;
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		const int k = min(min(best[0], best[1]), min(best[2], best[3]));
-		const int idx = k & 4095, nd = 2 * m + 1;
+		const uint32_t k = min(min(best[0], best[1]), min(best[2], best[3]));
+		const int idx = (int)(k & 4095u), nd = 2 * m + 1;
 		centers[2 * blk] = 2 * (idx / nd - m);
 		centers[2 * blk + 1] = 2 * (idx % nd - m);
 	}
@@ -168,7 +184,7 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 
 // ---- workspace
 struct CoarseWork {
-	size_t cells, planes, centers, list, count, amv, alist, bytes;
+	size_t cells, planes, centers, list, count, bytes;
 	explicit CoarseWork(const CoarseGeom& g) {
 		size_t o = 0;
 		auto take = [&](size_t n) { size_t r = o; o += (n + 255) & ~size_t(255); return r; };
@@ -177,8 +193,6 @@ struct CoarseWork {
 		centers = take(sizeof(int32_t) * 2 * g.nblk);
 		list = take(sizeof(int32_t) * g.nblk);
 		count = take(sizeof(int32_t) * 4);
-		amv = take(sizeof(int32_t) * 3 * g.nblk);
-		alist = take(sizeof(int32_t) * g.nblk);
 		bytes = o;
 	}
 	template <class T> T* at(void* ws, size_t off) const { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
@@ -200,8 +214,8 @@ umi_status centers_impl(const uint8_t* cur, const uint8_t* ref, int h, int w, in
 	const int grid = (int)std::min<size_t>((items + NT - 1) / NT, 152 * 16);
 	coarse_cells_kernel<<<grid, NT, 0, st>>>(cur, ref, g, words, K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes));
 	UMI_TRY(umi::launch_status("coarse_cells_kernel"));
-	coarse_search_kernel<<<g.nblk, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2,
-	                                             centers);
+	auto kern = range == 60 ? coarse_search_kernel<30> : coarse_search_kernel<-1>;
+	kern<<<g.nblk, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2, centers);
 	return umi::launch_status("coarse_search_kernel");
 }
 
@@ -244,8 +258,7 @@ extern "C" umi_status umi_me_coarse_u8(const uint8_t* cur, const uint8_t* ref, i
 	const CoarseWork K{CoarseGeom(h, w)};
 	int32_t* centers = K.at<int32_t>(workspace, K.centers);
 	UMI_TRY(centers_impl(cur, ref, h, w, (full_r - refine_r) & ~1, centers, workspace, st));
-	const umi::MeFinishBuffers fb{K.at<int32_t>(workspace, K.list), K.at<int32_t>(workspace, K.count),
-	                              K.at<int32_t>(workspace, K.amv), K.at<int32_t>(workspace, K.alist)};
+	const umi::MeFinishBuffers fb{K.at<int32_t>(workspace, K.list), K.at<int32_t>(workspace, K.count)};
 	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
 	                                     audit_sums, n_fallback, fb, st);
 }

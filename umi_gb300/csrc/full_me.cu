@@ -573,11 +573,13 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 }
 
 // ---- Small-range argmin search (16x16 blocks, r <= 7): the refine around
-// proposal centres.  A lane owns one horizontal displacement of one block and
-// keeps the block's 16 rows (64 words) in registers; each row of the
-// (16 + 2r)-row window is loaded once (four words realigned by prmt from five
-// aligned ones, or clamped bytes at the frame edge) and added to every
-// vertical displacement it meets: 16 (2r + 1) x 4 vabsdiff4 per lane, no
+// proposal centres.  A lane owns one horizontal displacement of one block.
+// It walks the block's 16 rows once, keeping the 2r + 1 window rows that the
+// current block row meets (at the 2r + 1 vertical displacements) in a
+// register ring: per block row one new window row enters (four words
+// realigned by prmt from five aligned ones, or clamped bytes at the frame
+// edge) and the block row (one 16-byte load, the same for the block's lanes)
+// is compared with every ring row: 16 (2r + 1) x 4 vabsdiff4 per lane, no
 // shared memory.  floor(32 / (2r + 1)) blocks per warp; the argmin key
 // (sad << 8) | raster index is reduced over each block's lanes by shuffles.
 // Same candidates, clamping and tie-break as full_me_kernel.
@@ -585,7 +587,7 @@ template <int R>
 __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
                                                        const int32_t* __restrict__ centers, int32_t* __restrict__ out,
                                                        int h, int w, int nbx, int nblk, bool cur16) {
-	constexpr int ND = 2 * R + 1, BPW = 32 / ND, WR = 16 + 2 * R;
+	constexpr int ND = 2 * R + 1, BPW = 32 / ND;
 	static_assert(ND <= 16 && ND * ND <= 256, "key layout and segment reduction");
 	const int lane = threadIdx.x & 31;
 	const int seg = lane / ND, dx = lane - seg * ND;
@@ -597,30 +599,13 @@ __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict
 		const int by = blk / nbx, bx = blk - by * nbx;
 		const int y0 = 16 * by, x0 = 16 * bx;
 		if (centers) { cy = __ldg(centers + 2 * blk); cx = __ldg(centers + 2 * blk + 1); }
-		uint32_t c[16][4];
-#pragma unroll
-		for (int r = 0; r < 16; ++r) {
-			const uint8_t* p = cur + (size_t)(y0 + r) * w + x0;
-			if (cur16) {
-				const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-				c[r][0] = v.x; c[r][1] = v.y; c[r][2] = v.z; c[r][3] = v.w;
-			} else {
-#pragma unroll
-				for (int k = 0; k < 4; ++k) c[r][k] = __ldg(reinterpret_cast<const uint32_t*>(p) + k);
-			}
-		}
-		uint32_t cost[ND];
-#pragma unroll
-		for (int d = 0; d < ND; ++d) cost[d] = 0;
 		const int ys = y0 + cy - R, xs = x0 + cx - R + dx;
 		// the 16 columns inside the row: five aligned words cover them (xa + 20 <= w when sh != 0, w % 4 == 0)
 		const bool inside = xs >= 0 && xs + 16 <= w;
 		const int xa = xs & ~3, sh = xs & 3;
 		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
-#pragma unroll
-		for (int wr = 0; wr < WR; ++wr) {
+		auto window_row = [&](int wr, uint32_t (&v)[4]) {
 			const uint8_t* row = ref + (size_t)min(max(ys + wr, 0), h - 1) * w;
-			uint32_t v[4];
 			if (inside) {
 				const uint32_t* rw = reinterpret_cast<const uint32_t*>(row + xa);
 				uint32_t u[5];
@@ -638,14 +623,28 @@ __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict
 					v[k] = t;
 				}
 			}
+		};
+		uint32_t ring[ND][4], cost[ND];
 #pragma unroll
-			for (int d = 0; d < ND; ++d) {
-				const int br = wr - d;  // block row meeting this window row at vertical displacement d - R
-				if (br >= 0 && br < 16) {
+		for (int d = 0; d < ND; ++d) cost[d] = 0;
 #pragma unroll
-					for (int k = 0; k < 4; ++k) cost[d] = sad4_acc(c[br][k], v[k], cost[d]);
-				}
+		for (int wr = 0; wr < ND - 1; ++wr) window_row(wr, ring[wr]);
+#pragma unroll
+		for (int br = 0; br < 16; ++br) {
+			window_row(br + ND - 1, ring[(br + ND - 1) % ND]);
+			const uint8_t* p = cur + (size_t)(y0 + br) * w + x0;
+			uint32_t c[4];
+			if (cur16) {
+				const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+				c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+			} else {
+#pragma unroll
+				for (int k = 0; k < 4; ++k) c[k] = __ldg(reinterpret_cast<const uint32_t*>(p) + k);
 			}
+#pragma unroll
+			for (int d = 0; d < ND; ++d)  // block row br meets window row br + d at vertical displacement d - R
+#pragma unroll
+				for (int k = 0; k < 4; ++k) cost[d] = sad4_acc(c[k], ring[(br + d) % ND][k], cost[d]);
 		}
 #pragma unroll
 		for (int d = 0; d < ND; ++d) key = min(key, (cost[d] << 8) | (uint32_t)(d * ND + dx));

@@ -53,7 +53,7 @@ struct Layout {
 // ---- workspace layout for a frame of h x w pixels
 struct Work {
 	int H4, W4, P, nbx, nby, nblk, tiles_wg;
-	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, amv, alist, wpart, hpart, lpart;
+	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, wpart, hpart, lpart;
 	size_t nhwc[2], wtc[NL], err;  // tensor-core inference: bf16 (H4, W4, 64) activations, packed weights
 	size_t bytes;
 	Work(int h, int w) {
@@ -70,9 +70,7 @@ struct Work {
 		pred = take(sizeof(float) * 2 * nblk);
 		centers = take(sizeof(int32_t) * 2 * nblk);
 		list = take(sizeof(int32_t) * nblk);
-		count = take(sizeof(int32_t) * 4);  // [0] fallback blocks, [1] audited blocks
-		amv = take(sizeof(int32_t) * 3 * nblk);
-		alist = take(sizeof(int32_t) * nblk);
+		count = take(sizeof(int32_t) * 4);  // [0] listed blocks, [1] fallback blocks
 		wpart = take(sizeof(float) * (size_t)tiles_wg * (CH * CH * 9 + CH));
 		hpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8) * (2 * HEADF + 2));
 		lpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8));
@@ -360,33 +358,34 @@ __global__ void centers_kernel(const float* __restrict__ pred, int32_t* __restri
 	}
 }
 
-// The audit sample: blocks 0, stride, 2 stride, ...
-__global__ void audit_list_kernel(int32_t* __restrict__ list, int32_t* __restrict__ count, int n, int stride) {
-	const int na = stride > 0 ? (n + stride - 1) / stride : 0;
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < na; i += gridDim.x * blockDim.x) list[i] = i * stride;
-	if (blockIdx.x == 0 && threadIdx.x == 0) *count = na;
-}
-
-// Audited blocks take their exhaustive result (and add both SADs to the
-// audit sums); other blocks whose refined SAD exceeds the threshold go to
-// the fallback list (order of discovery; the search is per block, so the
-// order does not change any result).
-__global__ void flag_kernel(int32_t* __restrict__ mv, const int32_t* __restrict__ amv, int n, int stride, int32_t thr,
+// One list for the exhaustive search: the audited blocks 0, stride, 2 stride,
+// ... (their refined SAD goes to audit_sums[0]) and every other block whose
+// refined SAD exceeds the threshold (counted in count[1]).  count[0] is the
+// list length.  List order is the order of discovery; the search is per
+// block, so the order changes no result.
+__global__ void flag_kernel(const int32_t* __restrict__ mv, int n, int stride, int32_t thr,
                             int32_t* __restrict__ list, int32_t* __restrict__ count,
                             unsigned long long* __restrict__ audit_sums) {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		if (stride > 0 && i % stride == 0) {
-			if (audit_sums) {
-				atomicAdd(audit_sums, (unsigned long long)mv[3 * i + 2]);
-				atomicAdd(audit_sums + 1, (unsigned long long)amv[3 * i + 2]);
-			}
-			mv[3 * i] = amv[3 * i];
-			mv[3 * i + 1] = amv[3 * i + 1];
-			mv[3 * i + 2] = amv[3 * i + 2];
+			if (audit_sums) atomicAdd(audit_sums, (unsigned long long)mv[3 * i + 2]);
+			list[atomicAdd(count, 1)] = i;
 		} else if (mv[3 * i + 2] > thr) {
 			list[atomicAdd(count, 1)] = i;
+			atomicAdd(count + 1, 1);
 		}
 	}
+}
+
+// audit_sums[1] += exhaustive SAD of the audited blocks (after the search).
+__global__ void audit_sum_kernel(const int32_t* __restrict__ mv, int n, int stride,
+                                 unsigned long long* __restrict__ audit_sums) {
+	const int na = (n + stride - 1) / stride;
+	unsigned long long s = 0;
+	for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x)
+		s += (unsigned long long)mv[3 * (size_t)a * stride + 2];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if ((threadIdx.x & 31) == 0 && s) atomicAdd(audit_sums + 1, s);
 }
 
 // ---- tensor-core inference path: bf16 NHWC activations, 64 channels per
@@ -657,8 +656,7 @@ extern "C" umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, 
 	centers_kernel<<<grid_for(2 * (size_t)K.nblk), NT, 0, st>>>(K.at<float>(ws, K.pred), centers, K.nblk,
 	                                                             full_r - refine_r);
 	UMI_TRY(umi::launch_status("centers_kernel"));
-	const umi::MeFinishBuffers fb{K.at<int32_t>(ws, K.list), K.at<int32_t>(ws, K.count), K.at<int32_t>(ws, K.amv),
-	                              K.at<int32_t>(ws, K.alist)};
+	const umi::MeFinishBuffers fb{K.at<int32_t>(ws, K.list), K.at<int32_t>(ws, K.count)};
 	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
 	                                     audit_sums, n_fallback, fb, st);
 }
@@ -676,20 +674,18 @@ umi_status me_refine_audit_fallback(const uint8_t* cur, const uint8_t* ref, int 
 	const int nblk = (h / 16) * (w / 16);
 	void* stream = st;
 	UMI_TRY(umi_full_me_u8(cur, ref, h, w, 16, refine_r, centers, mv, stream));
-	if (audit_stride > 0) {
-		audit_list_kernel<<<grid_for(nblk), NT, 0, st>>>(b.alist, b.count + 1, nblk, audit_stride);
-		UMI_TRY(umi::launch_status("audit_list_kernel"));
-		UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 1,
-		                            umi::ceil_div(nblk, audit_stride), b.amv, stream));
-	}
-	UMI_TRY(umi::cuda_status(cudaMemsetAsync(b.count, 0, sizeof(int32_t), st), "cudaMemsetAsync"));
+	UMI_TRY(umi::cuda_status(cudaMemsetAsync(b.count, 0, 2 * sizeof(int32_t), st), "cudaMemsetAsync"));
 	if (audit_sums)
 		UMI_TRY(umi::cuda_status(cudaMemsetAsync(audit_sums, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync"));
-	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, b.amv, nblk, audit_stride, sad_threshold, b.list, b.count, audit_sums);
+	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, nblk, audit_stride, sad_threshold, b.list, b.count, audit_sums);
 	UMI_TRY(umi::launch_status("flag_kernel"));
 	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.list, b.count, nblk, mv, stream));
+	if (audit_stride > 0 && audit_sums) {
+		audit_sum_kernel<<<grid_for(umi::ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, nblk, audit_stride, audit_sums);
+		UMI_TRY(umi::launch_status("audit_sum_kernel"));
+	}
 	if (n_fallback)
-		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(n_fallback, b.count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
+		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(n_fallback, b.count + 1, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
 		                         "cudaMemcpyAsync"));
 	return umi::ok();
 }
