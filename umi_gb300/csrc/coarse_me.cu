@@ -136,17 +136,22 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 	const int blk = blockIdx.x, by = blk / g.nbx, bx = blk - by * g.nbx;
 	const int pww = g.pw / 4;
 	const size_t plane_words = (size_t)g.pr * pww;
-	for (int e = threadIdx.x; e < 4 * WIN_ROWS * WIN_WORDS; e += blockDim.x) {
-		const int p = e / (WIN_ROWS * WIN_WORDS), r = (e - p * WIN_ROWS * WIN_WORDS) / WIN_WORDS;
-		const int k = e - p * WIN_ROWS * WIN_WORDS - r * WIN_WORDS;
-		// plane row 4 by + r < 4 nby + 31 < pr; word bx + k <= nbx + 7 < pww
-		win[p][r][k] = __ldg(planes + p * plane_words + (size_t)(4 * by + r) * pww + bx + k);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
+	{  // warp p stages plane p: lane -> word lane % 9 of rows lane / 9 + 3 j (27 lanes)
+		constexpr int RPP = 32 / WIN_WORDS;
+		const int kk = lane % WIN_WORDS, rr = lane / WIN_WORDS;
+		if (rr < RPP) {
+			// plane row 4 by + r < 4 nby + 31 < pr; word bx + k <= nbx + 7 < pww
+			const uint32_t* src = planes + warp * plane_words + (size_t)(4 * by + rr) * pww + bx + kk;
+#pragma unroll
+			for (int j = 0; j < (WIN_ROWS + RPP - 1) / RPP; ++j)
+				if (rr + RPP * j < WIN_ROWS) win[warp][rr + RPP * j][kk] = __ldg(src + (size_t)RPP * j * pww);
+		}
 	}
 	uint32_t c[4];
 #pragma unroll
 	for (int i = 0; i < 4; ++i) c[i] = __ldg(cells + 4 * (size_t)blk + i);
-	__syncthreads();
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
+	__syncwarp();
 	const int dx2 = 2 * (lane - 16) + px;
 	uint32_t key = 0xffffffffu;
 	if (dx2 >= -m && dx2 <= m) {

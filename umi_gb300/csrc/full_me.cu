@@ -573,56 +573,89 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 }
 
 // ---- Small-range argmin search (16x16 blocks, r <= 7): the refine around
-// proposal centres.  A lane owns one horizontal displacement of one block.
-// It walks the block's 16 rows once, keeping the 2r + 1 window rows that the
-// current block row meets (at the 2r + 1 vertical displacements) in a
-// register ring: per block row one new window row enters (four words
-// realigned by prmt from five aligned ones, or clamped bytes at the frame
-// edge) and the block row (one 16-byte load, the same for the block's lanes)
-// is compared with every ring row: 16 (2r + 1) x 4 vabsdiff4 per lane, no
-// shared memory.  floor(32 / (2r + 1)) blocks per warp; the argmin key
+// proposal centres.  A warp serves floor(32 / (2r + 1)) blocks.  It first
+// stages, for each of them, the (16 + 2r)-row window (rows clamped to the
+// frame, words from a 4-byte-aligned left edge, bytes outside the frame
+// replicated) and the current block in its shared-memory slice: all loads in
+// flight at once.  Then a lane owns one horizontal displacement of one block
+// and walks the block's 16 rows once, keeping the 2r + 1 window rows that
+// the current block row meets (at the 2r + 1 vertical displacements) in a
+// register ring: per block row one window row enters (four words realigned by
+// prmt from five) and the block row (one broadcast 16-byte load) is compared
+// with every ring row: 16 (2r + 1) x 4 vabsdiff4 per lane.  The argmin key
 // (sad << 8) | raster index is reduced over each block's lanes by shuffles.
 // Same candidates, clamping and tie-break as full_me_kernel.
 template <int R>
 __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
                                                        const int32_t* __restrict__ centers, int32_t* __restrict__ out,
-                                                       int h, int w, int nbx, int nblk, bool cur16) {
-	constexpr int ND = 2 * R + 1, BPW = 32 / ND;
+                                                       int h, int w, int nbx, int nblk) {
+	constexpr int ND = 2 * R + 1, BPW = 32 / ND, WR = 16 + 2 * R;
+	constexpr int WW = (2 * R + 22) / 4;          // words per window row: 16 + 2r bytes from an offset 0..3
+	constexpr int WIN = (WR * WW + 3) & ~3;       // window words, rounded so the block starts 16-byte aligned
+	constexpr int SEG = WIN + 64;                 // window + current block
+	constexpr int RPP = 32 / WW;                  // window rows staged per pass
 	static_assert(ND <= 16 && ND * ND <= 256, "key layout and segment reduction");
-	const int lane = threadIdx.x & 31;
+	__shared__ __align__(16) uint32_t sm[4][BPW * SEG];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int blk0 = (int)((size_t)blockIdx.x * 4 + warp) * BPW;
+	uint32_t* ws = sm[warp];
+	// 1. Staging (lane -> (row rr + RPP * pass, word kk) of the window, (row, word) of the block).
+	const int kk = lane % WW, rr = lane / WW;
+#pragma unroll
+	for (int s = 0; s < BPW; ++s) {
+		const int b = blk0 + s;
+		if (b >= nblk) break;  // warp-uniform
+		const int by = b / nbx, bx = b - by * nbx;
+		const int cy = centers ? __ldg(centers + 2 * b) : 0, cx = centers ? __ldg(centers + 2 * b + 1) : 0;
+		const int xa0 = (16 * bx + cx - R) & ~3, gx = xa0 + 4 * kk;
+		const bool word = gx >= 0 && gx + 4 <= w;  // 4-byte aligned: ref aligned, w % 4 == 0
+		const int y0 = 16 * by + cy - R;
+		uint32_t* dst = ws + s * SEG;
+		if (rr < RPP) {
+#pragma unroll
+			for (int pass = 0; pass < (WR + RPP - 1) / RPP; ++pass) {
+				const int r = rr + RPP * pass;
+				if (r < WR) {
+					const uint8_t* row = ref + (size_t)min(max(y0 + r, 0), h - 1) * w;
+					uint32_t v;
+					if (word) {
+						v = __ldg(reinterpret_cast<const uint32_t*>(row + gx));
+					} else {
+						v = 0;
+#pragma unroll
+						for (int j = 0; j < 4; ++j) v |= (uint32_t)__ldg(row + min(max(gx + j, 0), w - 1)) << (8 * j);
+					}
+					dst[r * WW + kk] = v;
+				}
+			}
+		}
+		const uint32_t* cb = reinterpret_cast<const uint32_t*>(cur + (size_t)(16 * by) * w + 16 * bx);
+#pragma unroll
+		for (int pass = 0; pass < 2; ++pass) {
+			const int r = (lane >> 2) + 8 * pass, k = lane & 3;
+			dst[WIN + 4 * r + k] = __ldg(cb + (size_t)r * (w >> 2) + k);
+		}
+	}
+	__syncwarp();
+	// 2. Search.
 	const int seg = lane / ND, dx = lane - seg * ND;
-	const int blk = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * BPW + seg;
+	const int blk = blk0 + seg;
 	const bool active = seg < BPW && blk < nblk;
 	uint32_t key = 0xffffffffu;
 	int cy = 0, cx = 0;
 	if (active) {
-		const int by = blk / nbx, bx = blk - by * nbx;
-		const int y0 = 16 * by, x0 = 16 * bx;
+		const int bx = blk - (blk / nbx) * nbx;
 		if (centers) { cy = __ldg(centers + 2 * blk); cx = __ldg(centers + 2 * blk + 1); }
-		const int ys = y0 + cy - R, xs = x0 + cx - R + dx;
-		// the 16 columns inside the row: five aligned words cover them (xa + 20 <= w when sh != 0, w % 4 == 0)
-		const bool inside = xs >= 0 && xs + 16 <= w;
-		const int xa = xs & ~3, sh = xs & 3;
-		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
+		const int off = ((16 * bx + cx - R) & 3) + dx;  // byte of this lane's first column in a staged row
+		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(off & 3);
+		const uint32_t* win = ws + seg * SEG + (off >> 2);  // words off/4 .. off/4 + 4 < WW
+		const uint4* blkrows = reinterpret_cast<const uint4*>(ws + seg * SEG + WIN);
 		auto window_row = [&](int wr, uint32_t (&v)[4]) {
-			const uint8_t* row = ref + (size_t)min(max(ys + wr, 0), h - 1) * w;
-			if (inside) {
-				const uint32_t* rw = reinterpret_cast<const uint32_t*>(row + xa);
-				uint32_t u[5];
+			uint32_t u[5];
 #pragma unroll
-				for (int k = 0; k < 4; ++k) u[k] = __ldg(rw + k);
-				u[4] = sh ? __ldg(rw + 4) : 0u;
+			for (int k = 0; k < 5; ++k) u[k] = win[wr * WW + k];
 #pragma unroll
-				for (int k = 0; k < 4; ++k) v[k] = __byte_perm(u[k], u[k + 1], sel);
-			} else {
-#pragma unroll
-				for (int k = 0; k < 4; ++k) {
-					uint32_t t = 0;
-#pragma unroll
-					for (int j = 0; j < 4; ++j) t |= (uint32_t)__ldg(row + min(max(xs + 4 * k + j, 0), w - 1)) << (8 * j);
-					v[k] = t;
-				}
-			}
+			for (int k = 0; k < 4; ++k) v[k] = __byte_perm(u[k], u[k + 1], sel);
 		};
 		uint32_t ring[ND][4], cost[ND];
 #pragma unroll
@@ -632,15 +665,8 @@ __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict
 #pragma unroll
 		for (int br = 0; br < 16; ++br) {
 			window_row(br + ND - 1, ring[(br + ND - 1) % ND]);
-			const uint8_t* p = cur + (size_t)(y0 + br) * w + x0;
-			uint32_t c[4];
-			if (cur16) {
-				const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-				c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
-			} else {
-#pragma unroll
-				for (int k = 0; k < 4; ++k) c[k] = __ldg(reinterpret_cast<const uint32_t*>(p) + k);
-			}
+			const uint4 cv = blkrows[br];
+			const uint32_t c[4] = {cv.x, cv.y, cv.z, cv.w};
 #pragma unroll
 			for (int d = 0; d < ND; ++d)  // block row br meets window row br + d at vertical displacement d - R
 #pragma unroll
@@ -650,9 +676,9 @@ __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict
 		for (int d = 0; d < ND; ++d) key = min(key, (cost[d] << 8) | (uint32_t)(d * ND + dx));
 	}
 #pragma unroll
-	for (int off = 1; off < 16; off <<= 1) {  // segmented min over the block's ND <= 16 lanes
-		const uint32_t o = __shfl_down_sync(0xffffffffu, key, off);
-		if (dx + off < ND) key = min(key, o);
+	for (int o = 1; o < 16; o <<= 1) {  // segmented min over the block's ND <= 16 lanes
+		const uint32_t v = __shfl_down_sync(0xffffffffu, key, o);
+		if (dx + o < ND) key = min(key, v);
 	}
 	if (active && dx == 0) {
 		const int idx = (int)(key & 0xffu), iy = idx / ND, ix = idx - iy * ND;
@@ -664,24 +690,23 @@ __global__ void __launch_bounds__(128) me_small_kernel(const uint8_t* __restrict
 
 template <int R>
 umi_status launch_small_r(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
-                          bool cur16, cudaStream_t st) {
+                          cudaStream_t st) {
 	constexpr int BPW = 32 / (2 * R + 1);
 	const int warps = (g.nblk + BPW - 1) / BPW;
-	me_small_kernel<R><<<(warps + 3) / 4, 128, 0, st>>>(cur, ref, centers, out, g.h, g.w, g.nbx, g.nblk, cur16);
+	me_small_kernel<R><<<(warps + 3) / 4, 128, 0, st>>>(cur, ref, centers, out, g.h, g.w, g.nbx, g.nblk);
 	return umi::launch_status("me_small_kernel");
 }
 
 umi_status launch_small(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
                         cudaStream_t st) {
-	const bool cur16 = umi::aligned(cur, 16) && g.w % 16 == 0;
 	switch (g.r) {
-		case 1: return launch_small_r<1>(cur, ref, centers, out, g, cur16, st);
-		case 2: return launch_small_r<2>(cur, ref, centers, out, g, cur16, st);
-		case 3: return launch_small_r<3>(cur, ref, centers, out, g, cur16, st);
-		case 4: return launch_small_r<4>(cur, ref, centers, out, g, cur16, st);
-		case 5: return launch_small_r<5>(cur, ref, centers, out, g, cur16, st);
-		case 6: return launch_small_r<6>(cur, ref, centers, out, g, cur16, st);
-		default: return launch_small_r<7>(cur, ref, centers, out, g, cur16, st);
+		case 1: return launch_small_r<1>(cur, ref, centers, out, g, st);
+		case 2: return launch_small_r<2>(cur, ref, centers, out, g, st);
+		case 3: return launch_small_r<3>(cur, ref, centers, out, g, st);
+		case 4: return launch_small_r<4>(cur, ref, centers, out, g, st);
+		case 5: return launch_small_r<5>(cur, ref, centers, out, g, st);
+		case 6: return launch_small_r<6>(cur, ref, centers, out, g, st);
+		default: return launch_small_r<7>(cur, ref, centers, out, g, st);
 	}
 }
 
