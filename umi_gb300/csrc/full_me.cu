@@ -825,6 +825,9 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	// 96 KB of shared memory (the argmin search keeps two such buffers) and
 	// the 64-slot argmin table.
 	int m = std::max(1, 256 / g.tasks_per_mb);
+	// Argmin search with one macroblock's tasks filling the CTA: two per group
+	// when two CTAs still fit an SM (half the group barriers per macroblock).
+	if (!volume && m == 1 && 2 * 2 * (size_t)g.mb_stride * 4 <= 112 * 1024) m = 2;
 	const int max_m_smem = std::max(1, (int)((96 * 1024) / (g.mb_stride * 4)));
 	m = std::min(std::min(m, max_m_smem), 64);
 	g.m = m;
