@@ -59,7 +59,8 @@ def test_wfilter3x3_pp_f32(umi, orc, dev, h, w):
 
 
 @pytest.mark.parametrize("c,h,w,nd", [(32, 4, 300, 64), (32, 3, 64, 64), (8, 5, 70, 32), (3, 2, 40, 16), (32, 1, 1, 64),
-                                      (13, 3, 257, 64)])
+                                      (13, 3, 257, 64), (13, 3, 256, 64), (32, 2, 4, 64), (32, 3, 640, 64),
+                                      (1, 1, 128, 64), (32, 2, 132, 64), (32, 1, 1924, 64)])
 def test_cost_volume_dot_f32(umi, orc, dev, c, h, w, nd):
     g = np.random.default_rng(c * 100 + w)
     L = g.standard_normal((c, h, w)).astype(np.float32)
@@ -115,14 +116,22 @@ def test_batch_cost_volume(umi, orc, dev):
     g = np.random.default_rng(6)
     Ls = [g.standard_normal((32,) + s).astype(np.float32) for s in sizes]
     Rs = [g.standard_normal((32,) + s).astype(np.float32) for s in sizes]
-    outs = [torch.full(s + (64,), -7.0, device=dev) for s in sizes]
-    umi.batch_run(umi.OP_COST_VOLUME, [(_t(L, dev), _t(R, dev), o) for L, R, o in zip(Ls, Rs, outs)],
-                  umi.BatchParams(0, 0.0, 0.0, 32, 64))
-    for L, R, o in zip(Ls, Rs, outs):
-        if L.size:
-            want = orc.cost_volume_dot_f64(L, R, 64)
-            got = o.cpu().numpy()
-            assert np.max(np.abs(got - want) / np.maximum(np.maximum(np.abs(want), _cv_scale(L, R, 64)), 1e-30)) <= TOL
+    want = [orc.cost_volume_dot_f64(L, R, 64) if L.size else None for L, R in zip(Ls, Rs)]
+    # variant 0: tensor cores, variant 1: FP32 pipe; ragged widths and widths cut to multiples of 4
+    sizes4 = [(h, w - w % 4) for h, w in sizes]
+    Ls4 = [L[:, :, :w] for L, (h, w) in zip(Ls, sizes4)]
+    Rs4 = [R[:, :, :w] for R, (h, w) in zip(Rs, sizes4)]
+    want4 = [orc.cost_volume_dot_f64(L, R, 64) if L.size else None for L, R in zip(Ls4, Rs4)]
+    for v in range(umi.batch_variants(umi.OP_COST_VOLUME)):
+        for ls, rs, sz, wn in ((Ls, Rs, sizes, want), (Ls4, Rs4, sizes4, want4)):
+            outs = [torch.full(s + (64,), -7.0, device=dev) for s in sz]
+            umi.batch_run(umi.OP_COST_VOLUME, [(_t(L, dev), _t(R, dev), o) for L, R, o in zip(ls, rs, outs)],
+                          umi.BatchParams(0, 0.0, 0.0, 32, 64), variant=v)
+            for L, R, o, wv in zip(ls, rs, outs, wn):
+                if wv is not None:
+                    got = o.cpu().numpy()
+                    err = np.max(np.abs(got - wv) / np.maximum(np.maximum(np.abs(wv), _cv_scale(L, R, 64)), 1e-30))
+                    assert err <= TOL, (v, L.shape)
 
 
 def test_autotune_batch_picks_a_variant(umi, dev):

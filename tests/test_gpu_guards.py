@@ -90,6 +90,14 @@ def test_guards_batched_ops(umi, dev):
     umi.cost_volume_dot_f32(L, R, 64, out=out)
     torch.cuda.synchronize()
     assert _guards_ok(full)
+    # the tensor-core cost volume (16-byte aligned rows): ragged last tile, bulk stores of partial warps
+    for w in (76, 200, 4, 131):
+        L = torch.rand((32, 13, w), generator=g, device=dev)
+        R = torch.rand((32, 13, w), generator=g, device=dev)
+        full, out = _guarded((13, w, 64), torch.float32, dev)
+        umi.cost_volume_dot_f32(L, R, 64, out=out)
+        torch.cuda.synchronize()
+        assert _guards_ok(full), w
 
 
 def test_guards_gemm_conv(umi, dev):

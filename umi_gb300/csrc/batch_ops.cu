@@ -18,6 +18,7 @@
 #include <new>
 
 #include "common.h"
+#include "tc_common.cuh"
 
 namespace {
 
@@ -325,6 +326,233 @@ struct CostVolume {
 	}
 };
 
+// ------------------------------------------------------------------ cost volume on tcgen05
+// cv[y, x, d] = sum_c L[c, y, x] R[c, y, x + d], d = 0..63, C <= 32, as a
+// banded matrix product per image row: for the 128 pixels x0 .. x0 + 127 and
+// the 192 right columns x0 .. x0 + 191 (zero past the row end),
+//   P = A B^T,  A[p][c] = L[c, y, x0 + p],  B[n][c] = R[c, y, x0 + n],
+//   cv[y, x0 + p, d] = P[p][p + d].
+// Each fp32 operand is split into tf32 parts x = hi + lo (hi = x rounded to
+// tf32, lo = x - hi exactly, then rounded to tf32), and
+// P = Ahi Bhi + Ahi Blo + Alo Bhi (the dropped lo*lo term is ~2^-22 of the
+// product) on tcgen05.mma kind::tf32 with fp32 accumulation in TMEM: three
+// M=128 N=192 MMAs per 8 channels.  A pixel's 32 channels are one 128-byte
+// row of the K-major, 128-byte-swizzled operand tiles (the layout of the
+// bf16 GEMM in gemm_tc.cu; a K step of 8 tf32 is 32 bytes).
+//
+// Roles (416 threads): warps 0-3 and 4-7 are two producer groups taking
+// alternate tiles, each filling its own operand stage (plain loads, split,
+// swizzled 16-byte stores, then a proxy fence and an mbarrier arrive), so two
+// tiles' loads are in flight per SM; warp 8 allocates TMEM (two accumulators
+// of 192 columns) and one lane issues the MMAs; warps 9-12 drain an
+// accumulator while the next tile computes: lane p of a warp holds TMEM row
+// p (one pixel), loads the 96 columns its warp's band touches, stores its 64
+// with predicated conflict-free shared stores (word 63 p + j) and the warp
+// writes its 32 pixels x 64 disparities (8 KB, contiguous in cv) with one
+// bulk copy.  Every wait is bounded (tc_common.cuh).
+namespace cvtc {
+constexpr int BM = 128, ND = 64, BNN = BM + ND, KC = 32;
+constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BNN * 128;
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // Ahi, Alo, Bhi, Blo
+constexpr uint32_t OUT_WARP_BYTES = 32 * ND * 4;
+constexpr int NTH = 13 * 32;
+constexpr size_t SMEM = 2 * (size_t)STAGE_BYTES + 4 * OUT_WARP_BYTES + 1024 + 256;
+constexpr uint32_t TMEM_COLS = 512;  // 2 x 192, rounded to a power of two
+// kind::tf32 instruction descriptor: fp32 accumulator (bits 4-5 = 1), A and
+// B tf32 (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BNN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+static_assert(SMEM <= 227 * 1024, "one CTA per SM");
+
+struct Params { int channels; };
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return r;
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"setp.ne.b32 p, %4, 0;\n\t"
+		"tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+		"l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)acc)
+		: "memory");
+}
+// shared -> global bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+	asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(umi_tc::smem_u32(src)),
+	             "r"(bytes)
+	             : "memory");
+}
+
+// Row `row` (pixel or right column) of the operand tiles: 32 channels of
+// column x of image row y, split into tf32 hi / lo and stored as 8 swizzled
+// 16-byte chunks (chunk j of row r at j ^ (r & 7)).
+__device__ __forceinline__ void load_row(const float* __restrict__ src, size_t plane, int C, bool valid, float (&v)[KC]) {
+#pragma unroll
+	for (int c = 0; c < KC; ++c) v[c] = (valid && c < C) ? __ldg(src + (size_t)c * plane) : 0.0f;
+}
+__device__ __forceinline__ void store_row(uint8_t* hi, uint8_t* lo, int row, const float (&v)[KC]) {
+#pragma unroll
+	for (int j = 0; j < 8; ++j) {
+		uint32_t h[4], l[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			h[k] = to_tf32(v[4 * j + k]);
+			l[k] = to_tf32(v[4 * j + k] - __uint_as_float(h[k]));
+		}
+		const uint32_t off = (uint32_t)row * 128u + ((uint32_t)(j ^ (row & 7)) << 4);
+		*reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+		*reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+	}
+}
+}  // namespace cvtc
+
+struct CostVolumeTc {  // tiles of 128 pixels of one row
+	static int tiles_x(int w) { return umi::ceil_div(w, cvtc::BM); }
+	static int tiles(int h, int w) { return tiles_x(w) * h; }
+};
+
+__global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Table t, const cvtc::Params prm, int* err) {
+	using namespace umi_tc;
+	using namespace cvtc;
+	extern __shared__ uint8_t smem_raw[];
+	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	uint8_t* outbuf = base + 2 * STAGE_BYTES;
+	uint64_t* full = reinterpret_cast<uint64_t*>(outbuf + 4 * OUT_WARP_BYTES);  // [2]
+	uint64_t* empty = full + 2;     // [2]
+	uint64_t* accfull = empty + 2;  // [2]
+	uint64_t* accempty = accfull + 2;
+	uint64_t* drain = accempty + 2;
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int total = t.start[t.n];
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < 2; ++s) {
+			mbar_init(&full[s], 128);  // the 128 threads of a producer group
+			mbar_init(&empty[s], 1);
+			mbar_init(&accfull[s], 1);
+			mbar_init(&accempty[s], 4);  // one arrive per epilogue warp
+		}
+		mbar_init(drain, 1);
+		*abort_flag = 0;
+		fence_mbar_init();
+	}
+	if (warp == 8) {
+		tmem_alloc(tmem_slot, TMEM_COLS);
+		tmem_relinquish();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = *tmem_slot;
+
+	if (warp < 8) {
+		// ---- producers: group G takes tiles G, G + 2, ... of this CTA into stage G
+		const int G = warp >> 2, tg = threadIdx.x & 127;
+		uint8_t* st_base = base + G * STAGE_BYTES;
+		int u = 0;
+		for (int tile = blockIdx.x + G * gridDim.x; tile < total && !*abort_flag; tile += 2 * gridDim.x, ++u) {
+			if (!mbar_wait(&empty[G], (uint32_t)(u & 1) ^ 1u, abort_flag, err, kErrTimeoutEmpty)) break;
+			const int i = find_image(t, tile);
+			const Img& im = t.img[i];
+			const int lt = tile - t.start[i], y = lt / im.tiles_x, x0 = (lt - y * im.tiles_x) * BM;
+			const size_t plane = (size_t)im.h * im.w, row0 = (size_t)y * im.w;
+			// rows tg (A pixel), 128 + tg and 256 + tg (B columns tg, 128 + tg) of the 320 operand rows
+			float va[KC], vb[KC], vc[KC];
+			load_row(im.in + row0 + x0 + tg, plane, prm.channels, x0 + tg < im.w, va);
+			load_row(im.aux + row0 + x0 + tg, plane, prm.channels, x0 + tg < im.w, vb);
+			const bool two = tg < BNN - BM;
+			load_row(im.aux + row0 + x0 + BM + tg, plane, prm.channels, two && x0 + BM + tg < im.w, vc);
+			store_row(st_base, st_base + A_BYTES, tg, va);
+			uint8_t* bhi = st_base + 2 * A_BYTES;
+			store_row(bhi, bhi + B_BYTES, tg, vb);
+			if (two) store_row(bhi, bhi + B_BYTES, BM + tg, vc);
+			fence_proxy_async_smem();  // generic-proxy stores visible to the MMA
+			mbar_arrive(&full[G]);
+		}
+	} else if (warp == 8) {
+		if (lane == 0) {
+			// ---- MMA issuer
+			int i = 0;
+			for (int tile = blockIdx.x; tile < total && !*abort_flag; tile += gridDim.x, ++i) {
+				const int s = i & 1;
+				const uint32_t use = (uint32_t)(i >> 1);
+				if (!mbar_wait(&accempty[s], (use & 1) ^ 1u, abort_flag, err, kErrTimeoutAccEmpty)) break;
+				if (!mbar_wait(&full[s], use & 1, abort_flag, err, kErrTimeoutFull)) break;
+				tc_fence_after();
+				const uint32_t acc = tmem + (uint32_t)(s * BNN);
+				const uint32_t sb = smem_u32(base + s * STAGE_BYTES);
+				const uint64_t ahi = desc_kmajor_sw128(sb), alo = desc_kmajor_sw128(sb + A_BYTES);
+				const uint64_t bhi = desc_kmajor_sw128(sb + 2 * A_BYTES), blo = desc_kmajor_sw128(sb + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+				for (int kk = 0; kk < KC / 8; ++kk) {  // 8 tf32 = 32 bytes per K step
+					mma_tf32(acc, ahi + 2 * kk, bhi + 2 * kk, IDESC, kk > 0);
+					mma_tf32(acc, ahi + 2 * kk, blo + 2 * kk, IDESC, true);
+					mma_tf32(acc, alo + 2 * kk, bhi + 2 * kk, IDESC, true);
+				}
+				mma_commit(&empty[s]);
+				mma_commit(&accfull[s]);
+			}
+			mma_commit(drain);  // every MMA issued above finishes before TMEM is freed
+			volatile int own = 0;
+			mbar_wait(drain, 0, &own, err, kErrTimeoutAccum);
+		}
+		__syncwarp();
+	} else {
+		// ---- epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (pixels of the tile)
+		const int qd = warp & 3;
+		float* ob = reinterpret_cast<float*>(outbuf + qd * OUT_WARP_BYTES);
+		int i = 0;
+		for (int tile = blockIdx.x; tile < total; tile += gridDim.x, ++i) {
+			const int s = i & 1;
+			const uint32_t use = (uint32_t)(i >> 1);
+			if (!mbar_wait(&accfull[s], use & 1, abort_flag, err, kErrTimeoutAccum)) break;
+			tc_fence_after();
+			float v0[32], v1[32], v2[32];
+			const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(s * BNN + 32 * qd);
+			tmem_ld32(ta, v0);
+			tmem_ld32(ta + 32, v1);
+			tmem_ld32(ta + 64, v2);
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&accempty[s]);
+			const int idx = find_image(t, tile);
+			const Img& im = t.img[idx];
+			const int lt = tile - t.start[idx], y = lt / im.tiles_x, x0 = (lt - y * im.tiles_x) * BM;
+			const int px0 = x0 + 32 * qd, nvalid = min(32, im.w - px0);
+			if (lane == 0) bulk_wait_all();  // the previous store has finished with ob
+			__syncwarp();
+			// lane p keeps columns p .. p + 63 of the 96 it holds: word 64 p + (j - p) = 63 p + j
+#pragma unroll
+			for (int j = 0; j < 32; ++j) {
+				if (j >= lane) ob[63 * lane + j] = v0[j];
+			}
+#pragma unroll
+			for (int j = 0; j < 32; ++j) ob[63 * lane + 32 + j] = v1[j];
+#pragma unroll
+			for (int j = 0; j < 32; ++j) {
+				if (64 + j - lane < ND) ob[63 * lane + 64 + j] = v2[j];
+			}
+			fence_proxy_async_smem();
+			__syncwarp();
+			if (lane == 0 && nvalid > 0) {
+				bulk_store(im.out + ((size_t)y * im.w + px0) * ND, ob, (uint32_t)nvalid * ND * 4);
+				bulk_commit();
+			}
+		}
+		if (lane == 0) bulk_wait_all();
+		__syncwarp();
+	}
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 8) {
+		tc_fence_after();
+		tmem_dealloc(tmem, TMEM_COLS);
+	}
+}
+
 // ------------------------------------------------------------------ launcher
 template <class Op, class P>
 __global__ void __launch_bounds__(NT, 2) batch_kernel(const Table t, const P p) {
@@ -336,9 +564,8 @@ __global__ void __launch_bounds__(NT, 2) batch_kernel(const Table t, const P p) 
 	}
 }
 
-template <class Op, class P>
-umi_status launch(const umi_batch_image* images, int n, const P& p, bool need_aux, cudaStream_t st) {
-	Table t;
+template <class Op>
+umi_status make_table(const umi_batch_image* images, int n, bool need_aux, Table& t) {
 	t.n = n;
 	t.start[0] = 0;
 	for (int i = 0; i < n; ++i) {
@@ -356,6 +583,13 @@ umi_status launch(const umi_batch_image* images, int n, const P& p, bool need_au
 		if (t.start[i] + nt > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "batch too large");
 		t.start[i + 1] = t.start[i] + (int)nt;
 	}
+	return UMI_OK;
+}
+
+template <class Op, class P>
+umi_status launch(const umi_batch_image* images, int n, const P& p, bool need_aux, cudaStream_t st) {
+	Table t;
+	UMI_TRY(make_table<Op>(images, n, need_aux, t));
 	if (t.start[n] == 0) return UMI_OK;
 	auto kern = batch_kernel<Op, P>;
 	const size_t smem = Op::smem;
@@ -372,6 +606,35 @@ umi_status launch(const umi_batch_image* images, int n, const P& p, bool need_au
 	return umi::launch_status("batch_kernel");
 }
 
+// The tensor-core cost volume: nd = 64, channels <= 32 and a 16-byte aligned
+// output for every image (its bulk stores start at multiples of 256 bytes
+// from it); inputs are read with scalar loads, any width (else the FP32
+// kernel serves).
+bool cv_tc_eligible(const umi_batch_image* images, int n, const umi_batch_params& bp) {
+	if (bp.nd != cvtc::ND || bp.channels < 1 || bp.channels > cvtc::KC) return false;
+	for (int i = 0; i < n; ++i) {
+		const umi_batch_image& b = images[i];
+		if (b.h == 0 || b.w == 0) continue;
+		if (!umi::aligned(b.out, 16)) return false;
+	}
+	return true;
+}
+
+umi_status launch_cv_tc(const umi_batch_image* images, int n, int channels, cudaStream_t st) {
+	Table t;
+	UMI_TRY(make_table<CostVolumeTc>(images, n, true, t));
+	if (t.start[n] == 0) return UMI_OK;
+	auto kern = cost_volume_tc_kernel;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cvtc::SMEM),
+	                         "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	const int grid = std::max(1, std::min(t.start[n], sms));  // one CTA per SM (shared memory, TMEM)
+	kern<<<grid, cvtc::NTH, cvtc::SMEM, st>>>(t, cvtc::Params{channels}, nullptr);
+	return umi::launch_status("cost_volume_tc_kernel");
+}
+
 // Variant tables.
 constexpr int kBilVariants = 4;
 template <int R>
@@ -384,7 +647,7 @@ umi_status run_bilateral_r(const umi_batch_image* im, int n, const BilParams& p,
 	}
 }
 constexpr int kWfVariants = 3;
-constexpr int kCvVariants = 1;
+constexpr int kCvVariants = 2;  // tensor cores (where eligible), FP32
 
 umi_status run_bilateral(const umi_batch_image* im, int n, const umi_batch_params& bp, int v, cudaStream_t st) {
 	if (bp.radius < 1 || bp.radius > 3) return umi::fail(UMI_ERR_UNSUPPORTED, "bilateral: radius %d (1..3)", bp.radius);
@@ -414,8 +677,9 @@ umi_status run_wfilter(const umi_batch_image* im, int n, int v, cudaStream_t st)
 }
 
 umi_status run_cost_volume(const umi_batch_image* im, int n, const umi_batch_params& bp, int v, cudaStream_t st) {
-	(void)v;
 	if (bp.channels < 1) return umi::fail(UMI_ERR_INVALID_ARG, "cost volume: %d channels", bp.channels);
+	// variant 0 (default): the tensor-core kernel where it applies; variant 1: the FP32 kernel
+	if (v != 1 && cv_tc_eligible(im, n, bp)) return launch_cv_tc(im, n, bp.channels, st);
 	const CvParams p{bp.channels};
 	switch (bp.nd) {
 		case 16: return launch<CostVolume<2>>(im, n, p, true, st);
