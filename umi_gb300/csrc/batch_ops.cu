@@ -340,23 +340,25 @@ struct CostVolume {
 // row of the K-major, 128-byte-swizzled operand tiles (the layout of the
 // bf16 GEMM in gemm_tc.cu; a K step of 8 tf32 is 32 bytes).
 //
-// Roles (416 threads): warps 0-3 and 4-7 are two producer groups taking
-// alternate tiles, each filling its own operand stage (plain loads, split,
-// swizzled 16-byte stores, then a proxy fence and an mbarrier arrive), so two
-// tiles' loads are in flight per SM; warp 8 allocates TMEM (two accumulators
-// of 192 columns) and one lane issues the MMAs; warps 9-12 drain an
-// accumulator while the next tile computes: lane p of a warp holds TMEM row
-// p (one pixel), loads the 96 columns its warp's band touches, stores its 64
-// with predicated conflict-free shared stores (word 63 p + j) and the warp
-// writes its 32 pixels x 64 disparities (8 KB, contiguous in cv) with one
-// bulk copy.  Every wait is bounded (tc_common.cuh).
+// Roles (480 threads): warps 0-4 and 5-9 are two producer groups taking
+// alternate tiles, each filling its own operand stage (plain loads of two
+// operand rows per thread, split, swizzled 16-byte stores, then a proxy fence
+// and an mbarrier arrive), so two tiles' loads are in flight per SM; warp 10
+// allocates TMEM (two accumulators of 192 columns) and one lane issues the
+// MMAs; warps 11-14 drain an accumulator while the next tile computes: lane p
+// of a warp holds TMEM row p (one pixel), loads the 96 columns its warp's band
+// touches (32 at a time), stores its 64 with predicated conflict-free shared
+// stores (word 63 p + j) into one of two staging buffers, and the warp writes
+// its 32 pixels x 64 disparities (8 KB, contiguous in cv) with one bulk copy.
+// Every wait is bounded (tc_common.cuh).
 namespace cvtc {
 constexpr int BM = 128, ND = 64, BNN = BM + ND, KC = 32;
 constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BNN * 128;
 constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // Ahi, Alo, Bhi, Blo
 constexpr uint32_t OUT_WARP_BYTES = 32 * ND * 4;
-constexpr int NTH = 13 * 32;
-constexpr size_t SMEM = 2 * (size_t)STAGE_BYTES + 4 * OUT_WARP_BYTES + 1024 + 256;
+constexpr int PG = 160;          // threads per producer group: 320 operand rows, two per thread
+constexpr int NTH = 15 * 32;    // warps 0-4, 5-9 producers; 10 MMA; 11-14 epilogue
+constexpr size_t SMEM = 2 * (size_t)STAGE_BYTES + 8 * OUT_WARP_BYTES + 1024 + 256;  // two staging buffers per epilogue warp
 constexpr uint32_t TMEM_COLS = 512;  // 2 x 192, rounded to a power of two
 // kind::tf32 instruction descriptor: fp32 accumulator (bits 4-5 = 1), A and
 // B tf32 (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 	uint8_t* outbuf = base + 2 * STAGE_BYTES;
-	uint64_t* full = reinterpret_cast<uint64_t*>(outbuf + 4 * OUT_WARP_BYTES);  // [2]
+	uint64_t* full = reinterpret_cast<uint64_t*>(outbuf + 8 * OUT_WARP_BYTES);  // [2]
 	uint64_t* empty = full + 2;     // [2]
 	uint64_t* accfull = empty + 2;  // [2]
 	uint64_t* accempty = accfull + 2;
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	const int total = t.start[t.n];
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < 2; ++s) {
-			mbar_init(&full[s], 128);  // the 128 threads of a producer group
+			mbar_init(&full[s], PG);  // the threads of a producer group
 			mbar_init(&empty[s], 1);
 			mbar_init(&accfull[s], 1);
 			mbar_init(&accempty[s], 4);  // one arrive per epilogue warp
@@ -439,7 +441,7 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 		*abort_flag = 0;
 		fence_mbar_init();
 	}
-	if (warp == 8) {
+	if (warp == 10) {
 		tmem_alloc(tmem_slot, TMEM_COLS);
 		tmem_relinquish();
 	}
@@ -448,31 +450,32 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	tc_fence_after();
 	const uint32_t tmem = *tmem_slot;
 
-	if (warp < 8) {
+	if (warp < 10) {
 		// ---- producers: group G takes tiles G, G + 2, ... of this CTA into stage G
-		const int G = warp >> 2, tg = threadIdx.x & 127;
+		const int G = warp / 5, tg = threadIdx.x - G * PG;
 		uint8_t* st_base = base + G * STAGE_BYTES;
 		int u = 0;
 		for (int tile = blockIdx.x + G * gridDim.x; tile < total && !*abort_flag; tile += 2 * gridDim.x, ++u) {
-			if (!mbar_wait(&empty[G], (uint32_t)(u & 1) ^ 1u, abort_flag, err, kErrTimeoutEmpty)) break;
 			const int i = find_image(t, tile);
 			const Img& im = t.img[i];
 			const int lt = tile - t.start[i], y = lt / im.tiles_x, x0 = (lt - y * im.tiles_x) * BM;
 			const size_t plane = (size_t)im.h * im.w, row0 = (size_t)y * im.w;
-			// rows tg (A pixel), 128 + tg and 256 + tg (B columns tg, 128 + tg) of the 320 operand rows
-			float va[KC], vb[KC], vc[KC];
-			load_row(im.in + row0 + x0 + tg, plane, prm.channels, x0 + tg < im.w, va);
-			load_row(im.aux + row0 + x0 + tg, plane, prm.channels, x0 + tg < im.w, vb);
-			const bool two = tg < BNN - BM;
-			load_row(im.aux + row0 + x0 + BM + tg, plane, prm.channels, two && x0 + BM + tg < im.w, vc);
-			store_row(st_base, st_base + A_BYTES, tg, va);
+			// operand rows r = tg and tg + 160 of 320: r < 128 is pixel r of A (L), else column r - 128 of B (R)
+			float va[KC], vb[KC];
+			const int r0 = tg, r1 = tg + PG;  // r1 >= 160: always a B row
+			const int xa = r0 < BM ? r0 : r0 - BM, xb = r1 - BM;
+			load_row((r0 < BM ? im.in : im.aux) + row0 + x0 + xa, plane, prm.channels, x0 + xa < im.w, va);
+			load_row(im.aux + row0 + x0 + xb, plane, prm.channels, x0 + xb < im.w, vb);
+			// the loads are in flight while the stage's previous MMAs finish
+			if (!mbar_wait(&empty[G], (uint32_t)(u & 1) ^ 1u, abort_flag, err, kErrTimeoutEmpty)) break;
 			uint8_t* bhi = st_base + 2 * A_BYTES;
-			store_row(bhi, bhi + B_BYTES, tg, vb);
-			if (two) store_row(bhi, bhi + B_BYTES, BM + tg, vc);
+			if (r0 < BM) store_row(st_base, st_base + A_BYTES, r0, va);
+			else store_row(bhi, bhi + B_BYTES, xa, va);
+			store_row(bhi, bhi + B_BYTES, xb, vb);
 			fence_proxy_async_smem();  // generic-proxy stores visible to the MMA
 			mbar_arrive(&full[G]);
 		}
-	} else if (warp == 8) {
+	} else if (warp == 10) {
 		if (lane == 0) {
 			// ---- MMA issuer
 			int i = 0;
@@ -503,38 +506,35 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	} else {
 		// ---- epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (pixels of the tile)
 		const int qd = warp & 3;
-		float* ob = reinterpret_cast<float*>(outbuf + qd * OUT_WARP_BYTES);
 		int i = 0;
 		for (int tile = blockIdx.x; tile < total; tile += gridDim.x, ++i) {
 			const int s = i & 1;
 			const uint32_t use = (uint32_t)(i >> 1);
 			if (!mbar_wait(&accfull[s], use & 1, abort_flag, err, kErrTimeoutAccum)) break;
 			tc_fence_after();
-			float v0[32], v1[32], v2[32];
-			const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(s * BNN + 32 * qd);
-			tmem_ld32(ta, v0);
-			tmem_ld32(ta + 32, v1);
-			tmem_ld32(ta + 64, v2);
-			tc_fence_before();
-			__syncwarp();
-			if (lane == 0) mbar_arrive(&accempty[s]);
 			const int idx = find_image(t, tile);
 			const Img& im = t.img[idx];
 			const int lt = tile - t.start[idx], y = lt / im.tiles_x, x0 = (lt - y * im.tiles_x) * BM;
 			const int px0 = x0 + 32 * qd, nvalid = min(32, im.w - px0);
-			if (lane == 0) bulk_wait_all();  // the previous store has finished with ob
+			float* ob = reinterpret_cast<float*>(outbuf + (2 * qd + (i & 1)) * OUT_WARP_BYTES);
+			if (lane == 0) bulk_wait_read_1();  // the store that last used ob (two tiles ago) has read it
 			__syncwarp();
-			// lane p keeps columns p .. p + 63 of the 96 it holds: word 64 p + (j - p) = 63 p + j
+			// lane p keeps columns p .. p + 63 of the 96 its warp's band touches, at word
+			// 64 p + (j - p) = 63 p + j (conflict-free); one 32-column load at a time
+			const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(s * BNN + 32 * qd);
 #pragma unroll
-			for (int j = 0; j < 32; ++j) {
-				if (j >= lane) ob[63 * lane + j] = v0[j];
+			for (int k = 0; k < 3; ++k) {
+				float v[32];
+				tmem_ld32(ta + 32 * k, v);
+#pragma unroll
+				for (int j = 0; j < 32; ++j) {
+					const int d = 32 * k + j - lane;
+					if (d >= 0 && d < ND) ob[63 * lane + 32 * k + j] = v[j];
+				}
 			}
-#pragma unroll
-			for (int j = 0; j < 32; ++j) ob[63 * lane + 32 + j] = v1[j];
-#pragma unroll
-			for (int j = 0; j < 32; ++j) {
-				if (64 + j - lane < ND) ob[63 * lane + 64 + j] = v2[j];
-			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&accempty[s]);
 			fence_proxy_async_smem();
 			__syncwarp();
 			if (lane == 0 && nvalid > 0) {
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	}
 	tc_fence_before();
 	__syncthreads();
-	if (warp == 8) {
+	if (warp == 10) {
 		tc_fence_after();
 		tmem_dealloc(tmem, TMEM_COLS);
 	}
