@@ -45,7 +45,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # scaled to the configured batch.
 NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
                "fprop_n32": 67321088 + 206541312, "learned_me_4k": None, "coarse_me_4k": None}
-NCU_TRAFFIC_PER_PX = {"batched_uneven": (3605180000 + 3255675000) / 12896910}
+NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 + 3253943000) / 12896910}
 
 
 def parse():
