@@ -1013,11 +1013,24 @@ def run_ours(args, wl, dist):
     elif isinstance(wl, Fprop):
         kt = kms["conv2d_fprop_bf16"]
         ach = wl.flops / (kt * 1e-3) / 1e12
+        # compulsory bytes: bf16 NHWC input + bf16 weights read once, fp32 NCHW output written once
+        nbytes = 2 * wl.N * wl.H * wl.W * wl.C + 2 * wl.K * wl.R * wl.R * wl.C + 4 * wl.N * wl.K * wl.H * wl.W
+        gbs = nbytes / (kt * 1e-3) / 1e9
         kernels["conv2d_fprop_bf16"] = {"ms_per_launch": kt, "achieved": ach, "unit": "TFLOP/s",
-                                        "frac": ach / pk["bf16_tflops"]}
-        roof = dict(kernels["conv2d_fprop_bf16"], bound="tensor", kernel="tc_kernel<conv> (bf16)",
-                    peak=pk["bf16_tflops"], traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
-                    flops_per_launch=wl.flops)
+                                        "frac": ach / pk["bf16_tflops"], "bytes_per_launch": nbytes,
+                                        "achieved_gbs": gbs, "frac_of_hbm": gbs / pk["hbm_gbs"],
+                                        "tensor_floor_ms": wl.flops / (pk["bf16_tflops"] * 1e12) * 1e3,
+                                        "hbm_floor_ms": nbytes / (pk["hbm_gbs"] * 1e9) * 1e3}
+        k = kernels["conv2d_fprop_bf16"]
+        if k["hbm_floor_ms"] >= k["tensor_floor_ms"]:  # the fp32 output makes the launch HBM-bound
+            roof = {"bound": "hbm", "kernel": "tc_kernel<conv> (bf16)", "achieved": gbs, "peak": pk["hbm_gbs"],
+                    "unit": "GB/s", "frac": gbs / pk["hbm_gbs"], "traffic": NCU_TRAFFIC.get(wl.name),
+                    "peak_source": pk["source"], "bytes_per_launch": nbytes, "ms_per_launch": kt,
+                    "tensor_frac": k["frac"]}
+        else:
+            roof = dict(k, bound="tensor", kernel="tc_kernel<conv> (bf16)", peak=pk["bf16_tflops"],
+                        traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
+                        flops_per_launch=wl.flops)
     elif isinstance(wl, LearnedMe):
         sad_peak = probe_sad4_peak(dev)
         for name, kt in kms.items():
