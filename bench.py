@@ -202,7 +202,7 @@ class IntPair:
         self.h_ref = torch.from_numpy(self.ref).pin_memory()
         self.h_ii = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
-        self.launches_per_step = 3  # iimg: 2 kernels, full_me: 1
+        self.launches_per_step = 4  # iimg: 3 kernels (column sums, carry, output), full_me: 1
 
     def step(self, i):
         k = i % self.n_rot
