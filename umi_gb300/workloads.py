@@ -77,6 +77,28 @@ def me_pair(seed: int = 3, h: int = 1080, w: int = 1920, block: int = 16, shift_
     return b, a, true_mv
 
 
+def video_frames(seed: int = 11, n: int = 8, h: int = 1080, w: int = 1920, velocity=(3, -5),
+                 noise_sigma: float = 2.0, blur_sigma: float = 2.0):
+    """A panning camera over a still scene: frame t is the window of a larger
+    clip(blur_{blur_sigma}(N(128, 40^2))) canvas whose origin moves by
+    `velocity` (dy, dx) pixels per frame, plus N(0, noise_sigma^2) sensor
+    noise per frame, as uint8.  Every block of frame t matches frame t - 1
+    at displacement (dy, dx): the scene point at (y, x) of frame t sat at
+    (y + dy, x + dx) one frame earlier."""
+    g = rng(seed)
+    vy, vx = velocity
+    my, mx = abs(vy) * max(n - 1, 0), abs(vx) * max(n - 1, 0)
+    canvas = g.normal(128.0, 40.0, size=(h + my, w + mx)).astype(np.float32)
+    canvas = gaussian_blur(canvas, blur_sigma)
+    y0, x0 = (my if vy < 0 else 0), (mx if vx < 0 else 0)
+    frames = []
+    for t in range(n):
+        oy, ox = y0 + vy * t, x0 + vx * t
+        f = canvas[oy:oy + h, ox:ox + w] + g.normal(0.0, noise_sigma, size=(h, w)).astype(np.float32)
+        frames.append(np.clip(np.rint(f), 0, 255).astype(np.uint8))
+    return frames
+
+
 def me_pair_cuda(seed: int, h: int = 2160, w: int = 3840, block: int = 16, shift_sigma: float = 16.0,
                  max_shift: int = 64, noise_sigma: float = 2.0, blur_sigma: float = 2.0, device="cuda"):
     """me_pair's distribution drawn on the GPU (torch's Philox generator, seeded).
