@@ -137,7 +137,12 @@ typedef enum umi_strategy {
 	UMI_STRATEGY_ABS_DIFF_SUM_I32 = 3,   /* main/cost_volume.cu:8-15 and main/full_me.cu: Loop(2 in) s += |a - b|; Post out = s */
 	UMI_STRATEGY_RUNNING_SUM_I32 = 4,    /* main/iimg.cu:11-18: Loop(1 in, 1 out) out = t += x */
 	UMI_STRATEGY_DOT_I32 = 5,            /* main/gemm.cu:8-15 and main/fprop.cu: Loop(2 in) t += a * b; Post out = t */
-	UMI_STRATEGY_DOT_F32 = 6             /* the same on float */
+	UMI_STRATEGY_DOT_F32 = 6,            /* the same on float */
+	/* window operators of the same family (no reference example) */
+	UMI_STRATEGY_CENSUS_I32 = 7,         /* Pre(1 in) centre; Loop(1 in) bits = bits << 1 | (x < centre); Post out = bits (last 32) */
+	UMI_STRATEGY_WEIGHTED_SUM_F32 = 8,   /* Pre t = init; Loop(2 in) t = fma(x, w, t); Post out = t; constants {float init} */
+	UMI_STRATEGY_MAX_I32 = 9,            /* Pre t = init; Loop(1 in) t = max(t, x); Post out = t; constants {int init} */
+	UMI_STRATEGY_MIN_I32 = 10            /* Pre t = init; Loop(1 in) t = min(t, x); Post out = t; constants {int init} */
 } umi_strategy;
 
 /* Generic operator through the C ABI: runs `strategy` over the plan's P x A

@@ -170,8 +170,9 @@ def plan_build(desc: Desc) -> Plan:
 
 
 (STRATEGY_NEIGHBOUR_SUM_I32, STRATEGY_WEIGHTED_SUM_I32, STRATEGY_RANGE_WEIGHTED_F32, STRATEGY_ABS_DIFF_SUM_I32,
- STRATEGY_RUNNING_SUM_I32, STRATEGY_DOT_I32, STRATEGY_DOT_F32) = range(7)
-_STRATEGY_FLOAT = {STRATEGY_RANGE_WEIGHTED_F32, STRATEGY_DOT_F32}
+ STRATEGY_RUNNING_SUM_I32, STRATEGY_DOT_I32, STRATEGY_DOT_F32, STRATEGY_CENSUS_I32, STRATEGY_WEIGHTED_SUM_F32,
+ STRATEGY_MAX_I32, STRATEGY_MIN_I32) = range(11)
+_STRATEGY_FLOAT = {STRATEGY_RANGE_WEIGHTED_F32, STRATEGY_DOT_F32, STRATEGY_WEIGHTED_SUM_F32}
 
 
 def launch(desc: Desc, strategy: int, ins, outs, pads=None, consts=None, stream=None) -> None:

@@ -11,6 +11,11 @@
 //   UMI_STRATEGY_RUNNING_SUM_I32    main/iimg.cu:11-18
 //   UMI_STRATEGY_DOT_I32            main/gemm.cu:8-15, main/fprop.cu (same strategy)
 //   UMI_STRATEGY_DOT_F32            the gemm strategy on float
+// and four more window operators of the same family (no reference example):
+//   UMI_STRATEGY_CENSUS_I32         Pre(1 in) centre; Loop(1 in) bits = bits << 1 | (x < centre); Post out = bits
+//   UMI_STRATEGY_WEIGHTED_SUM_F32   the wfilter3x3 strategy on float (constant: float init)
+//   UMI_STRATEGY_MAX_I32            Loop t = max(t, x) (grey-level dilation; constant: int init)
+//   UMI_STRATEGY_MIN_I32            Loop t = min(t, x) (grey-level erosion; constant: int init)
 // The kernel is the same closed-form generic kernel as the header-only
 // drop-in (include/umi/UMI_gpu.h); tiling never changes results, so the
 // launch runs the plan with one point per thread.
@@ -86,6 +91,41 @@ struct DotT {
 	STRATEGY_PRE_STUB(0, 0) { total = T(0); }
 	STRATEGY_LOOP_STUB(2, 0) { total += IMEM(0, 0) * IMEM(1, 0); }
 	STRATEGY_POST_STUB(0, 1) { OMEM(0, 0) = total; }
+};
+
+// Census transform: one bit per window element in the A loop order, set
+// where the element is below the centre (the last 32 elements for larger
+// windows; the centre itself contributes a 0).
+struct CensusI32 {
+	uint32_t bits;
+	int centre;
+	struct Constant {};
+	STRATEGY_TYPEDEF_STUB(int, Constant)
+	STRATEGY_PRE_STUB(1, 0) {
+		bits = 0u;
+		centre = IMEM(0, 0);
+	}
+	STRATEGY_LOOP_STUB(1, 0) { bits = (bits << 1) | (IMEM(0, 0) < centre ? 1u : 0u); }
+	STRATEGY_POST_STUB(0, 1) { OMEM(0, 0) = (int)bits; }
+};
+
+struct WeightedSumF32 {
+	float total;
+	struct Constant { float init; };
+	STRATEGY_TYPEDEF_STUB(float, Constant)
+	STRATEGY_PRE_STUB(0, 0) { total = c.init; }
+	STRATEGY_LOOP_STUB(2, 0) { total = fmaf(IMEM(0, 0), IMEM(1, 0), total); }
+	STRATEGY_POST_STUB(0, 1) { OMEM(0, 0) = total; }
+};
+
+template <bool MAX>
+struct ExtremumI32 {
+	int t;
+	struct Constant { int init; };
+	STRATEGY_TYPEDEF_STUB(int, Constant)
+	STRATEGY_PRE_STUB(0, 0) { t = c.init; }
+	STRATEGY_LOOP_STUB(1, 0) { t = MAX ? max(t, IMEM(0, 0)) : min(t, IMEM(0, 0)); }
+	STRATEGY_POST_STUB(0, 1) { OMEM(0, 0) = t; }
 };
 
 constexpr uint64_t kOnePtr = 0x1111111111111111ull;
@@ -185,6 +225,10 @@ extern "C" umi_status umi_launch(const umi_plan* plan, int32_t op, const void* c
 		case UMI_STRATEGY_RUNNING_SUM_I32: return launch_as<RunningSumI32>(*plan, in, pad, out, user_const, uc_bytes, st);
 		case UMI_STRATEGY_DOT_I32: return launch_as<DotT<int>>(*plan, in, pad, out, user_const, uc_bytes, st);
 		case UMI_STRATEGY_DOT_F32: return launch_as<DotT<float>>(*plan, in, pad, out, user_const, uc_bytes, st);
+		case UMI_STRATEGY_CENSUS_I32: return launch_as<CensusI32>(*plan, in, pad, out, user_const, uc_bytes, st);
+		case UMI_STRATEGY_WEIGHTED_SUM_F32: return launch_as<WeightedSumF32>(*plan, in, pad, out, user_const, uc_bytes, st);
+		case UMI_STRATEGY_MAX_I32: return launch_as<ExtremumI32<true>>(*plan, in, pad, out, user_const, uc_bytes, st);
+		case UMI_STRATEGY_MIN_I32: return launch_as<ExtremumI32<false>>(*plan, in, pad, out, user_const, uc_bytes, st);
 		default: return umi::fail(UMI_ERR_UNSUPPORTED, "umi_launch: unknown strategy %d", op);
 	}
 }
