@@ -45,7 +45,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # scaled to the configured batch.
 NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
                "fprop_n32": 67321088 + 206541312, "learned_me_4k": None, "coarse_me_4k": None,
-               "video_y4m_1080p": None}
+               "video_y4m_1080p": None, "apps_1080p": None}
 NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 + 3253943000) / 12896910}
 
 
@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096",
-                                           "fprop_n32", "learned_me_4k", "coarse_me_4k", "video_y4m_1080p"],
+                                           "fprop_n32", "learned_me_4k", "coarse_me_4k", "video_y4m_1080p",
+                                           "apps_1080p"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
@@ -64,7 +65,7 @@ def parse():
     if a.steps is None:
         a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
                    "gemm_4096": 3000, "fprop_n32": 3000, "learned_me_4k": 200, "coarse_me_4k": 2000,
-                   "video_y4m_1080p": 2000}[a.workload]
+                   "video_y4m_1080p": 2000, "apps_1080p": 500}[a.workload]
     return a
 
 
@@ -912,9 +913,152 @@ class VideoY4M:
         return nblocks / self.nblk
 
 
+class Apps1080p:
+    """Four window operators of the UMI family on the generic operator
+    (umi_gb300/apps.py, umi_launch with built-in strategies) over one
+    1920x1080 frame per step: census 5x5 (int32), grey-level dilation 3x3
+    (int32), box sums 15x15 via the integral image (uint8 -> int32) and a
+    separable Gaussian, sigma 2, 13 taps (float32, two passes)."""
+    name = "apps_1080p"
+    metric = "UMI window apps Mpx/s (1080p: census 5x5 + dilate 3x3 + box 15x15 via iimg + gaussian sigma 2)"
+    unit = "Mpx/s"
+    dtype = "i32 / u8 / f32"
+    H, W = 1080, 1920
+    # bytes moved per pixel as implemented (read + write of every launch)
+    BYTES = {"census": 8, "dilate": 8, "box_sum": 5 + 8 + 8, "gaussian": 16}
+
+    def __init__(self, seed=21, **_):
+        self.seed = seed
+        self.px = self.H * self.W
+
+    def config(self):
+        return {"workload": self.name, "frame": f"{self.W}x{self.H}", "ops": "census r2, dilate r1, box r7 "
+                "(integral image + 4 corner reads), gaussian sigma 2 (13 taps, two passes)",
+                "bytes_per_px": self.BYTES, "l2": "4 frame sets rotated (> L2)"}
+
+    def units_per_step(self):
+        return self.px / 1e6
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        from umi_gb300 import apps
+        self.U, self.apps = U, apps
+        self.n_rot = 4
+        g = np.random.default_rng(self.seed)
+        frames = [g.integers(0, 256, (self.H, self.W), dtype=np.uint8) for _ in range(self.n_rot)]
+        self.h_u8 = [torch.from_numpy(f).pin_memory() for f in frames]
+        self.u8 = [t.to(dev) for t in self.h_u8]
+        self.i32 = [t.to(torch.int32) for t in self.u8]
+        self.f32 = [t.to(torch.float32) * (1.0 / 255.0) for t in self.u8]
+        mk = lambda dt: [torch.empty((self.H, self.W), dtype=dt, device=dev) for _ in range(self.n_rot)]
+        self.o_census, self.o_dil, self.o_box, self.ii = mk(torch.int32), mk(torch.int32), mk(torch.int32), mk(torch.int32)
+        self.o_g, self.tmp = mk(torch.float32), mk(torch.float32)
+        self.J = [torch.zeros((self.H + 1, self.W + 1), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
+        self.ws = torch.empty(U.iimg_workspace_bytes(self.H, self.W), dtype=torch.uint8, device=dev)
+        self.h_out = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
+        # census + dilate + (iimg 3 kernels + J copy + box) + gaussian 2
+        self.launches_per_step = 1 + 1 + 5 + 2
+        for k in range(self.n_rot):  # constants made before any graph capture
+            self.step(k)
+
+    def _op(self, name, k):
+        a = self.apps
+        if name == "census":
+            a.census(self.i32[k], 2, out=self.o_census[k])
+        elif name == "dilate":
+            a.dilate(self.i32[k], 1, out=self.o_dil[k])
+        elif name == "box_sum":
+            a.box_sum(self.u8[k], 7, out=self.o_box[k], J=self.J[k], ii=self.ii[k], workspace=self.ws)
+        else:
+            a.gaussian(self.f32[k], 2.0, out=self.o_g[k], tmp=self.tmp[k])
+
+    def step(self, i):
+        k = i % self.n_rot
+        for name in ("census", "dilate", "box_sum", "gaussian"):
+            self._op(name, k)
+
+    def h2d(self, k):
+        self.u8[k].copy_(self.h_u8[k], non_blocking=True)
+        self.i32[k].copy_(self.u8[k])
+        self.f32[k].copy_(self.u8[k])
+        self.f32[k].mul_(1.0 / 255.0)
+
+    def d2h(self, k):
+        self.h_out.copy_(self.o_box[k], non_blocking=True)
+
+    def e2e_bytes(self):
+        return self.px, 4 * self.px
+
+    def check(self):
+        """Sampled rows against numpy restatements of the four definitions."""
+        import torch
+        k = 0
+        self.step(k)
+        torch.cuda.synchronize()
+        x = self.u8[k].cpu().numpy()
+        rows = [0, 1, 539, 1078, 1079]
+        errs = {}
+        xi = x.astype(np.int64)
+        p2 = np.pad(xi, 2, mode="edge")
+        cen = np.zeros((len(rows), self.W), np.uint64)
+        for dy in range(5):
+            for dx in range(5):
+                nb = np.stack([p2[r + dy, dx:dx + self.W] for r in rows])
+                cen = (cen << np.uint64(1)) | (nb < xi[rows]).astype(np.uint64)
+        errs["census_rows_exact"] = bool(np.array_equal(self.o_census[k].cpu().numpy()[rows].view(np.uint32),
+                                                       cen.astype(np.uint32)))
+        p1 = np.pad(xi, 1, mode="edge")
+        dil = np.max([[p1[r + dy, dx:dx + self.W] for r in rows] for dy in range(3) for dx in range(3)], axis=0)
+        errs["dilate_rows_exact"] = bool(np.array_equal(self.o_dil[k].cpu().numpy()[rows], dil))
+        c = np.pad(np.pad(xi, 7).cumsum(0).cumsum(1), ((1, 0), (1, 0)))
+        box = np.stack([c[r + 15, 15:15 + self.W] - c[r, 15:15 + self.W] - c[r + 15, :self.W] + c[r, :self.W]
+                        for r in rows])
+        errs["box_rows_exact"] = bool(np.array_equal(self.o_box[k].cpu().numpy()[rows], box))
+        kern = self.apps.gaussian_kernel(2.0).astype(np.float64)
+        pf = np.pad(x.astype(np.float64) / 255.0, 6, mode="edge")
+        hz = sum(kern[i] * pf[:, i:i + self.W] for i in range(13))
+        gw = np.stack([sum(kern[i] * hz[r + i] for i in range(13)) for r in rows])
+        got = self.o_g[k].cpu().numpy()[rows]
+        errs["gaussian_max_rel_err"] = float(np.max(np.abs(got - gw) / np.maximum(np.abs(gw), 1e-3)))
+        return errs
+
+    def kernels(self, dev, peaks, n=20):
+        fns = {name: (lambda nm: (lambda i: self._op(nm, i % self.n_rot)))(name)
+               for name in ("census", "dilate", "box_sum", "gaussian")}
+        return {name: time_launches(fn, self.n_rot, n) for name, fn in fns.items()}, None, None
+
+    def cpu_setup(self):
+        from umi_gb300 import apps
+        self.apps_np = apps
+        self.cx = np.random.default_rng(self.seed).integers(0, 256, (self.H, self.W), dtype=np.uint8)
+        self.row = 0
+
+    def cpu_step(self, nrows, threads):
+        """The four operators on `nrows` rows of the frame in numpy (FP64 Gaussian)."""
+        r0 = self.row % (self.H - nrows)
+        self.row += nrows
+        x = self.cx[max(r0 - 7, 0):r0 + nrows + 7].astype(np.int64)
+        p2 = np.pad(x, 2, mode="edge")
+        h, w = x.shape
+        bits = np.zeros((h, w), np.uint64)
+        for dy in range(5):
+            for dx in range(5):
+                bits = (bits << np.uint64(1)) | (p2[dy:dy + h, dx:dx + w] < x).astype(np.uint64)
+        p1 = np.pad(x, 1, mode="edge")
+        np.max([p1[dy:dy + h, dx:dx + w] for dy in range(3) for dx in range(3)], axis=0)
+        c = np.pad(np.pad(x, 7).cumsum(0).cumsum(1), ((1, 0), (1, 0)))
+        _ = c[15:15 + h, 15:15 + w] - c[:h, 15:15 + w] - c[15:15 + h, :w] + c[:h, :w]
+        kern = self.apps_np.gaussian_kernel(2.0).astype(np.float64)
+        pf = np.pad(x / 255.0, 6, mode="edge")
+        hz = sum(kern[i] * pf[:, i:i + w] for i in range(13))
+        _ = sum(kern[i] * hz[i:i + h] for i in range(13))
+        return nrows * self.W / 1e6
+
+
 WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm,
              "fprop_n32": Fprop, "learned_me_4k": LearnedMe, "coarse_me_4k": CoarseMe4k,
-             "video_y4m_1080p": VideoY4M}
+             "video_y4m_1080p": VideoY4M, "apps_1080p": Apps1080p}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -1178,6 +1322,16 @@ def run_ours(args, wl, dist):
                 "traffic": NCU_TRAFFIC[wl.name],
                 "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
                 "work_per_launch": absdiff, "ms_per_launch": kms[roof_k]}
+    elif isinstance(wl, Apps1080p):
+        for name, kt in kms.items():
+            b = wl.BYTES[name] * wl.px
+            kernels[name] = {"ms_per_launch": kt, "achieved": b / (kt * 1e-3) / 1e9, "unit": "GB/s",
+                             "frac": b / (kt * 1e-3) / 1e9 / pk["hbm_gbs"], "bytes_per_launch": b}
+        dom = max(kms, key=kms.get)
+        cg = copy_gbs(dev, wl.BYTES[dom] * wl.px)
+        roof = dict(kernels[dom], bound="hbm", kernel=f"generic_kernel ({dom})", peak=pk["hbm_gbs"], traffic=None,
+                    peak_source=pk["source"], size_matched_copy_gbs=cg,
+                    frac_of_size_matched_copy=kernels[dom]["achieved"] / cg)
     elif isinstance(wl, VideoY4M):
         sad_peak = probe_sad4_peak(dev)
         for name, kt in kms.items():
@@ -1233,7 +1387,9 @@ def cpu_baseline(wl, sample_s=10.0):
     """The reference's CPU loop (oracle restatement) on a bounded sample, all host threads."""
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    if isinstance(wl, VideoY4M):
+    if isinstance(wl, Apps1080p):
+        chunk, what = 16, "rows of the 1080p frame through numpy restatements of census 5x5, dilation 3x3, box 15x15 (integral image) and the FP64 separable Gaussian (the reference has none of these: its operator has no CPU path)"
+    elif isinstance(wl, VideoY4M):
         chunk, what = 8, "random blocks of a 1080p pair of the video, +-64 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin (the reference has no I/O and no proposal), units = pairs"
     elif isinstance(wl, LearnedMe):
         chunk, what = 8, "random blocks of a 4K pair, +-64 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin (the reference has no learned path)"

@@ -18,7 +18,10 @@
 //  * inputs are read through the read-only data path with the same
 //    clamp/pad rule instead of a 64-thread shared-memory fill; ZeroStrideOpt
 //    is accepted and has no effect on results (the cache deduplicates the
-//    loads it would have saved).
+//    loads it would have saved);
+//  * a Loop input whose whole accumulation window stays inside its extent at
+//    a point (no clamp, no padding) is addressed linearly: base + a . stride,
+//    precomputed per point; points near the edges take the clamped map.
 //
 // Checked builds: compiled with -DUMI_CHECKED, every output write whose
 // physical coordinate falls outside [0, size) of its dimension (size 0 counts
@@ -93,6 +96,56 @@ __device__ __forceinline__ void gather(const umi_plan& plan, const P& ptrs, cons
 	}
 }
 
+// Fast addressing of a Loop input at one point: when every accumulation step
+// of the point keeps every physical coordinate inside [0, size-1] (no clamp,
+// no padding), the element of step a sits at base + sum_d a[d] * astride[d]:
+// the same element the clamped map reads, without recomputing it per step.
+struct LinearAddr {
+	int64_t base;
+	bool inside;
+};
+
+__device__ __forceinline__ LinearAddr linear_addr(const umi_mem_plan& m, const umi_plan& plan, const int (&p)[4]) {
+	LinearAddr f{0, true};
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		int64_t c = m.base[k];
+#pragma unroll
+		for (int d = 0; d < 4; ++d) c += (int64_t)m.pcoef[k][d] * p[d];
+		int64_t lo = c, hi = c;
+#pragma unroll
+		for (int d = 0; d < 4; ++d) {
+			const int64_t span = (int64_t)m.acoef[k][d] * (plan.atotal[d] > 0 ? plan.atotal[d] - 1 : 0);
+			if (span < 0) lo += span;
+			else hi += span;
+		}
+		f.inside &= lo >= 0 && hi <= (int64_t)m.size[k] - 1;
+		f.base += c * m.rowstride[k];
+	}
+	return f;
+}
+
+__device__ __forceinline__ int64_t a_stride(const umi_mem_plan& m, int d) {
+	int64_t s = 0;
+#pragma unroll
+	for (int k = 0; k < 4; ++k) s += (int64_t)m.acoef[k][d] * m.rowstride[k];
+	return s;
+}
+
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+__device__ __forceinline__ void gather_linear(const P& ptrs, const int64_t (&base)[SafeArrayLength(N)],
+                                              const int64_t (&astr)[SafeArrayLength(N)][4], const int (&a)[4],
+                                              Arr& in) {
+#pragma unroll
+	for (int i = 0; i < N; ++i) {
+		const int mem = OFS + i;
+		const int64_t addr = base[i] + a[0] * astr[i][0] + a[1] * astr[i][1] + a[2] * astr[i][2] + a[3] * astr[i][3];
+#pragma unroll
+		for (int j = 0; j < MAX_PTR; ++j)
+			if (j < (int)Slice(PtrNum, 4, mem)) in[i * MAX_PTR + j] = ptrs.in[mem * MAX_PTR + j][addr];
+	}
+}
+
 template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
 __device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
                                         bool with_a, const Arr& out) {
@@ -119,8 +172,8 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, con
 // the Loop over A in blocked row-major order (src/UMI_gpu.h:287-346), then
 // Post; points outside P are skipped (the reference runs them and drops the
 // writes).
-template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType>
-__global__ void __launch_bounds__(1024) generic_kernel(const umi_plan plan, const CType uc,
+template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType, int MAXT = 1024>
+__global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(const umi_plan plan, const CType uc,
                                                         const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs) {
 	constexpr int E0 = (int)Slice(Expand, 4, 3), E1 = (int)Slice(Expand, 4, 2);
 	constexpr int E2 = (int)Slice(Expand, 4, 1), E3 = (int)Slice(Expand, 4, 0);
@@ -168,36 +221,56 @@ __global__ void __launch_bounds__(1024) generic_kernel(const umi_plan plan, cons
 			ctx[e].Pre(uc, in, out);
 			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, ptrs, pts[e], zero, false, out);
 		}
-		// Loop: accumulation blocks row-major, steps row-major inside a block.
+		// Loop inputs: linear addressing for points whose whole window is inside.
+		constexpr int NLI = SafeArrayLength(Umi::N_LOOP_IN);
+		int64_t lbase[ES][NLI];
+		int64_t astr[NLI][4];
+		bool fast[ES];
+#pragma unroll
+		for (int i = 0; i < Umi::N_LOOP_IN; ++i)
+#pragma unroll
+			for (int d = 0; d < 4; ++d) astr[i][d] = a_stride(plan.mem[LOOP_I + i], d);
+#pragma unroll
+		for (int e = 0; e < ES; ++e) {
+			bool f = Umi::N_LOOP_IN > 0;
+#pragma unroll
+			for (int i = 0; i < Umi::N_LOOP_IN; ++i) {
+				const LinearAddr la = linear_addr(plan.mem[LOOP_I + i], plan, pts[e]);
+				lbase[e][i] = la.base;
+				f &= la.inside;
+			}
+			fast[e] = f;
+		}
+		// Loop: accumulation blocks row-major, steps row-major inside a block
+		// (dimension 3 fastest), as four nested loops clipped to the A extent.
 		if (plan.n_ablock > 0) {
 			int ab[4] = {0, 0, 0, 0};
 			for (int bi = 0; bi < plan.n_ablock; ++bi) {
-				int as[4] = {0, 0, 0, 0};
-				for (int si = 0; si < plan.ablock_size; ++si) {
-					int a[4];
-					bool ok = true;
+				int a0[4], lim[4];
 #pragma unroll
-					for (int d = 0; d < 4; ++d) {
-						a[d] = ab[d] * plan.ablock[d] + as[d];
-						ok &= a[d] < plan.atotal[d];
-					}
-					if (ok) {
-#pragma unroll
-						for (int e = 0; e < ES; ++e) {
-							if (!valid[e]) continue;
-							simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
-							simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
-							gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
-							ctx[e].Loop(uc, in, out);
-							scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, ptrs, pts[e], a, true, out);
-						}
-					}
-#pragma unroll
-					for (int d = 3; d >= 0; --d) {
-						if (++as[d] < plan.ablock[d]) break;
-						as[d] = 0;
-					}
+				for (int d = 0; d < 4; ++d) {
+					a0[d] = ab[d] * plan.ablock[d];
+					lim[d] = min(plan.ablock[d], plan.atotal[d] - a0[d]);
 				}
+				for (int s0 = 0; s0 < lim[0]; ++s0)
+					for (int s1 = 0; s1 < lim[1]; ++s1)
+						for (int s2 = 0; s2 < lim[2]; ++s2)
+							for (int s3 = 0; s3 < lim[3]; ++s3) {
+								const int a[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3] + s3};
+#pragma unroll
+								for (int e = 0; e < ES; ++e) {
+									if (!valid[e]) continue;
+									simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
+									simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
+									if (fast[e])
+										gather_linear<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(ptrs, lbase[e], astr, a,
+										                                                           in);
+									else
+										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+									ctx[e].Loop(uc, in, out);
+									scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, ptrs, pts[e], a, true, out);
+								}
+							}
 #pragma unroll
 				for (int d = 3; d >= 0; --d) {
 					if (++ab[d] < plan.agrid[d]) break;
@@ -305,7 +378,11 @@ umi_status Execute(
 				return UMI_ERR_INVALID_ARG;
 	if (plan.n_cta == 0) return UMI_OK;
 	const unsigned grid = (unsigned)(plan.n_cta < 0x7fffffff ? plan.n_cta : 0x7fffffff);
-	gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
+	// plans of at most 256 threads (the common case) get the variant with a larger register budget
+	if (plan.n_threads <= 256)
+		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType, 256><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
+	else
+		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
 	return cudaGetLastError() == cudaSuccess ? UMI_OK : UMI_ERR_CUDA;
 }
 

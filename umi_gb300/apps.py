@@ -29,6 +29,17 @@ import umi_gb300 as U
 PAD, WRAP = 0, 1
 
 
+_CONST = {}  # small constant tensors (weights) per (device, key): made once, so calls can be graph-captured
+
+
+def _const(dev, key, make):
+    import torch
+    k = (str(dev), key)
+    if k not in _CONST:
+        _CONST[k] = torch.from_numpy(np.ascontiguousarray(make())).to(dev)
+    return _CONST[k]
+
+
 def _p(h, w):
     return [(1, 1, 1, 1), (1, 1, 1, 1), (h, 16, 4, 1), (w, 16, 8, 1)]
 
@@ -94,7 +105,7 @@ def box_sum(img_u8, radius: int, out=None, J=None, ii=None, workspace=None, stre
     if J is None:
         J = torch.zeros((h + 1, w + 1), dtype=torch.int32, device=dev)  # J[y][x] = sum of img[:y, :x]
     J[1:, 1:] = U.iimg_u8_i32(img_u8, out=ii, workspace=workspace, stream=stream)
-    wts = torch.tensor([[1, -1], [-1, 1]], dtype=torch.int32, device=dev)
+    wts = _const(dev, "box", lambda: np.array([[1, -1], [-1, 1]], np.int32))
     if out is None:
         out = torch.empty((h, w), dtype=torch.int32, device=dev)
     # corner (a_y, a_x) of point (y, x): J[clamp(y - r + a_y k)][clamp(x - r + a_x k)]
@@ -124,7 +135,7 @@ def gaussian(img, sigma: float, radius: int | None = None, out=None, tmp=None, s
     k = kern.size
     r = k // 2
     dev = img.device
-    wt = torch.from_numpy(kern).to(dev)
+    wt = _const(dev, ("gauss", float(sigma), k), lambda: kern)
     if tmp is None:
         tmp = torch.empty((h, w), dtype=torch.float32, device=dev)
     if out is None:

@@ -190,7 +190,10 @@ umi_status launch_as(const umi_plan& plan0, const void* const* in, const void* p
 	plan.n_cta = n_cta;
 	if (n_cta == 0) return umi::ok();
 	const unsigned grid = (unsigned)(n_cta < 0x7fffffff ? n_cta : 0x7fffffff);
-	gpu_detail::generic_kernel<Umi, kOnePtr, 0x1111, E, C><<<grid, plan.n_threads, 0, st>>>(plan, c, ptrs);
+	if (plan.n_threads <= 256)
+		gpu_detail::generic_kernel<Umi, kOnePtr, 0x1111, E, C, 256><<<grid, plan.n_threads, 0, st>>>(plan, c, ptrs);
+	else
+		gpu_detail::generic_kernel<Umi, kOnePtr, 0x1111, E, C><<<grid, plan.n_threads, 0, st>>>(plan, c, ptrs);
 	return umi::launch_status("generic_kernel");
 }
 
