@@ -133,20 +133,6 @@ __device__ __forceinline__ int64_t a_stride(const umi_mem_plan& m, int d) {
 }
 
 template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
-__device__ __forceinline__ void gather_linear(const P& ptrs, const int64_t (&base)[SafeArrayLength(N)],
-                                              const int64_t (&astr)[SafeArrayLength(N)][4], const int (&a)[4],
-                                              Arr& in) {
-#pragma unroll
-	for (int i = 0; i < N; ++i) {
-		const int mem = OFS + i;
-		const int64_t addr = base[i] + a[0] * astr[i][0] + a[1] * astr[i][1] + a[2] * astr[i][2] + a[3] * astr[i][3];
-#pragma unroll
-		for (int j = 0; j < MAX_PTR; ++j)
-			if (j < (int)Slice(PtrNum, 4, mem)) in[i * MAX_PTR + j] = ptrs.in[mem * MAX_PTR + j][addr];
-	}
-}
-
-template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
 __device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
                                         bool with_a, const Arr& out) {
 #pragma unroll
@@ -184,11 +170,22 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 	for (int64_t cta = blockIdx.x; cta < plan.n_cta; cta += gridDim.x) {
 		int g[4], t[4];
 		{
-			int64_t r = cta;
+			if (cta <= 0x7fffffff) {  // 32-bit index arithmetic (every CTA of plans below 2^31 CTAs)
+				uint32_t r = (uint32_t)cta;
 #pragma unroll
-			for (int d = 3; d >= 0; --d) {
-				g[d] = (int)(r % plan.grid[d]);
-				r /= plan.grid[d];
+				for (int d = 3; d >= 0; --d) {
+					const uint32_t gd = (uint32_t)plan.grid[d];
+					const uint32_t q = r / gd;
+					g[d] = (int)(r - q * gd);
+					r = q;
+				}
+			} else {
+				int64_t r = cta;
+#pragma unroll
+				for (int d = 3; d >= 0; --d) {
+					g[d] = (int)(r % plan.grid[d]);
+					r /= plan.grid[d];
+				}
 			}
 			int s = threadIdx.x;
 #pragma unroll
@@ -254,7 +251,18 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 				}
 				for (int s0 = 0; s0 < lim[0]; ++s0)
 					for (int s1 = 0; s1 < lim[1]; ++s1)
-						for (int s2 = 0; s2 < lim[2]; ++s2)
+						for (int s2 = 0; s2 < lim[2]; ++s2) {
+							// linear addresses of the row of steps s3 = 0.. (fast points), then one stride per step
+							int64_t row[ES][NLI];
+							{
+								const int ar[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3]};
+#pragma unroll
+								for (int e = 0; e < ES; ++e)
+#pragma unroll
+									for (int i = 0; i < NLI; ++i)
+										row[e][i] = lbase[e][i] + ar[0] * astr[i][0] + ar[1] * astr[i][1] +
+										            ar[2] * astr[i][2] + ar[3] * astr[i][3];
+							}
 							for (int s3 = 0; s3 < lim[3]; ++s3) {
 								const int a[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3] + s3};
 #pragma unroll
@@ -262,15 +270,24 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 									if (!valid[e]) continue;
 									simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
 									simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
-									if (fast[e])
-										gather_linear<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(ptrs, lbase[e], astr, a,
-										                                                           in);
-									else
+									if (fast[e]) {
+#pragma unroll
+										for (int i = 0; i < Umi::N_LOOP_IN; ++i) {
+											const int mem = LOOP_I + i;
+#pragma unroll
+											for (int j = 0; j < MAX_PTR; ++j)
+												if (j < (int)Slice(PtrNum, 4, mem))
+													in[i * MAX_PTR + j] = ptrs.in[mem * MAX_PTR + j][row[e][i]];
+											row[e][i] += astr[i][3];
+										}
+									} else {
 										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+									}
 									ctx[e].Loop(uc, in, out);
 									scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, ptrs, pts[e], a, true, out);
 								}
 							}
+						}
 #pragma unroll
 				for (int d = 3; d >= 0; --d) {
 					if (++ab[d] < plan.agrid[d]) break;
