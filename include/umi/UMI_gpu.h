@@ -96,55 +96,95 @@ __device__ __forceinline__ void gather(const umi_plan& plan, const P& ptrs, cons
 	}
 }
 
+// Linear forms of the address maps, computed once on the host per launch:
+// without clamping, memory m's element for point p and step a is
+//   lin[m] + sum_d p[d] * pstr[m][d] + sum_d a[d] * astr[m][d],
+// and its coordinate k spans [c_k + alo[m][k], c_k + ahi[m][k]] over the
+// accumulation range (c_k its coordinate at a = 0).  fit32: every
+// coordinate of every point and step fits comfortably in 32 bits.
+struct LinearMaps {
+	int64_t lin[UMI_MAX_MEMS];
+	int64_t pstr[UMI_MAX_MEMS][4];
+	int64_t astr[UMI_MAX_MEMS][4];
+	int64_t alo[UMI_MAX_MEMS][4];
+	int64_t ahi[UMI_MAX_MEMS][4];
+	int32_t fit32;
+};
+
+inline LinearMaps linear_maps(const umi_plan& plan) {
+	LinearMaps L;
+	std::memset(&L, 0, sizeof(L));
+	bool fit = true;
+	for (int m = 0; m < plan.n_in + plan.n_out && m < UMI_MAX_MEMS; ++m) {
+		const umi_mem_plan& mp = plan.mem[m];
+		for (int k = 0; k < 4; ++k) {
+			L.lin[m] += (int64_t)mp.base[k] * mp.rowstride[k];
+			int64_t bound = mp.base[k] < 0 ? -(int64_t)mp.base[k] : mp.base[k];
+			for (int d = 0; d < 4; ++d) {
+				L.pstr[m][d] += (int64_t)mp.pcoef[k][d] * mp.rowstride[k];
+				L.astr[m][d] += (int64_t)mp.acoef[k][d] * mp.rowstride[k];
+				const int64_t span = (int64_t)mp.acoef[k][d] * (plan.atotal[d] > 0 ? plan.atotal[d] - 1 : 0);
+				if (span < 0) L.alo[m][k] += span;
+				else L.ahi[m][k] += span;
+				const int64_t pc = mp.pcoef[k][d] < 0 ? -(int64_t)mp.pcoef[k][d] : mp.pcoef[k][d];
+				bound += pc * (plan.ptotal[d] > 0 ? plan.ptotal[d] : 0);
+			}
+			bound += L.ahi[m][k] - L.alo[m][k];
+			fit &= bound < ((int64_t)1 << 30);
+		}
+	}
+	L.fit32 = fit;
+	return L;
+}
+
 // Fast addressing of a Loop input at one point: when every accumulation step
 // of the point keeps every physical coordinate inside [0, size-1] (no clamp,
-// no padding), the element of step a sits at base + sum_d a[d] * astride[d]:
+// no padding), the element of step a sits at base + sum_d a[d] * astr[d]:
 // the same element the clamped map reads, without recomputing it per step.
 struct LinearAddr {
 	int64_t base;
 	bool inside;
 };
 
-__device__ __forceinline__ LinearAddr linear_addr(const umi_mem_plan& m, const umi_plan& plan, const int (&p)[4]) {
-	LinearAddr f{0, true};
+template <typename I>
+__device__ __forceinline__ bool window_inside(const umi_mem_plan& m, const LinearMaps& L, int mi, const int (&p)[4]) {
+	bool in = true;
 #pragma unroll
 	for (int k = 0; k < 4; ++k) {
-		int64_t c = m.base[k];
+		I c = (I)m.base[k];
 #pragma unroll
-		for (int d = 0; d < 4; ++d) c += (int64_t)m.pcoef[k][d] * p[d];
-		int64_t lo = c, hi = c;
-#pragma unroll
-		for (int d = 0; d < 4; ++d) {
-			const int64_t span = (int64_t)m.acoef[k][d] * (plan.atotal[d] > 0 ? plan.atotal[d] - 1 : 0);
-			if (span < 0) lo += span;
-			else hi += span;
-		}
-		f.inside &= lo >= 0 && hi <= (int64_t)m.size[k] - 1;
-		f.base += c * m.rowstride[k];
+		for (int d = 0; d < 4; ++d) c += (I)m.pcoef[k][d] * (I)p[d];
+		in &= c + (I)L.alo[mi][k] >= 0 && c + (I)L.ahi[mi][k] <= (I)m.size[k] - 1;
 	}
+	return in;
+}
+
+__device__ __forceinline__ LinearAddr linear_addr(const umi_mem_plan& m, const LinearMaps& L, int mi, const int (&p)[4]) {
+	LinearAddr f;
+	f.base = L.lin[mi] + p[0] * L.pstr[mi][0] + p[1] * L.pstr[mi][1] + p[2] * L.pstr[mi][2] + p[3] * L.pstr[mi][3];
+	f.inside = L.fit32 ? window_inside<int32_t>(m, L, mi, p) : window_inside<int64_t>(m, L, mi, p);
 	return f;
 }
 
-__device__ __forceinline__ int64_t a_stride(const umi_mem_plan& m, int d) {
-	int64_t s = 0;
-#pragma unroll
-	for (int k = 0; k < 4; ++k) s += (int64_t)m.acoef[k][d] * m.rowstride[k];
-	return s;
-}
-
 template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
-__device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
-                                        bool with_a, const Arr& out) {
+__device__ __forceinline__ void scatter(const umi_plan& plan, const LinearMaps& lm, const P& ptrs, const int (&p)[4],
+                                        const int (&a)[4], bool with_a, const Arr& out) {
 #pragma unroll
 	for (int i = 0; i < N; ++i) {
 		const int mem = OFS + i;
+#ifdef UMI_CHECKED
 		bool outside;
 		const int64_t addr = address<false>(plan.mem[Umi::TOTAL_IN + mem], p, a, with_a, outside);
-#ifdef UMI_CHECKED
 		if (outside) {
 			atomicOr(&checked_flags_word, 1u);
 			continue;
 		}
+#else
+		// outputs are not clamped: the linear form is the map
+		const int mi = Umi::TOTAL_IN + mem;
+		int64_t addr = lm.lin[mi] + p[0] * lm.pstr[mi][0] + p[1] * lm.pstr[mi][1] + p[2] * lm.pstr[mi][2] +
+		               p[3] * lm.pstr[mi][3];
+		if (with_a) addr += a[0] * lm.astr[mi][0] + a[1] * lm.astr[mi][1] + a[2] * lm.astr[mi][2] + a[3] * lm.astr[mi][3];
 #endif
 #pragma unroll
 		for (int j = 0; j < MAX_PTR; ++j) {
@@ -160,7 +200,8 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const P& ptrs, con
 // writes).
 template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType, int MAXT = 1024>
 __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(const umi_plan plan, const CType uc,
-                                                        const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs) {
+                                                        const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs,
+                                                        const LinearMaps lm) {
 	constexpr int E0 = (int)Slice(Expand, 4, 3), E1 = (int)Slice(Expand, 4, 2);
 	constexpr int E2 = (int)Slice(Expand, 4, 1), E3 = (int)Slice(Expand, 4, 0);
 	constexpr int ES = E0 * E1 * E2 * E3;
@@ -216,7 +257,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			simple_array<EType, Umi::N_PRE_OUT * MAX_PTR> out;
 			gather<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType>(plan, ptrs, pts[e], zero, false, in);
 			ctx[e].Pre(uc, in, out);
-			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, ptrs, pts[e], zero, false, out);
+			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
 		// Loop inputs: linear addressing for points whose whole window is inside.
 		constexpr int NLI = SafeArrayLength(Umi::N_LOOP_IN);
@@ -226,13 +267,13 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 #pragma unroll
 		for (int i = 0; i < Umi::N_LOOP_IN; ++i)
 #pragma unroll
-			for (int d = 0; d < 4; ++d) astr[i][d] = a_stride(plan.mem[LOOP_I + i], d);
+			for (int d = 0; d < 4; ++d) astr[i][d] = lm.astr[LOOP_I + i][d];
 #pragma unroll
 		for (int e = 0; e < ES; ++e) {
 			bool f = Umi::N_LOOP_IN > 0;
 #pragma unroll
 			for (int i = 0; i < Umi::N_LOOP_IN; ++i) {
-				const LinearAddr la = linear_addr(plan.mem[LOOP_I + i], plan, pts[e]);
+				const LinearAddr la = linear_addr(plan.mem[LOOP_I + i], lm, LOOP_I + i, pts[e]);
 				lbase[e][i] = la.base;
 				f &= la.inside;
 			}
@@ -284,7 +325,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
 									}
 									ctx[e].Loop(uc, in, out);
-									scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, ptrs, pts[e], a, true, out);
+									scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
 								}
 							}
 						}
@@ -303,7 +344,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			simple_array<EType, Umi::N_POST_OUT * MAX_PTR> out;
 			gather<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType>(plan, ptrs, pts[e], zero, false, in);
 			ctx[e].Post(uc, in, out);
-			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType>(plan, ptrs, pts[e], zero, false, out);
+			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
 	}
 }
@@ -397,9 +438,11 @@ umi_status Execute(
 	const unsigned grid = (unsigned)(plan.n_cta < 0x7fffffff ? plan.n_cta : 0x7fffffff);
 	// plans of at most 256 threads (the common case) get the variant with a larger register budget
 	if (plan.n_threads <= 256)
-		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType, 256><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
+		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType, 256><<<grid, plan.n_threads, 0, stream>>>(
+			plan, c, ptrs, gpu_detail::linear_maps(plan));
 	else
-		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs);
+		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(
+			plan, c, ptrs, gpu_detail::linear_maps(plan));
 	return cudaGetLastError() == cudaSuccess ? UMI_OK : UMI_ERR_CUDA;
 }
 
