@@ -109,6 +109,7 @@ struct LinearMaps {
 	int64_t alo[UMI_MAX_MEMS][4];
 	int64_t ahi[UMI_MAX_MEMS][4];
 	int32_t fit32;
+	int32_t bshift[4];  // log2 of the CTA block along each P dimension, -1 if not a power of two
 };
 
 inline LinearMaps linear_maps(const umi_plan& plan) {
@@ -134,7 +135,46 @@ inline LinearMaps linear_maps(const umi_plan& plan) {
 		}
 	}
 	L.fit32 = fit;
+	for (int d = 0; d < 4; ++d) {
+		const int b = plan.block[d];
+		L.bshift[d] = -1;
+		for (int sh = 0; sh < 31; ++sh)
+			if (b == (1 << sh)) L.bshift[d] = sh;
+	}
 	return L;
+}
+
+// A Pre / Post input at point p: the linear form when every coordinate is
+// inside the extent (no clamp, no padding), else the clamped map.
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+__device__ __forceinline__ void gather_point(const umi_plan& plan, const LinearMaps& lm, const P& ptrs,
+                                             const int (&p)[4], Arr& in) {
+#pragma unroll
+	for (int i = 0; i < N; ++i) {
+		const int mem = OFS + i;
+		const umi_mem_plan& m = plan.mem[mem];
+		bool inside = true;
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			int64_t c = m.base[k];
+#pragma unroll
+			for (int d = 0; d < 4; ++d) c += (int64_t)m.pcoef[k][d] * p[d];
+			inside &= c >= 0 && c <= (int64_t)m.size[k] - 1;
+		}
+		int64_t addr;
+		bool outside = false;
+		if (inside) {
+			addr = lm.lin[mem] + p[0] * lm.pstr[mem][0] + p[1] * lm.pstr[mem][1] + p[2] * lm.pstr[mem][2] +
+			       p[3] * lm.pstr[mem][3];
+		} else {
+			const int zero[4] = {0, 0, 0, 0};
+			addr = address<true>(m, p, zero, false, outside);
+		}
+#pragma unroll
+		for (int j = 0; j < MAX_PTR; ++j)
+			if (j < (int)Slice(PtrNum, 4, mem))
+				in[i * MAX_PTR + j] = outside ? ptrs.pad[mem * MAX_PTR + j] : ptrs.in[mem * MAX_PTR + j][addr];
+	}
 }
 
 // Fast addressing of a Loop input at one point: when every accumulation step
@@ -229,10 +269,16 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 				}
 			}
 			int s = threadIdx.x;
+			const bool pow2 = lm.bshift[0] >= 0 && lm.bshift[1] >= 0 && lm.bshift[2] >= 0 && lm.bshift[3] >= 0;
 #pragma unroll
 			for (int d = 3; d >= 0; --d) {
-				t[d] = s % plan.block[d];
-				s /= plan.block[d];
+				if (pow2) {
+					t[d] = s & ((1 << lm.bshift[d]) - 1);
+					s >>= lm.bshift[d];
+				} else {
+					t[d] = s % plan.block[d];
+					s /= plan.block[d];
+				}
 			}
 		}
 		int pts[ES][4];
@@ -255,7 +301,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			if (!valid[e]) continue;
 			simple_array<EType, Umi::N_PRE_IN * MAX_PTR> in;
 			simple_array<EType, Umi::N_PRE_OUT * MAX_PTR> out;
-			gather<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType>(plan, ptrs, pts[e], zero, false, in);
+			gather_point<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType>(plan, lm, ptrs, pts[e], in);
 			ctx[e].Pre(uc, in, out);
 			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
@@ -342,7 +388,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			if (!valid[e]) continue;
 			simple_array<EType, Umi::N_POST_IN * MAX_PTR> in;
 			simple_array<EType, Umi::N_POST_OUT * MAX_PTR> out;
-			gather<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType>(plan, ptrs, pts[e], zero, false, in);
+			gather_point<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType>(plan, lm, ptrs, pts[e], in);
 			ctx[e].Post(uc, in, out);
 			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
