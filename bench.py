@@ -45,7 +45,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # scaled to the configured batch.
 NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
                "fprop_n32": 67321088 + 206541312, "learned_me_4k": None, "coarse_me_4k": None,
-               "video_y4m_1080p": None, "apps_1080p": None}
+               "video_y4m_1080p": None, "apps_1080p": None, "serve_bilateral_8x512": None}
 NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 + 3253943000) / 12896910}
 
 
@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096",
                                            "fprop_n32", "learned_me_4k", "coarse_me_4k", "video_y4m_1080p",
-                                           "apps_1080p"],
+                                           "apps_1080p", "serve_bilateral_8x512"],
                     default="int_pair_1080p")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--images", type=int, default=64, help="batched_uneven: number of images (64 in the benchmark)")
@@ -65,7 +65,7 @@ def parse():
     if a.steps is None:
         a.steps = {"int_pair_1080p": 2000, "filter3x3_1024": 200000, "batched_uneven": 100,
                    "gemm_4096": 3000, "fprop_n32": 3000, "learned_me_4k": 200, "coarse_me_4k": 2000,
-                   "video_y4m_1080p": 2000, "apps_1080p": 500}[a.workload]
+                   "video_y4m_1080p": 2000, "apps_1080p": 500, "serve_bilateral_8x512": 2000}[a.workload]
     return a
 
 
@@ -1056,9 +1056,115 @@ class Apps1080p:
         return nrows * self.W / 1e6
 
 
+class ServeBilateral:
+    """Serving small batches (umi_gb300/serve.py): a request is 8 float32
+    images of 512x512 through the batched bilateral 5x5 (sigma_s 2, sigma_r
+    0.1).  value: requests/s of the recorded batch graph replayed with the
+    images resident in HBM (8 rotating buffer sets); e2e: requests/s through
+    BatchServer with 4 instances (streams) from host arrays: copy into pinned
+    staging, upload, replay, download per request (wall clock); the same
+    server with 1 instance is timed beside it."""
+    name = "serve_bilateral_8x512"
+    metric = "served requests/s (8 x 512x512 float32 bilateral 5x5 per request)"
+    unit = "requests/s"
+    dtype = "f32"
+    N_IMG, S, INSTANCES = 8, 512, 4
+    e2e_max_steps = 2000
+
+    def __init__(self, seed=31, **_):
+        self.seed = seed
+        self.px = self.N_IMG * self.S * self.S
+
+    def config(self):
+        return {"workload": self.name, "request": f"{self.N_IMG} x {self.S}x{self.S} f32",
+                "op": "bilateral r2 sigma_s 2 sigma_r 0.1", "instances": self.INSTANCES,
+                "l2": "8 resident request buffers rotated (134 MB > L2)"}
+
+    def units_per_step(self):
+        return 1.0
+
+    def setup(self, dev):
+        import torch
+        import umi_gb300 as U
+        from umi_gb300 import serve
+        self.U, self.serve, self.dev = U, serve, dev
+        self.prm = U.BatchParams(2, 2.0, 0.1, 0, 0)
+        g = np.random.default_rng(self.seed)
+        shp = (self.S, self.S)
+        self.reqs = [[g.random(shp, dtype=np.float32) for _ in range(self.N_IMG)] for _ in range(8)]
+        self.n_rot = 8
+        self.d_in = [[torch.from_numpy(x).to(dev) for x in r] for r in self.reqs]
+        self.d_out = [[torch.empty(shp, dtype=torch.float32, device=dev) for _ in range(self.N_IMG)]
+                      for _ in range(self.n_rot)]
+        self.tables = [list(zip(self.d_in[k], [None] * self.N_IMG, self.d_out[k])) for k in range(self.n_rot)]
+        self.launches_per_step = 1
+
+    def step(self, i):
+        # the batched launch a request's graph holds (the timed steps are themselves replayed from a graph)
+        self.U.batch_run(self.U.OP_BILATERAL, self.tables[i % self.n_rot], self.prm)
+
+    def e2e_bytes(self):
+        return 4 * self.px, 4 * self.px
+
+    def _serve(self, instances, n):
+        import torch
+        slots = [((self.S, self.S), None, (self.S, self.S))] * self.N_IMG
+        srv = self.serve.BatchServer(self.U.OP_BILATERAL, slots, self.prm, instances=instances, device=self.dev)
+        for r in self.reqs[:instances]:  # warm-up: graphs instantiated
+            srv.submit(r)
+        srv.drain()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        inflight = []
+        for i in range(n):
+            inflight.append(srv.submit(self.reqs[i % len(self.reqs)]))
+            if len(inflight) == instances:  # consumed in place, before its instance is reused
+                srv.result(inflight.pop(0), copy=False)
+        for t in inflight:
+            srv.result(t, copy=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        srv.close()
+        return dt
+
+    def e2e_run(self, steps, warmup):
+        """ms for `steps` requests through BatchServer with INSTANCES streams."""
+        dt = self._serve(self.INSTANCES, steps)
+        self.one_instance_rps = steps / self._serve(1, steps)
+        return dt * 1e3
+
+    def check(self):
+        """Every output of one served request against the direct call."""
+        import torch
+        srv = self.serve.BatchServer(self.U.OP_BILATERAL, [((self.S, self.S), None, (self.S, self.S))] * self.N_IMG,
+                                     self.prm, instances=2, device=self.dev)
+        out = srv.result(srv.submit(self.reqs[3]))
+        srv.close()
+        same = all(np.array_equal(o, self.U.bilateral_f32(torch.from_numpy(x).to(self.dev), 2, 2.0, 0.1).cpu().numpy())
+                   for x, o in zip(self.reqs[3], out))
+        return {"served_equals_direct": bool(same)}
+
+    def kernels(self, dev, peaks, n=50):
+        return {"bilateral_batch": time_launches(self.step, self.n_rot, n)}, None, 8 * self.px
+
+    def cpu_setup(self):
+        import oracle
+        self.orc = oracle
+        self.k = 0
+
+    def cpu_step(self, nrows, threads):
+        """FP64 bilateral of `nrows` rows of one 512x512 image of a request; units = requests."""
+        x = self.reqs[self.k % len(self.reqs)][0] if hasattr(self, "reqs") else \
+            np.random.default_rng(self.seed).random((self.S, self.S), dtype=np.float32)
+        self.k += 1
+        r0 = (self.k * nrows) % (self.S - nrows - 4)
+        self.orc.bilateral_f64(np.ascontiguousarray(x[r0:r0 + nrows + 4]), 2, 2.0, 0.1, threads=threads)
+        return nrows / (self.S * self.N_IMG)
+
+
 WORKLOADS = {"int_pair_1080p": IntPair, "filter3x3_1024": Filter3x3, "batched_uneven": Batched, "gemm_4096": Gemm,
              "fprop_n32": Fprop, "learned_me_4k": LearnedMe, "coarse_me_4k": CoarseMe4k,
-             "video_y4m_1080p": VideoY4M, "apps_1080p": Apps1080p}
+             "video_y4m_1080p": VideoY4M, "apps_1080p": Apps1080p, "serve_bilateral_8x512": ServeBilateral}
 
 
 def time_launches(fn, period: int, n: int) -> float:
@@ -1322,6 +1428,14 @@ def run_ours(args, wl, dist):
                 "traffic": NCU_TRAFFIC[wl.name],
                 "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
                 "work_per_launch": absdiff, "ms_per_launch": kms[roof_k]}
+    elif isinstance(wl, ServeBilateral):
+        kt = kms["bilateral_batch"]
+        ach = hbm_bytes / (kt * 1e-3) / 1e9
+        kernels["bilateral_batch"] = {"ms_per_launch": kt, "achieved": ach, "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
+                                      "bytes_per_launch": hbm_bytes, "ex2_per_s": 25 * wl.px / (kt * 1e-3)}
+        kernels["served_requests_per_s_one_instance"] = getattr(wl, "one_instance_rps", None)
+        roof = dict(kernels["bilateral_batch"], bound="hbm", kernel="batch_kernel<Bilateral> (graph replay)",
+                    peak=pk["hbm_gbs"], traffic=None, peak_source=pk["source"])
     elif isinstance(wl, Apps1080p):
         for name, kt in kms.items():
             b = wl.BYTES[name] * wl.px
@@ -1387,7 +1501,9 @@ def cpu_baseline(wl, sample_s=10.0):
     """The reference's CPU loop (oracle restatement) on a bounded sample, all host threads."""
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    if isinstance(wl, Apps1080p):
+    if isinstance(wl, ServeBilateral):
+        chunk, what = 16, "rows of one 512x512 request image through the FP64 bilateral 5x5 (units = requests of 8 images)"
+    elif isinstance(wl, Apps1080p):
         chunk, what = 16, "rows of the 1080p frame through numpy restatements of census 5x5, dilation 3x3, box 15x15 (integral image) and the FP64 separable Gaussian (the reference has none of these: its operator has no CPU path)"
     elif isinstance(wl, VideoY4M):
         chunk, what = 8, "random blocks of a 1080p pair of the video, +-64 full search with per-pixel clamp (main/full_me.cu:68-87) + argmin (the reference has no I/O and no proposal), units = pairs"
