@@ -325,6 +325,9 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			}
 			fast[e] = f;
 		}
+		bool all_fast = true;
+#pragma unroll
+		for (int e = 0; e < ES; ++e) all_fast &= fast[e] || !valid[e];
 		// Loop: accumulation blocks row-major, steps row-major inside a block
 		// (dimension 3 fastest), as four nested loops clipped to the A extent.
 		if (plan.n_ablock > 0) {
@@ -336,12 +339,13 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 					a0[d] = ab[d] * plan.ablock[d];
 					lim[d] = min(plan.ablock[d], plan.atotal[d] - a0[d]);
 				}
-				for (int s0 = 0; s0 < lim[0]; ++s0)
-					for (int s1 = 0; s1 < lim[1]; ++s1)
-						for (int s2 = 0; s2 < lim[2]; ++s2) {
-							// linear addresses of the row of steps s3 = 0.. (fast points), then one stride per step
-							int64_t row[ES][NLI];
-							{
+				if (ES == 1 && all_fast) {
+					// every point of the thread reads inside its extents: linear rows, one stride per step
+					// (one point per thread only: with several, the optimiser's time grows steeply)
+					for (int s0 = 0; s0 < lim[0]; ++s0)
+						for (int s1 = 0; s1 < lim[1]; ++s1)
+							for (int s2 = 0; s2 < lim[2]; ++s2) {
+								int64_t row[ES][NLI];
 								const int ar[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3]};
 #pragma unroll
 								for (int e = 0; e < ES; ++e)
@@ -349,15 +353,13 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 									for (int i = 0; i < NLI; ++i)
 										row[e][i] = lbase[e][i] + ar[0] * astr[i][0] + ar[1] * astr[i][1] +
 										            ar[2] * astr[i][2] + ar[3] * astr[i][3];
-							}
-							for (int s3 = 0; s3 < lim[3]; ++s3) {
-								const int a[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3] + s3};
+								for (int s3 = 0; s3 < lim[3]; ++s3) {
+									const int a[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3] + s3};
 #pragma unroll
-								for (int e = 0; e < ES; ++e) {
-									if (!valid[e]) continue;
-									simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
-									simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
-									if (fast[e]) {
+									for (int e = 0; e < ES; ++e) {
+										if (!valid[e]) continue;
+										simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
+										simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
 #pragma unroll
 										for (int i = 0; i < Umi::N_LOOP_IN; ++i) {
 											const int mem = LOOP_I + i;
@@ -367,14 +369,29 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 													in[i * MAX_PTR + j] = ptrs.in[mem * MAX_PTR + j][row[e][i]];
 											row[e][i] += astr[i][3];
 										}
-									} else {
-										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+										ctx[e].Loop(uc, in, out);
+										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
 									}
-									ctx[e].Loop(uc, in, out);
-									scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
 								}
 							}
-						}
+				} else {
+					// points near the edges: the clamped map for every step
+					for (int s0 = 0; s0 < lim[0]; ++s0)
+						for (int s1 = 0; s1 < lim[1]; ++s1)
+							for (int s2 = 0; s2 < lim[2]; ++s2)
+								for (int s3 = 0; s3 < lim[3]; ++s3) {
+									const int a[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3] + s3};
+#pragma unroll
+									for (int e = 0; e < ES; ++e) {
+										if (!valid[e]) continue;
+										simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
+										simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
+										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+										ctx[e].Loop(uc, in, out);
+										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
+									}
+								}
+				}
 #pragma unroll
 				for (int d = 3; d >= 0; --d) {
 					if (++ab[d] < plan.agrid[d]) break;
