@@ -22,7 +22,7 @@ def cache_path() -> str:
 
 
 def size_class(images) -> str:
-    """Batch size class: image count, log2 of the mean pixel count, log2 of the aspect spread."""
+    """Batch size class: image count and log2 of the mean pixel count."""
     if not images:
         return "empty"
     px = [max(1, t.shape[-2] * t.shape[-1]) for t, _, _ in images]
@@ -53,7 +53,8 @@ def tuned_variant(op: int, images, params=None, reps: int = 3, refresh: bool = F
     import torch
     key = f"{torch.cuda.get_device_name()}|{OP_NAMES[op]}|{size_class(images)}"
     cache = _load()
-    if not refresh and key in cache:
+    # a cached winner stands while the operator offers the same variants
+    if not refresh and key in cache and cache[key].get("variants") == U.batch_variants(op):
         return cache[key]["variant"], cache[key]["ms"], True
     v, ms = U.autotune_batch(op, images, params, reps=reps)
     cache[key] = {"variant": v, "ms": ms, "variants": U.batch_variants(op)}
