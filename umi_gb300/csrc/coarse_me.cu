@@ -84,23 +84,68 @@ struct CoarseGeom {
 	}
 };
 
+// Bytes x0 .. x0 + 19 of a row as five words, columns clamped to the row.
+__device__ __forceinline__ void row_words5(const uint8_t* __restrict__ row, int w, int x0, bool fast, uint32_t (&v)[5]) {
+	if (fast) {  // 4-byte aligned and inside the row
+		const uint32_t* p = reinterpret_cast<const uint32_t*>(row + x0);
+#pragma unroll
+		for (int k = 0; k < 5; ++k) v[k] = __ldg(p + k);
+	} else {
+#pragma unroll
+		for (int k = 0; k < 5; ++k) {
+			uint32_t t = 0;
+#pragma unroll
+			for (int b = 0; b < 4; ++b) t |= (uint32_t)__ldg(row + min(max(x0 + 4 * k + b, 0), w - 1)) << (8 * b);
+			v[k] = t;
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t pack_cells(const uint32_t (&s)[4]) {
+	return ((s[0] + 8) >> 4) | (((s[1] + 8) >> 4) << 8) | (((s[2] + 8) >> 4) << 16) | (((s[3] + 8) >> 4) << 24);
+}
+
 // cells[4 blk + i] = cells of cur's block row i; planes as described above.
-// One thread per output word.
+// A plane thread owns word k of plane row `row` in all four planes: the cells
+// q(4 (row - 16) + 2 py, 16 k - 64 + 2 px + 4 j) for py, px in {0, 1} and
+// j = 0..3 cover pixel rows 4 row - 64 .. +5 and bytes 16 k - 64 .. +19, so
+// the thread reads six rows of five words once (row sums by vabsdiff4
+// against zero; rows 2-3 are shared by both row parities).  A cell thread
+// owns one word of cur's cells.
 __global__ void __launch_bounds__(NT) coarse_cells_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
                                                           CoarseGeom g, bool words, uint32_t* __restrict__ cells,
                                                           uint32_t* __restrict__ planes) {
 	const int pww = g.pw / 4;
-	const size_t nplane = 4 * (size_t)g.pr * pww, n = nplane + 4 * (size_t)g.nblk;
-	for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+	const int nplane = g.pr * pww, n = nplane + 4 * g.nblk;  // < 2^31: frames up to 2^30 pixels
+	const size_t plane_words = (size_t)nplane;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
 		if (e < nplane) {
-			const int p = (int)(e / ((size_t)g.pr * pww));
-			const int r = (int)(e - (size_t)p * g.pr * pww);
-			const int row = r / pww, k = r - row * pww;
-			const int py = p >> 1, px = p & 1;
-			// cells b = 4k - 16 + j, j = 0..3: pixels x = 4b + 2px = 16k - 64 + 2px + 4j
-			planes[e] = box_word(ref, g.h, g.w, 4 * (row - MARGIN) + 2 * py, 16 * k - 4 * MARGIN + 2 * px, words);
+			const int row = e / pww, k = e - row * pww;
+			const int y0 = 4 * (row - MARGIN), x0 = 16 * k - 4 * MARGIN;
+			const bool fast = words && x0 >= 0 && x0 + 20 <= g.w;
+			uint32_t acc[3][2][4];  // [pixel row pair][px][j]
+#pragma unroll
+			for (int u = 0; u < 6; ++u) {
+				uint32_t v[5];
+				row_words5(ref + (size_t)min(max(y0 + u, 0), g.h - 1) * g.w, g.w, x0, fast, v);
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const uint32_t odd = __byte_perm(v[j], v[j + 1], 0x5432u);  // bytes 4j + 2 .. 4j + 5
+					acc[u >> 1][0][j] = sad4_acc(v[j], 0u, (u & 1) ? acc[u >> 1][0][j] : 0u);
+					acc[u >> 1][1][j] = sad4_acc(odd, 0u, (u & 1) ? acc[u >> 1][1][j] : 0u);
+				}
+			}
+#pragma unroll
+			for (int py = 0; py < 2; ++py)
+#pragma unroll
+				for (int px = 0; px < 2; ++px) {
+					uint32_t s[4];
+#pragma unroll
+					for (int j = 0; j < 4; ++j) s[j] = acc[py][px][j] + acc[py + 1][px][j];
+					planes[(2 * py + px) * plane_words + e] = pack_cells(s);
+				}
 		} else {
-			const int c = (int)(e - nplane), blk = c >> 2, i = c & 3;
+			const int c = e - nplane, blk = c >> 2, i = c & 3;
 			const int by = blk / g.nbx, bx = blk - by * g.nbx;
 			cells[c] = box_word(cur, g.h, g.w, 16 * by + 4 * i, 16 * bx, words);
 		}
@@ -215,7 +260,7 @@ umi_status centers_impl(const uint8_t* cur, const uint8_t* ref, int h, int w, in
 	const CoarseGeom g(h, w);
 	const CoarseWork K(g);
 	const bool words = umi::aligned(cur, 4) && umi::aligned(ref, 4);
-	const size_t items = 4 * g.plane_bytes / 4 + 4 * (size_t)g.nblk;
+	const size_t items = (size_t)g.pr * (g.pw / 4) + 4 * (size_t)g.nblk;
 	const int grid = (int)std::min<size_t>((items + NT - 1) / NT, 152 * 16);
 	coarse_cells_kernel<<<grid, NT, 0, st>>>(cur, ref, g, words, K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes));
 	UMI_TRY(umi::launch_status("coarse_cells_kernel"));
