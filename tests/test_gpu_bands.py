@@ -1,0 +1,57 @@
+"""Row-band split (umi_gb300/bands.py) on one GPU: the bands of 1 to 5 ranks,
+run one after another through the CUDA kernels, reproduce the whole-frame
+results bit for bit (full search on halo slices, 3x3 filter, integral image
+with the carry of the bands above, int32 wrap included)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+WORLDS = [1, 2, 3, 5]
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("h,w,b,r", [(272, 320, 16, 32), (130, 104, 8, 5), (1080, 1920, 16, 32), (200, 256, 16, 64)])
+@pytest.mark.parametrize("world", WORLDS)
+def test_me_bands(umi, dev, h, w, b, r, world):
+    import torch
+    from umi_gb300 import bands
+    g = np.random.default_rng(h + world)
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = np.roll(cur, (5, -3), (0, 1)) ^ g.integers(0, 8, (h, w), dtype=np.uint8)
+    c, rf = _t(cur, dev), _t(ref, dev)
+    whole = umi.full_me_u8(c, rf, block=b, search=r)
+    parts = torch.cat([bands.me_band(c, rf, world, k, block=b, search=r) for k in range(world)])
+    assert torch.equal(parts, whole.reshape(-1, 3))
+
+
+@pytest.mark.parametrize("h,w", [(67, 129), (1, 40), (1024, 1024)])
+@pytest.mark.parametrize("world", WORLDS)
+def test_filter3x3_bands(umi, dev, h, w, world):
+    import torch
+    from umi_gb300 import bands
+    g = np.random.default_rng(h * w + world)
+    img = _t(g.standard_normal((h, w)).astype(np.float32), dev)
+    w9 = g.standard_normal(9).astype(np.float32)  # host weights, as the C-ABI takes them
+    whole = umi.filter3x3_f32(img, w9, 0.5)
+    parts = torch.cat([bands.filter3x3_band(img, w9, world, k, pad=0.5) for k in range(world)])
+    assert torch.equal(parts, whole)
+
+
+@pytest.mark.parametrize("h,w,full", [(37, 53, False), (1080, 1920, False), (2304, 4096, True)])
+@pytest.mark.parametrize("world", WORLDS)
+def test_iimg_bands(umi, dev, h, w, full, world):
+    import torch
+    from umi_gb300 import bands
+    g = np.random.default_rng(h + w + world)
+    img = np.full((h, w), 255, np.uint8) if full else g.integers(0, 256, (h, w), dtype=np.uint8)
+    x = _t(img, dev)
+    whole = umi.iimg_u8_i32(x)  # 2304 x 4096 x 255 > 2^31: the int32 sums wrap
+    locals_ = [bands.iimg_band_local(x, world, k) for k in range(world)]
+    totals = [bands.band_totals(l) for l in locals_]
+    parts = torch.cat([bands.add_carry(l, totals, k) for k, l in enumerate(locals_)])
+    assert torch.equal(parts, whole)
