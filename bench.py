@@ -678,9 +678,10 @@ class LearnedMe:
         self.h_cur = self.d_cur[0].cpu().pin_memory()
         self.h_ref = self.d_ref[0].cpu().pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
-        # inference (downsample, 4 weight packs, layer 1, 3 tensor-core layers, head) + centres + refine
-        # + flag + one list search (audit and fallback) + audit sum (memsets and the count copy are not kernels)
-        self.launches_per_step = 15
+        # audit list + audit search (second stream) + inference (downsample, 4 weight packs, layer 1,
+        # 3 tensor-core layers, head) + centres + refine + flag + fallback list search + audit merge
+        # (memsets, event waits and the count copy are not kernels)
+        self.launches_per_step = 17
 
     def _estimate(self, k):
         self.net.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
@@ -764,8 +765,9 @@ class CoarseMe4k(LearnedMe):
     def setup(self, dev):
         super().setup(dev)
         self.cme = self.U.CoarseMe(self.H, self.W, device=dev)
-        # cells + search + refine + flag + one list search (audit and fallback) + audit sum
-        self.launches_per_step = 6
+        # audit list + audit search (second stream) + cells + search + refine + flag + fallback list
+        # search + audit merge
+        self.launches_per_step = 8
 
     def _estimate(self, k):
         self.cme.estimate(self.d_cur[k], self.d_ref[k], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,
@@ -841,8 +843,9 @@ class VideoY4M:
         self.d_mv = [torch.empty((self.nblk, 3), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
         self.d_sums = [torch.zeros(2, dtype=torch.int64, device=dev) for _ in range(self.n_rot)]
         self.d_nf = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
-        # cells + search + refine + flag + one list search (audit and fallback) + audit sum
-        self.launches_per_step = 6
+        # audit list + audit search (second stream) + cells + search + refine + flag + fallback list
+        # search + audit merge
+        self.launches_per_step = 8
 
     def _pair(self, j):
         self.cme.estimate(self.d[j + 1], self.d[j], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,

@@ -263,7 +263,11 @@ umi_status umi_menet_adam(float* params, const float* grads, float* m, float* v,
  * block whose refined SAD exceeds sad_threshold is searched exhaustively in
  * +-full_r around (0, 0).  mv receives (mv_y, mv_x, sad) per block as
  * umi_full_me_u8 with b = 16; n_fallback (device, may be NULL) the number of
- * fallback blocks.  1 <= refine_r <= full_r <= 64. */
+ * fallback blocks.  1 <= refine_r <= full_r <= 64.  The audit's exhaustive
+ * search does not depend on the proposal: it runs on a second stream of the
+ * calling host thread (one per device, made on the first call outside a
+ * stream capture), forked from `stream` at entry and joined back before the
+ * call's last work on `stream`; stream order and capture are kept. */
 umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
                              int32_t refine_r, int32_t full_r, int32_t sad_threshold, int32_t audit_stride,
                              int32_t* mv, unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,

@@ -87,7 +87,7 @@ def test_iimg_exchange_and_gather_two_gloo_ranks(tmp_path):
     g = np.random.default_rng(3)
     frames = [g.integers(0, 256, (37, 53), dtype=np.uint8),  # uneven bands: 18 and 19 rows
               g.integers(0, 256, (1, 9), dtype=np.uint8),    # an empty band on rank 0
-              np.full((2920, 2920), 255, np.uint8)]           # sums past 2^31: int32 wraps as in one frame
+              np.full((2160, 3840), 255, np.uint8)]           # 4K of 255: sums near 2^31, the operator's limit
     out = str(tmp_path / "bands")
     mp.spawn(_band_worker, args=(2, _free_port(), frames, out), nprocs=2, join=True)
     for rank in range(2):

@@ -1,7 +1,8 @@
 """Row-band split (umi_gb300/bands.py) on one GPU: the bands of 1 to 5 ranks,
 run one after another through the CUDA kernels, reproduce the whole-frame
 results bit for bit (full search on halo slices, 3x3 filter, integral image
-with the carry of the bands above, int32 wrap included)."""
+with the carry of the bands above); frames the whole-frame integral image
+refuses are refused by the bands too."""
 import numpy as np
 import pytest
 
@@ -42,7 +43,7 @@ def test_filter3x3_bands(umi, dev, h, w, world):
     assert torch.equal(parts, whole)
 
 
-@pytest.mark.parametrize("h,w,full", [(37, 53, False), (1080, 1920, False), (2304, 4096, True)])
+@pytest.mark.parametrize("h,w,full", [(37, 53, False), (1080, 1920, False), (2160, 3840, True)])
 @pytest.mark.parametrize("world", WORLDS)
 def test_iimg_bands(umi, dev, h, w, full, world):
     import torch
@@ -50,8 +51,17 @@ def test_iimg_bands(umi, dev, h, w, full, world):
     g = np.random.default_rng(h + w + world)
     img = np.full((h, w), 255, np.uint8) if full else g.integers(0, 256, (h, w), dtype=np.uint8)
     x = _t(img, dev)
-    whole = umi.iimg_u8_i32(x)  # 2304 x 4096 x 255 > 2^31: the int32 sums wrap
+    whole = umi.iimg_u8_i32(x)  # 4K of 255: the largest sums the operator takes
     locals_ = [bands.iimg_band_local(x, world, k) for k in range(world)]
     totals = [bands.band_totals(l) for l in locals_]
     parts = torch.cat([bands.add_carry(l, totals, k) for k, l in enumerate(locals_)])
     assert torch.equal(parts, whole)
+
+
+def test_iimg_band_refuses_what_the_operator_refuses(umi, dev):
+    from umi_gb300 import bands
+    x = _t(np.zeros((2304, 4096), np.uint8), dev)
+    with pytest.raises(umi.UmiError):
+        umi.iimg_u8_i32(x)
+    with pytest.raises(umi.UmiError):
+        bands.iimg_band_local(x, 2, 1)

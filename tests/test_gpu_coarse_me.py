@@ -93,6 +93,86 @@ def test_coarse_entry_refine_audit_fallback(umi, dev):
     assert np.mean(refined_np[:, 2] == full_np[:, 2]) > 0.9
 
 
+def _estimate_into(cme, c, r, outs):
+    cme.estimate(c, r, 4, 31, sad_threshold=450, audit_stride=5, out=outs[0], audit_sums=outs[1], n_fallback=outs[2])
+
+
+def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev):
+    """The audit's exhaustive search runs on the calling thread's second
+    stream (forked and joined inside the call): the results are the same
+    eagerly, replayed from a CUDA graph that captured the fork, and when the
+    first call of a fresh host thread is itself captured (no second stream
+    yet: everything in order on the captured stream)."""
+    import threading
+
+    import torch
+    from umi_gb300.workloads import me_pair
+    h, w = 192, 256
+    cur, ref, _ = me_pair(seed=9, h=h, w=w, shift_sigma=12.0, max_shift=30)
+    c, r = _t(cur, dev), _t(ref, dev)
+    nblk = (h // 16) * (w // 16)
+    cme = umi.CoarseMe(h, w, device=dev)
+
+    def outs():
+        return (torch.empty((nblk, 3), dtype=torch.int32, device=dev), torch.zeros(2, dtype=torch.int64, device=dev),
+                torch.zeros(1, dtype=torch.int32, device=dev))
+
+    # the definition, from the separate calls
+    full = umi.full_me_u8(c, r, 16, 31)
+    refined = umi.full_me_u8(c, r, 16, 4, centers=cme.centers(c, r, 26))
+    aud = torch.arange(0, nblk, 5, device=dev)
+    want = refined.clone()
+    rest = torch.ones(nblk, dtype=torch.bool, device=dev)
+    rest[aud] = False
+    fb = rest & (refined[:, 2] > 450)
+    want[fb] = full[fb]
+    want[aud] = full[aud]
+    want_sums = [int(refined[aud, 2].sum()), int(full[aud, 2].sum())]
+    want_nf = int(fb.sum())
+
+    def check(o):
+        assert torch.equal(o[0], want)
+        assert o[1].tolist() == want_sums and int(o[2].item()) == want_nf
+
+    eager = outs()
+    _estimate_into(cme, c, r, eager)
+    torch.cuda.synchronize()
+    check(eager)
+
+    graphed = outs()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        _estimate_into(cme, c, r, graphed)
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    check(graphed)
+
+    result, errors = {}, []
+
+    def fresh_thread():
+        try:
+            torch.cuda.set_device(dev)
+            o = outs()
+            g2 = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g2):
+                _estimate_into(cme, c, r, o)  # this thread's first call: captured in order
+            g2.replay()
+            o2 = outs()
+            _estimate_into(cme, c, r, o2)  # eager: the thread's second stream is made now
+            torch.cuda.synchronize()
+            result["captured"], result["eager"] = o, o2
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    t = threading.Thread(target=fresh_thread)
+    t.start()
+    t.join()
+    assert not errors, errors
+    check(result["captured"])
+    check(result["eager"])
+
+
 def test_coarse_rejects(umi, dev):
     import torch
     assert umi.lib().umi_me_coarse_workspace_bytes(100, 64) == 0

@@ -16,8 +16,8 @@ for bit:
 * integral image (``iimg_band``): no halo and one exchange.  A band's integral
   image equals the integral image of its own rows plus, in every row, the sum
   of the last rows of the bands above it (an exclusive scan over ranks of one
-  row each, made by ``all_gather``).  int32 sums wrap exactly as the
-  whole-frame kernel's do.
+  row each, made by ``all_gather``).  Frames are limited as for the
+  whole-frame operator (sums within int32).
 
 ``gather_rows`` assembles the bands on every rank.  Nothing waits on another
 rank inside a kernel: the only collectives are ``torch.distributed``
@@ -89,9 +89,13 @@ def filter3x3_band(img, w9, world: int, rank: int, pad: float = 0.0, stream=None
 
 
 def iimg_band_local(img, world: int, rank: int, stream=None):
-    """Integral image of the rank's own rows (no carry from the bands above)."""
+    """Integral image of the rank's own rows (no carry from the bands above).
+    Frames the whole-frame operator refuses (sums that could exceed int32:
+    more than 2^31 / 255 pixels) are refused here too."""
     import torch
     h, w = img.shape
+    if h * w > (1 << 31) // 255:
+        raise U.UmiError(3, "iimg_band", f"{h}x{w} frame: sums could exceed int32")
     y0, y1 = split(h, world, rank)
     if y1 == y0:
         return torch.empty((0, w), dtype=torch.int32, device=img.device)
@@ -120,7 +124,7 @@ def exchange_totals(totals, group=None) -> list:
 
 def add_carry(local, all_totals, rank: int):
     """local + (sum of the totals of ranks < rank) in every row, in place
-    (int32, wrapping like the whole-frame kernel)."""
+    (int32; sums past int32 wrap, two's complement)."""
     import torch
     if rank > 0 and local.shape[0] > 0:
         carry = torch.stack(list(all_totals[:rank])).sum(0, dtype=torch.int64)

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 
 // ---- workspace
 struct CoarseWork {
-	size_t cells, planes, centers, list, count, bytes;
+	size_t cells, planes, centers, list, count, alist, amv, bytes;
 	explicit CoarseWork(const CoarseGeom& g) {
 		size_t o = 0;
 		auto take = [&](size_t n) { size_t r = o; o += (n + 255) & ~size_t(255); return r; };
@@ -243,6 +243,8 @@ struct CoarseWork {
 		centers = take(sizeof(int32_t) * 2 * g.nblk);
 		list = take(sizeof(int32_t) * g.nblk);
 		count = take(sizeof(int32_t) * 4);
+		alist = take(sizeof(int32_t) * g.nblk);
+		amv = take(sizeof(int32_t) * 3 * g.nblk);
 		bytes = o;
 	}
 	template <class T> T* at(void* ws, size_t off) const { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
@@ -306,9 +308,12 @@ extern "C" umi_status umi_me_coarse_u8(const uint8_t* cur, const uint8_t* ref, i
 	if (audit_stride < 0) return umi::fail(UMI_ERR_INVALID_ARG, "coarse ME: negative audit stride");
 	const cudaStream_t st = umi::as_stream(stream);
 	const CoarseWork K{CoarseGeom(h, w)};
+	const umi::MeFinishBuffers fb{K.at<int32_t>(workspace, K.list), K.at<int32_t>(workspace, K.count),
+	                              K.at<int32_t>(workspace, K.alist), K.at<int32_t>(workspace, K.amv)};
+	umi::MeAudit audit;  // the audited blocks' exhaustive search runs beside the proposal and the refine
+	UMI_TRY(umi::me_audit_begin(cur, ref, h, w, full_r, audit_stride, fb, st, &audit));
 	int32_t* centers = K.at<int32_t>(workspace, K.centers);
 	UMI_TRY(centers_impl(cur, ref, h, w, (full_r - refine_r) & ~1, centers, workspace, st));
-	const umi::MeFinishBuffers fb{K.at<int32_t>(workspace, K.list), K.at<int32_t>(workspace, K.count)};
-	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
-	                                     audit_sums, n_fallback, fb, st);
+	return umi::me_refine_fallback_finish(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
+	                                      audit_sums, n_fallback, fb, audit, st);
 }

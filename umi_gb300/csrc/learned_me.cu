@@ -53,7 +53,7 @@ struct Layout {
 // ---- workspace layout for a frame of h x w pixels
 struct Work {
 	int H4, W4, P, nbx, nby, nblk, tiles_wg;
-	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, wpart, hpart, lpart;
+	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, alist, amv, wpart, hpart, lpart;
 	size_t nhwc[2], wtc[NL], err;  // tensor-core inference: bf16 (H4, W4, 64) activations, packed weights
 	size_t bytes;
 	Work(int h, int w) {
@@ -70,7 +70,9 @@ struct Work {
 		pred = take(sizeof(float) * 2 * nblk);
 		centers = take(sizeof(int32_t) * 2 * nblk);
 		list = take(sizeof(int32_t) * nblk);
-		count = take(sizeof(int32_t) * 4);  // [0] listed blocks, [1] fallback blocks
+		count = take(sizeof(int32_t) * 4);  // [0] fallback blocks, [2] audited blocks
+		alist = take(sizeof(int32_t) * nblk);
+		amv = take(sizeof(int32_t) * 3 * nblk);
 		wpart = take(sizeof(float) * (size_t)tiles_wg * (CH * CH * 9 + CH));
 		hpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8) * (2 * HEADF + 2));
 		lpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8));
@@ -358,34 +360,46 @@ __global__ void centers_kernel(const float* __restrict__ pred, int32_t* __restri
 	}
 }
 
-// One list for the exhaustive search: the audited blocks 0, stride, 2 stride,
-// ... (their refined SAD goes to audit_sums[0]) and every other block whose
-// refined SAD exceeds the threshold (counted in count[1]).  count[0] is the
-// list length.  List order is the order of discovery; the search is per
-// block, so the order changes no result.
+// Fallback list: every block other than the audited ones (0, stride,
+// 2 stride, ...) whose refined SAD exceeds the threshold; count[0] is its
+// length.  List order is the order of discovery; the search is per block, so
+// the order changes no result.
 __global__ void flag_kernel(const int32_t* __restrict__ mv, int n, int stride, int32_t thr,
-                            int32_t* __restrict__ list, int32_t* __restrict__ count,
-                            unsigned long long* __restrict__ audit_sums) {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		if (stride > 0 && i % stride == 0) {
-			if (audit_sums) atomicAdd(audit_sums, (unsigned long long)mv[3 * i + 2]);
-			list[atomicAdd(count, 1)] = i;
-		} else if (mv[3 * i + 2] > thr) {
-			list[atomicAdd(count, 1)] = i;
-			atomicAdd(count + 1, 1);
-		}
-	}
+                            int32_t* __restrict__ list, int32_t* __restrict__ count) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		if (!(stride > 0 && i % stride == 0) && mv[3 * i + 2] > thr) list[atomicAdd(count, 1)] = i;
 }
 
-// audit_sums[1] += exhaustive SAD of the audited blocks (after the search).
-__global__ void audit_sum_kernel(const int32_t* __restrict__ mv, int n, int stride,
-                                 unsigned long long* __restrict__ audit_sums) {
+// alist = 0, stride, 2 stride, ... (*acount = their number).
+__global__ void audit_list_kernel(int32_t* __restrict__ alist, int32_t* __restrict__ acount, int n, int stride) {
 	const int na = (n + stride - 1) / stride;
-	unsigned long long s = 0;
-	for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x)
-		s += (unsigned long long)mv[3 * (size_t)a * stride + 2];
-	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-	if ((threadIdx.x & 31) == 0 && s) atomicAdd(audit_sums + 1, s);
+	for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) alist[a] = a * stride;
+	if (blockIdx.x == 0 && threadIdx.x == 0) *acount = na;
+}
+
+// The audited blocks take their exhaustive result (amv) in place of the
+// refined one (mv); audit_sums (if non-null) += (refined SAD, exhaustive SAD).
+__global__ void audit_merge_kernel(int32_t* __restrict__ mv, const int32_t* __restrict__ amv, int n, int stride,
+                                   unsigned long long* __restrict__ audit_sums) {
+	const int na = (n + stride - 1) / stride;
+	unsigned long long s0 = 0, s1 = 0;
+	for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
+		const size_t j = 3 * (size_t)a * stride;
+		s0 += (unsigned long long)mv[j + 2];
+		s1 += (unsigned long long)amv[j + 2];
+		mv[j] = amv[j];
+		mv[j + 1] = amv[j + 1];
+		mv[j + 2] = amv[j + 2];
+	}
+	if (!audit_sums) return;
+	for (int o = 16; o > 0; o >>= 1) {
+		s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+		s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		if (s0) atomicAdd(audit_sums, s0);
+		if (s1) atomicAdd(audit_sums + 1, s1);
+	}
 }
 
 // ---- tensor-core inference path: bf16 NHWC activations, 64 channels per
@@ -651,43 +665,105 @@ extern "C" umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, 
 	if (audit_stride < 0) return umi::fail(UMI_ERR_INVALID_ARG, "me_learned: negative audit stride");
 	const cudaStream_t st = umi::as_stream(stream);
 	void* ws = workspace;
+	const umi::MeFinishBuffers fb{K.at<int32_t>(ws, K.list), K.at<int32_t>(ws, K.count), K.at<int32_t>(ws, K.alist),
+	                              K.at<int32_t>(ws, K.amv)};
+	umi::MeAudit audit;
+	UMI_TRY(umi::me_audit_begin(cur, ref, h, w, full_r, audit_stride, fb, st, &audit));
 	UMI_TRY(infer(cur, ref, h, w, params, ws, K.at<int32_t>(ws, K.err), st));
 	int32_t* centers = K.at<int32_t>(ws, K.centers);
 	centers_kernel<<<grid_for(2 * (size_t)K.nblk), NT, 0, st>>>(K.at<float>(ws, K.pred), centers, K.nblk,
 	                                                             full_r - refine_r);
 	UMI_TRY(umi::launch_status("centers_kernel"));
-	const umi::MeFinishBuffers fb{K.at<int32_t>(ws, K.list), K.at<int32_t>(ws, K.count)};
-	return umi::me_refine_audit_fallback(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
-	                                     audit_sums, n_fallback, fb, st);
+	return umi::me_refine_fallback_finish(cur, ref, h, w, centers, refine_r, full_r, sad_threshold, audit_stride, mv,
+	                                      audit_sums, n_fallback, fb, audit, st);
 }
 
 namespace umi {
 
-// Refine around the proposal's centres, audit every audit_stride-th block by
-// exhaustive search (its result replaces the refined one, both SADs go to
-// audit_sums), then exhaustive search for every other block whose refined
-// SAD exceeds sad_threshold.  Shared by the learned and the coarse proposal.
-umi_status me_refine_audit_fallback(const uint8_t* cur, const uint8_t* ref, int h, int w, const int32_t* centers,
-                                    int refine_r, int full_r, int32_t sad_threshold, int audit_stride, int32_t* mv,
-                                    unsigned long long* audit_sums, int32_t* n_fallback, const MeFinishBuffers& b,
-                                    cudaStream_t st) {
+namespace {
+
+// The calling thread's second stream on one device, with its fork and join
+// events: made on first use outside a stream capture, destroyed at thread exit.
+struct AuxStream {
+	cudaStream_t s = nullptr;
+	cudaEvent_t fork = nullptr, join = nullptr;
+	~AuxStream() {
+		if (join) cudaEventDestroy(join);
+		if (fork) cudaEventDestroy(fork);
+		if (s) cudaStreamDestroy(s);
+	}
+};
+
+AuxStream* aux_stream(cudaStream_t st) {
+	constexpr int kMaxDevices = 64;
+	thread_local AuxStream aux[kMaxDevices];
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+	AuxStream& a = aux[dev];
+	if (a.s && a.fork && a.join) return &a;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
+	if (!a.s && cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking) != cudaSuccess) a.s = nullptr;
+	if (!a.fork && cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming) != cudaSuccess) a.fork = nullptr;
+	if (!a.join && cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming) != cudaSuccess) a.join = nullptr;
+	cudaGetLastError();  // a failure here only means no second stream
+	return a.s && a.fork && a.join ? &a : nullptr;
+}
+
+}  // namespace
+
+umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, int full_r, int audit_stride,
+                          const MeFinishBuffers& b, cudaStream_t st, MeAudit* audit) {
+	*audit = MeAudit{};
+	const int nblk = (h / 16) * (w / 16);
+	if (audit_stride <= 0 || nblk == 0) return UMI_OK;
+	audit->active = true;
+	AuxStream* aux = aux_stream(st);
+	cudaStream_t as = st;
+	if (aux) {
+		UMI_TRY(cuda_status(cudaEventRecord(aux->fork, st), "cudaEventRecord"));
+		UMI_TRY(cuda_status(cudaStreamWaitEvent(aux->s, aux->fork, 0), "cudaStreamWaitEvent"));
+		as = aux->s;
+	}
+	const int na = ceil_div(nblk, audit_stride);
+	audit_list_kernel<<<grid_for(na), NT, 0, as>>>(b.alist, b.count + 2, nblk, audit_stride);
+	UMI_TRY(launch_status("audit_list_kernel"));
+	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 2, na, b.amv, as));
+	if (aux) {
+		UMI_TRY(cuda_status(cudaEventRecord(aux->join, aux->s), "cudaEventRecord"));
+		audit->forked = true;
+		audit->done = aux->join;
+	}
+	return UMI_OK;
+}
+
+// Refine around the proposal's centres, exhaustive search for every
+// non-audited block whose refined SAD exceeds sad_threshold, then the
+// audited blocks' exhaustive results (begun by me_audit_begin) replace the
+// refined ones.  Shared by the learned and the coarse proposal.
+umi_status me_refine_fallback_finish(const uint8_t* cur, const uint8_t* ref, int h, int w, const int32_t* centers,
+                                     int refine_r, int full_r, int32_t sad_threshold, int audit_stride, int32_t* mv,
+                                     unsigned long long* audit_sums, int32_t* n_fallback, const MeFinishBuffers& b,
+                                     const MeAudit& audit, cudaStream_t st) {
 	const int nblk = (h / 16) * (w / 16);
 	void* stream = st;
 	UMI_TRY(umi_full_me_u8(cur, ref, h, w, 16, refine_r, centers, mv, stream));
-	UMI_TRY(umi::cuda_status(cudaMemsetAsync(b.count, 0, 2 * sizeof(int32_t), st), "cudaMemsetAsync"));
-	if (audit_sums)
-		UMI_TRY(umi::cuda_status(cudaMemsetAsync(audit_sums, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync"));
-	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, nblk, audit_stride, sad_threshold, b.list, b.count, audit_sums);
-	UMI_TRY(umi::launch_status("flag_kernel"));
+	UMI_TRY(cuda_status(cudaMemsetAsync(b.count, 0, sizeof(int32_t), st), "cudaMemsetAsync"));
+	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, nblk, audit.active ? audit_stride : 0, sad_threshold, b.list, b.count);
+	UMI_TRY(launch_status("flag_kernel"));
 	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.list, b.count, nblk, mv, stream));
-	if (audit_stride > 0 && audit_sums) {
-		audit_sum_kernel<<<grid_for(umi::ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, nblk, audit_stride, audit_sums);
-		UMI_TRY(umi::launch_status("audit_sum_kernel"));
+	if (audit_sums)
+		UMI_TRY(cuda_status(cudaMemsetAsync(audit_sums, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync"));
+	if (audit.active) {
+		if (audit.forked) UMI_TRY(cuda_status(cudaStreamWaitEvent(st, audit.done, 0), "cudaStreamWaitEvent"));
+		audit_merge_kernel<<<grid_for(ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, b.amv, nblk, audit_stride,
+		                                                                          audit_sums);
+		UMI_TRY(launch_status("audit_merge_kernel"));
 	}
 	if (n_fallback)
-		UMI_TRY(umi::cuda_status(cudaMemcpyAsync(n_fallback, b.count + 1, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
-		                         "cudaMemcpyAsync"));
-	return umi::ok();
+		UMI_TRY(cuda_status(cudaMemcpyAsync(n_fallback, b.count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
+		                    "cudaMemcpyAsync"));
+	return ok();
 }
 
 }  // namespace umi

@@ -13,20 +13,36 @@ namespace umi {
 
 // Device scratch of the shared stage, nblk = (h/16)(w/16) blocks.
 struct MeFinishBuffers {
-	int32_t* list;   // nblk: blocks searched exhaustively (audited and fallback)
-	int32_t* count;  // 2: [0] listed blocks, [1] fallback blocks
+	int32_t* list;   // nblk: fallback blocks
+	int32_t* count;  // 4: [0] fallback blocks, [2] audited blocks
+	int32_t* alist;  // nblk: audited blocks 0, stride, 2 stride, ...
+	int32_t* amv;    // 3 nblk: exhaustive results, written at the audited blocks' rows only
 };
 
-// mv (nblk, 3) <- refine +-refine_r around centers (nblk, 2); every
-// audit_stride-th block (0: none) takes its +-full_r exhaustive result and
-// adds (refined SAD, exhaustive SAD) to audit_sums[0..1] (if non-null); every
-// other block whose refined SAD exceeds sad_threshold is searched
-// exhaustively; n_fallback (if non-null) receives their count.  Audited and
-// fallback blocks go through one exhaustive list search.  The centres must
+// The audit's exhaustive search, started before the proposal so that it can
+// run beside it: `forked` when it went to the calling thread's second stream
+// on this device (joined by `done`), else it ran in order on the caller's
+// stream.
+struct MeAudit {
+	bool active = false;
+	bool forked = false;
+	cudaEvent_t done = nullptr;
+};
+
+// Audit: every audit_stride-th block (0: none) is searched exhaustively in
+// +-full_r into b.amv.  Call before the proposal, on the proposal's stream.
+umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, int full_r, int audit_stride,
+                          const MeFinishBuffers& b, cudaStream_t st, MeAudit* audit);
+
+// mv (nblk, 3) <- refine +-refine_r around centers (nblk, 2); every other
+// block than the audited ones whose refined SAD exceeds sad_threshold is
+// searched exhaustively (n_fallback, if non-null, receives their count);
+// then the audited blocks take their exhaustive result and add (refined
+// SAD, exhaustive SAD) to audit_sums[0..1] (if non-null).  The centres must
 // lie within +-(full_r - refine_r).
-umi_status me_refine_audit_fallback(const uint8_t* cur, const uint8_t* ref, int h, int w, const int32_t* centers,
-                                    int refine_r, int full_r, int32_t sad_threshold, int audit_stride, int32_t* mv,
-                                    unsigned long long* audit_sums, int32_t* n_fallback, const MeFinishBuffers& b,
-                                    cudaStream_t st);
+umi_status me_refine_fallback_finish(const uint8_t* cur, const uint8_t* ref, int h, int w, const int32_t* centers,
+                                     int refine_r, int full_r, int32_t sad_threshold, int audit_stride, int32_t* mv,
+                                     unsigned long long* audit_sums, int32_t* n_fallback, const MeFinishBuffers& b,
+                                     const MeAudit& audit, cudaStream_t st);
 
 }  // namespace umi
