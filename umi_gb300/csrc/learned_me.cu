@@ -702,7 +702,11 @@ AuxStream* aux_stream(cudaStream_t st) {
 	AuxStream& a = aux[dev];
 	if (a.s && a.fork && a.join) return &a;
 	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-	if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
+	if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+		cudaGetLastError();  // not an error of this call: the stage runs in order on st
+		return nullptr;
+	}
+	if (cs != cudaStreamCaptureStatusNone) return nullptr;
 	if (!a.s && cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking) != cudaSuccess) a.s = nullptr;
 	if (!a.fork && cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming) != cudaSuccess) a.fork = nullptr;
 	if (!a.join && cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming) != cudaSuccess) a.join = nullptr;
