@@ -843,9 +843,9 @@ class VideoY4M:
         self.d_mv = [torch.empty((self.nblk, 3), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
         self.d_sums = [torch.zeros(2, dtype=torch.int64, device=dev) for _ in range(self.n_rot)]
         self.d_nf = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
-        # audit list + audit search (second stream) + cells + search + refine + flag + fallback list
-        # search + audit merge
-        self.launches_per_step = 8
+        # cells + search + refine + flag + one list search (the 126 audited blocks, fewer than the
+        # SMs, join the fallback blocks' list) + audit sum
+        self.launches_per_step = 6
 
     def _pair(self, j):
         self.cme.estimate(self.d[j + 1], self.d[j], self.REFINE_R, self.FULL_R, self.thr, self.AUDIT,

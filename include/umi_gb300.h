@@ -3,8 +3,10 @@
  * Everything here is plain C: raw device pointers, sizes, and a CUDA stream
  * passed as `void*` (a cudaStream_t; NULL = the legacy default stream).  All
  * entry points are asynchronous on that stream, never allocate device memory
- * unless stated, keep no mutable global state, and report failures by status
- * code (the reference aborts or ignores CUDA errors instead).
+ * unless stated, keep no mutable global state beyond what is stated (the
+ * built-in scratch of umi_iimg_u8_i32_noalloc, the per-thread second stream
+ * of the motion-estimation pipelines), and report failures by status code
+ * (the reference aborts or ignores CUDA errors instead).
  *
  * The reference exposes one templated entry point, UMI::Execute
  * (src/UMI_gpu.h:409-623).  Its two halves map onto this library as:
@@ -264,10 +266,12 @@ umi_status umi_menet_adam(float* params, const float* grads, float* m, float* v,
  * +-full_r around (0, 0).  mv receives (mv_y, mv_x, sad) per block as
  * umi_full_me_u8 with b = 16; n_fallback (device, may be NULL) the number of
  * fallback blocks.  1 <= refine_r <= full_r <= 64.  The audit's exhaustive
- * search does not depend on the proposal: it runs on a second stream of the
- * calling host thread (one per device, made on the first call outside a
- * stream capture), forked from `stream` at entry and joined back before the
- * call's last work on `stream`; stream order and capture are kept. */
+ * search does not depend on the proposal: when it has at least as many
+ * blocks as the GPU has SMs, it runs on a second stream of the calling host
+ * thread (one per device, made on the first call outside a stream capture),
+ * forked from `stream` at entry and joined back before the call's last work
+ * on `stream`; stream order and capture are kept.  A smaller audit joins the
+ * fallback blocks' exhaustive search. */
 umi_status umi_me_learned_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, const float* params,
                              int32_t refine_r, int32_t full_r, int32_t sad_threshold, int32_t audit_stride,
                              int32_t* mv, unsigned long long* audit_sums, int32_t* n_fallback, void* workspace,

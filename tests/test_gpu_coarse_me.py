@@ -93,21 +93,23 @@ def test_coarse_entry_refine_audit_fallback(umi, dev):
     assert np.mean(refined_np[:, 2] == full_np[:, 2]) > 0.9
 
 
-def _estimate_into(cme, c, r, outs):
-    cme.estimate(c, r, 4, 31, sad_threshold=450, audit_stride=5, out=outs[0], audit_sums=outs[1], n_fallback=outs[2])
+def _estimate_into(cme, c, r, outs, stride):
+    cme.estimate(c, r, 4, 31, sad_threshold=450, audit_stride=stride, out=outs[0], audit_sums=outs[1],
+                 n_fallback=outs[2])
 
 
-def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev):
-    """The audit's exhaustive search runs on the calling thread's second
-    stream (forked and joined inside the call): the results are the same
-    eagerly, replayed from a CUDA graph that captured the fork, and when the
-    first call of a fresh host thread is itself captured (no second stream
-    yet: everything in order on the captured stream)."""
+@pytest.mark.parametrize("h,w,stride", [(192, 256, 5), (384, 512, 3)])
+def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev, h, w, stride):
+    """An audit of fewer blocks than SMs (39 here) joins the fallback
+    blocks' list search; a larger one (256) runs on the calling thread's
+    second stream, forked and joined inside the call.  The results are the
+    same eagerly, replayed from a CUDA graph that captured the call, and when
+    the first call of a fresh host thread is itself captured (no second
+    stream yet: everything in order on the captured stream)."""
     import threading
 
     import torch
     from umi_gb300.workloads import me_pair
-    h, w = 192, 256
     cur, ref, _ = me_pair(seed=9, h=h, w=w, shift_sigma=12.0, max_shift=30)
     c, r = _t(cur, dev), _t(ref, dev)
     nblk = (h // 16) * (w // 16)
@@ -120,7 +122,7 @@ def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev):
     # the definition, from the separate calls
     full = umi.full_me_u8(c, r, 16, 31)
     refined = umi.full_me_u8(c, r, 16, 4, centers=cme.centers(c, r, 26))
-    aud = torch.arange(0, nblk, 5, device=dev)
+    aud = torch.arange(0, nblk, stride, device=dev)
     want = refined.clone()
     rest = torch.ones(nblk, dtype=torch.bool, device=dev)
     rest[aud] = False
@@ -135,14 +137,14 @@ def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev):
         assert o[1].tolist() == want_sums and int(o[2].item()) == want_nf
 
     eager = outs()
-    _estimate_into(cme, c, r, eager)
+    _estimate_into(cme, c, r, eager, stride)
     torch.cuda.synchronize()
     check(eager)
 
     graphed = outs()
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
-        _estimate_into(cme, c, r, graphed)
+        _estimate_into(cme, c, r, graphed, stride)
     for _ in range(2):
         g.replay()
     torch.cuda.synchronize()
@@ -156,10 +158,10 @@ def test_coarse_audit_stream_fork_eager_graph_and_fresh_thread(umi, dev):
             o = outs()
             g2 = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g2):
-                _estimate_into(cme, c, r, o)  # this thread's first call: captured in order
+                _estimate_into(cme, c, r, o, stride)  # this thread's first call: captured in order
             g2.replay()
             o2 = outs()
-            _estimate_into(cme, c, r, o2)  # eager: the thread's second stream is made now
+            _estimate_into(cme, c, r, o2, stride)  # eager: the thread's second stream is made now
             torch.cuda.synchronize()
             result["captured"], result["eager"] = o, o2
         except Exception as e:  # surfaced below

@@ -360,14 +360,38 @@ __global__ void centers_kernel(const float* __restrict__ pred, int32_t* __restri
 	}
 }
 
-// Fallback list: every block other than the audited ones (0, stride,
-// 2 stride, ...) whose refined SAD exceeds the threshold; count[0] is its
-// length.  List order is the order of discovery; the search is per block, so
-// the order changes no result.
-__global__ void flag_kernel(const int32_t* __restrict__ mv, int n, int stride, int32_t thr,
-                            int32_t* __restrict__ list, int32_t* __restrict__ count) {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-		if (!(stride > 0 && i % stride == 0) && mv[3 * i + 2] > thr) list[atomicAdd(count, 1)] = i;
+// List for the exhaustive search: every block other than the audited ones
+// (0, stride, 2 stride, ...) whose refined SAD exceeds the threshold
+// (counted in count[1]), and, when `with_audit`, the audited blocks too
+// (their refined SAD goes to audit_sums[0]).  count[0] is the list length.
+// List order is the order of discovery; the search is per block, so the
+// order changes no result.
+__global__ void flag_kernel(const int32_t* __restrict__ mv, int n, int stride, int32_t thr, bool with_audit,
+                            int32_t* __restrict__ list, int32_t* __restrict__ count,
+                            unsigned long long* __restrict__ audit_sums) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		if (stride > 0 && i % stride == 0) {
+			if (with_audit) {
+				if (audit_sums) atomicAdd(audit_sums, (unsigned long long)mv[3 * i + 2]);
+				list[atomicAdd(count, 1)] = i;
+			}
+		} else if (mv[3 * i + 2] > thr) {
+			list[atomicAdd(count, 1)] = i;
+			atomicAdd(count + 1, 1);
+		}
+	}
+}
+
+// audit_sums[1] += exhaustive SAD of the audited blocks, searched in the
+// same list as the fallback blocks.
+__global__ void audit_sum_kernel(const int32_t* __restrict__ mv, int n, int stride,
+                                 unsigned long long* __restrict__ audit_sums) {
+	const int na = (n + stride - 1) / stride;
+	unsigned long long s = 0;
+	for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x)
+		s += (unsigned long long)mv[3 * (size_t)a * stride + 2];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if ((threadIdx.x & 31) == 0 && s) atomicAdd(audit_sums + 1, s);
 }
 
 // alist = 0, stride, 2 stride, ... (*acount = their number).
@@ -722,6 +746,17 @@ umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, 
 	const int nblk = (h / 16) * (w / 16);
 	if (audit_stride <= 0 || nblk == 0) return UMI_OK;
 	audit->active = true;
+	// A +-64 list search runs one block per SM at a time.  An audit of fewer
+	// blocks than SMs leaves room in the fallback search's round, so it joins
+	// that list; a larger one runs apart, beside the proposal.
+	const int na = ceil_div(nblk, audit_stride);
+	int dev = 0, sms = 0;
+	UMI_TRY(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	if (na < sms) {
+		audit->combined = true;
+		return UMI_OK;
+	}
 	AuxStream* aux = aux_stream(st);
 	cudaStream_t as = st;
 	if (aux) {
@@ -729,7 +764,6 @@ umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, 
 		UMI_TRY(cuda_status(cudaStreamWaitEvent(aux->s, aux->fork, 0), "cudaStreamWaitEvent"));
 		as = aux->s;
 	}
-	const int na = ceil_div(nblk, audit_stride);
 	audit_list_kernel<<<grid_for(na), NT, 0, as>>>(b.alist, b.count + 2, nblk, audit_stride);
 	UMI_TRY(launch_status("audit_list_kernel"));
 	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 2, na, b.amv, as));
@@ -752,20 +786,24 @@ umi_status me_refine_fallback_finish(const uint8_t* cur, const uint8_t* ref, int
 	const int nblk = (h / 16) * (w / 16);
 	void* stream = st;
 	UMI_TRY(umi_full_me_u8(cur, ref, h, w, 16, refine_r, centers, mv, stream));
-	UMI_TRY(cuda_status(cudaMemsetAsync(b.count, 0, sizeof(int32_t), st), "cudaMemsetAsync"));
-	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, nblk, audit.active ? audit_stride : 0, sad_threshold, b.list, b.count);
-	UMI_TRY(launch_status("flag_kernel"));
-	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.list, b.count, nblk, mv, stream));
+	UMI_TRY(cuda_status(cudaMemsetAsync(b.count, 0, 2 * sizeof(int32_t), st), "cudaMemsetAsync"));
 	if (audit_sums)
 		UMI_TRY(cuda_status(cudaMemsetAsync(audit_sums, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync"));
-	if (audit.active) {
+	flag_kernel<<<grid_for(nblk), NT, 0, st>>>(mv, nblk, audit.active ? audit_stride : 0, sad_threshold, audit.combined,
+	                                           b.list, b.count, audit_sums);
+	UMI_TRY(launch_status("flag_kernel"));
+	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.list, b.count, nblk, mv, stream));
+	if (audit.combined && audit_sums) {
+		audit_sum_kernel<<<grid_for(ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, nblk, audit_stride, audit_sums);
+		UMI_TRY(launch_status("audit_sum_kernel"));
+	} else if (audit.active && !audit.combined) {
 		if (audit.forked) UMI_TRY(cuda_status(cudaStreamWaitEvent(st, audit.done, 0), "cudaStreamWaitEvent"));
 		audit_merge_kernel<<<grid_for(ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, b.amv, nblk, audit_stride,
 		                                                                          audit_sums);
 		UMI_TRY(launch_status("audit_merge_kernel"));
 	}
 	if (n_fallback)
-		UMI_TRY(cuda_status(cudaMemcpyAsync(n_fallback, b.count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
+		UMI_TRY(cuda_status(cudaMemcpyAsync(n_fallback, b.count + 1, sizeof(int32_t), cudaMemcpyDeviceToDevice, st),
 		                    "cudaMemcpyAsync"));
 	return ok();
 }

@@ -13,24 +13,28 @@ namespace umi {
 
 // Device scratch of the shared stage, nblk = (h/16)(w/16) blocks.
 struct MeFinishBuffers {
-	int32_t* list;   // nblk: fallback blocks
-	int32_t* count;  // 4: [0] fallback blocks, [2] audited blocks
+	int32_t* list;   // nblk: fallback blocks (and audited blocks when the audit is combined)
+	int32_t* count;  // 4: [0] list length, [1] fallback blocks, [2] audited blocks (audit apart)
 	int32_t* alist;  // nblk: audited blocks 0, stride, 2 stride, ...
 	int32_t* amv;    // 3 nblk: exhaustive results, written at the audited blocks' rows only
 };
 
-// The audit's exhaustive search, started before the proposal so that it can
-// run beside it: `forked` when it went to the calling thread's second stream
-// on this device (joined by `done`), else it ran in order on the caller's
-// stream.
+// The audit's exhaustive search.  An audit of fewer blocks than SMs is
+// `combined`: its blocks join the fallback blocks' list search after the
+// refine (one round holds both).  A larger one is started before the
+// proposal, so that it can run beside it: `forked` when it went to the
+// calling thread's second stream on this device (joined by `done`), else
+// in order on the caller's stream.
 struct MeAudit {
 	bool active = false;
+	bool combined = false;
 	bool forked = false;
 	cudaEvent_t done = nullptr;
 };
 
 // Audit: every audit_stride-th block (0: none) is searched exhaustively in
-// +-full_r into b.amv.  Call before the proposal, on the proposal's stream.
+// +-full_r (into b.amv when not combined).  Call before the proposal, on
+// the proposal's stream.
 umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, int full_r, int audit_stride,
                           const MeFinishBuffers& b, cudaStream_t st, MeAudit* audit);
 
