@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(PKG, "libumi_gb300.so")
 HEADER = os.path.join(ROOT, "include", "umi_gb300.h")
 
 UMI_OK = 0
+UMI_ERR_UNSUPPORTED = 3
 STATUS_NAMES = {
     0: "UMI_OK", 1: "UMI_ERR_INVALID_DESC", 2: "UMI_ERR_INVALID_ARG", 3: "UMI_ERR_UNSUPPORTED",
     4: "UMI_ERR_CUDA", 5: "UMI_ERR_NO_MEMORY", 6: "UMI_ERR_TIMEOUT",

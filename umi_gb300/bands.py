@@ -95,7 +95,7 @@ def iimg_band_local(img, world: int, rank: int, stream=None):
     import torch
     h, w = img.shape
     if h * w > (1 << 31) // 255:
-        raise U.UmiError(3, "iimg_band", f"{h}x{w} frame: sums could exceed int32")
+        raise U.UmiError(U.UMI_ERR_UNSUPPORTED, "iimg_band", f"{h}x{w} frame: sums could exceed int32")
     y0, y1 = split(h, world, rank)
     if y1 == y0:
         return torch.empty((0, w), dtype=torch.int32, device=img.device)
