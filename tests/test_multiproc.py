@@ -68,3 +68,26 @@ def test_single_process_dist_is_identity():
         d.done()
     finally:
         os.environ.update(env)
+
+
+WORKLOADS = ["int_pair_1080p", "filter3x3_1024", "batched_uneven", "gemm_4096", "fprop_n32", "learned_me_4k",
+             "coarse_me_4k", "video_y4m_1080p", "apps_1080p", "serve_bilateral_8x512"]
+
+
+@pytest.mark.parametrize("workload", WORKLOADS)
+def test_reference_arm_line_per_workload(workload):
+    """Every workload's reference arm (the reference's CPU path, restated in
+    the oracle) prints one line with the keys of the bench contract, on the
+    same metric and config as the GPU arm."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", workload,
+           "--steps", "1", "--warmup", "0"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline", "gpu_launches"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["config"]["workload"] == workload and d["value"] > 0
+    assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] in ("port", "reference")
