@@ -44,7 +44,9 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # volume's traffic grows with the pixel count, so it is kept per pixel and
 # scaled to the configured batch.
 NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
-               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None, "coarse_me_4k": None,
+               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None,
+               # the proposal: cells kernel (both frames read once) + coarse search (planes and cells)
+               "coarse_me_4k": (16615680 + 0) + (2795520 + 0),
                "video_y4m_1080p": None, "apps_1080p": None, "serve_bilateral_8x512": None}
 NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 + 3253943000) / 12896910}
 
