@@ -38,17 +38,33 @@ sys.path.insert(0, ROOT)
 
 L2_BYTES = 129 * 2 ** 20
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
-# from the ncu captures summarised under profiles/ (None where not captured).
-# batched_uneven was captured on its 8-image case (12 896 910 px): the cost
-# volume's traffic grows with the pixel count, so it is kept per pixel and
-# scaled to the configured batch.
-NCU_TRAFFIC = {"int_pair_1080p": 4197632 + 0, "filter3x3_1024": 4204544 + 0, "gemm_4096": 76233472 + 35101184,
-               "fprop_n32": 67321088 + 206541312, "learned_me_4k": None,
+# (dram__bytes_read.sum, dram__bytes_write.sum) per launch of the dominant
+# kernel, from the ncu captures summarised under profiles/ (None where not
+# captured).  batched_uneven was captured on its 8-image case (12 896 910 px):
+# the cost volume's traffic grows with the pixel count, so it is kept per
+# pixel and scaled to the configured batch.
+NCU_TRAFFIC = {"int_pair_1080p": (4197632, 0), "filter3x3_1024": (4204544, 0), "gemm_4096": (76233472, 35101184),
+               "fprop_n32": (67321088, 206541312), "learned_me_4k": None,
                # the proposal: cells kernel (both frames read once) + coarse search (planes and cells)
-               "coarse_me_4k": (16615680 + 0) + (2795520 + 0),
+               "coarse_me_4k": (16615680 + 2795520, 0),
                "video_y4m_1080p": None, "apps_1080p": None, "serve_bilateral_8x512": None}
-NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 + 3253943000) / 12896910}
+NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 / 12896910, 3253943000 / 12896910)}
+
+
+def traffic_fields(rw, alg_write_bytes=None):
+    """`traffic` = DRAM read + write bytes per launch (ncu), with the two
+    counters beside it.  dram__bytes_write counts only the lines written back
+    to DRAM while the launch runs: an output that is still dirty in L2 when
+    the kernel ends is not counted, so a write figure below the algorithmic
+    output bytes is flagged instead of being read as saved traffic."""
+    if rw is None:
+        return {"traffic": None}
+    r, w = rw
+    d = {"traffic": r + w, "traffic_read": r, "traffic_write": w}
+    if alg_write_bytes and w < 0.9 * alg_write_bytes:
+        d["traffic_note"] = (f"dram__bytes_write {w:.0f} B < {alg_write_bytes:.0f} B of output: "
+                             "the rest was still dirty in L2 at kernel end (written back after the launch)")
+    return d
 
 
 def parse():
@@ -1202,6 +1218,26 @@ def copy_gbs(dev, nbytes: int, n: int = 400) -> float:
 
 
 # --------------------------------------------------------------------- arms
+def sad4_peak(dev):
+    """Denominator of the integer-pipe roofline (byte absdiffs/s) and its
+    source: the larger of the measured throughput of a loop of nothing but
+    `vabsdiff4.add` (probe/sad4_peak.cu) and the issue-rate figure 64 SAD
+    instructions/clk/SM x 4 bytes x SMs x the maximum SM clock (the ALU pipe
+    takes a 32-lane warp instruction every 2 cycles per sub-partition)."""
+    import torch
+    measured = probe_sad4_peak(dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = 2070.0
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        mhz = float(json.load(open(path)).get("sm_max_mhz", mhz))
+    derived = 64 * 4 * sms * mhz * 1e6
+    peak = max(measured, derived)
+    src = (f"max(measured vabsdiff4.add loop {measured / 1e9:.0f} G/s (probe/libumi_probe.so), "
+           f"issue rate 64/clk/SM x 4 B x {sms} SMs x {mhz:.0f} MHz = {derived / 1e9:.0f} G/s)")
+    return peak, src
+
+
 def probe_sad4_peak(dev):
     """Measured throughput (byte absdiffs/s) of the packed SAD instruction."""
     import ctypes
@@ -1373,12 +1409,11 @@ def run_ours(args, wl, dist):
     kms, absdiff, hbm_bytes = wl.kernels(dev, pk)
     kernels = {}
     if isinstance(wl, IntPair):
-        sad_peak = probe_sad4_peak(dev)
+        sad_peak, sad_src = sad4_peak(dev)
         ach = absdiff / (kms["full_me_u8"] * 1e-3)
         roof = {"bound": "int", "kernel": "full_me_u8", "achieved": ach / 1e9, "peak": sad_peak / 1e9,
-                "unit": "Gabsdiff/s", "frac": ach / sad_peak, "traffic": NCU_TRAFFIC[wl.name],
-                "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
-                "work_per_launch": absdiff, "ms_per_launch": kms["full_me_u8"]}
+                "unit": "Gabsdiff/s", "frac": ach / sad_peak, **traffic_fields(NCU_TRAFFIC[wl.name]),
+                "peak_source": sad_src, "work_per_launch": absdiff, "ms_per_launch": kms["full_me_u8"]}
         ig = hbm_bytes / (kms["iimg_u8_i32"] * 1e-3) / 1e9
         cg = copy_gbs(dev, hbm_bytes)
         kernels["iimg_u8_i32"] = {"ms_per_launch": kms["iimg_u8_i32"], "achieved": ig, "unit": "GB/s",
@@ -1394,7 +1429,7 @@ def run_ours(args, wl, dist):
                              if name == "gemm_f32_bf16x3" else None}
         kernels["gemm_f32_bf16x3"]["fp32_gemm_tflops"] = wl.flops / (kms["gemm_f32_bf16x3"] * 1e-3) / 1e12
         roof = dict(kernels["gemm_bf16"], bound="tensor", kernel="gemm_tc_kernel (bf16)", peak=pk["bf16_tflops"],
-                    traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
+                    **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.M * wl.N), peak_source=pk["source"] + " (burst)",
                     flops_per_launch=wl.flops)
     elif isinstance(wl, Fprop):
         kt = kms["conv2d_fprop_bf16"]
@@ -1410,15 +1445,17 @@ def run_ours(args, wl, dist):
         k = kernels["conv2d_fprop_bf16"]
         if k["hbm_floor_ms"] >= k["tensor_floor_ms"]:  # the fp32 output makes the launch HBM-bound
             roof = {"bound": "hbm", "kernel": "tc_kernel<conv> (bf16)", "achieved": gbs, "peak": pk["hbm_gbs"],
-                    "unit": "GB/s", "frac": gbs / pk["hbm_gbs"], "traffic": NCU_TRAFFIC.get(wl.name),
+                    "unit": "GB/s", "frac": gbs / pk["hbm_gbs"],
+                    **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.N * wl.K * wl.H * wl.W),
                     "peak_source": pk["source"], "bytes_per_launch": nbytes, "ms_per_launch": kt,
                     "tensor_frac": k["frac"]}
         else:
             roof = dict(k, bound="tensor", kernel="tc_kernel<conv> (bf16)", peak=pk["bf16_tflops"],
-                        traffic=NCU_TRAFFIC.get(wl.name), peak_source=pk["source"] + " (burst)",
+                        **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.N * wl.K * wl.H * wl.W),
+                        peak_source=pk["source"] + " (burst)",
                         flops_per_launch=wl.flops)
     elif isinstance(wl, LearnedMe):
-        sad_peak = probe_sad4_peak(dev)
+        sad_peak, sad_src = sad4_peak(dev)
         for name, kt in kms.items():
             kernels[name] = {"ms_per_launch": kt, "Mblocks_per_s": wl.nblk / (kt * 1e-3) / 1e6}
         kernels["speedup_learned_vs_full_search"] = kms["full_me_u8_r64"] / kms["me_learned_u8"]
@@ -1430,8 +1467,7 @@ def run_ours(args, wl, dist):
         ach = absdiff / (kms[roof_k] * 1e-3)
         roof = {"bound": "int", "kernel": roof_name, "achieved": ach / 1e9,
                 "peak": sad_peak / 1e9, "unit": "Gabsdiff/s", "frac": ach / sad_peak,
-                "traffic": NCU_TRAFFIC[wl.name],
-                "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
+                **traffic_fields(NCU_TRAFFIC[wl.name]), "peak_source": sad_src,
                 "work_per_launch": absdiff, "ms_per_launch": kms[roof_k]}
     elif isinstance(wl, ServeBilateral):
         kt = kms["bilateral_batch"]
@@ -1452,14 +1488,14 @@ def run_ours(args, wl, dist):
                     peak_source=pk["source"], size_matched_copy_gbs=cg,
                     frac_of_size_matched_copy=kernels[dom]["achieved"] / cg)
     elif isinstance(wl, VideoY4M):
-        sad_peak = probe_sad4_peak(dev)
+        sad_peak, sad_src = sad4_peak(dev)
         for name, kt in kms.items():
             kernels[name] = {"ms_per_launch": kt, "pairs_per_s": 1e3 / kt}
         kernels["speedup_coarse_vs_full_search"] = kms["full_me_u8_r64"] / kms["me_coarse_u8"]
         ach = absdiff / (kms["coarse_centers"] * 1e-3)
         roof = {"bound": "int", "kernel": "coarse_cells + coarse_search (the proposal)", "achieved": ach / 1e9,
                 "peak": sad_peak / 1e9, "unit": "Gabsdiff/s", "frac": ach / sad_peak, "traffic": None,
-                "peak_source": "measured: vabsdiff4.add throughput probe (libumi_probe.so) on this GPU",
+                "peak_source": sad_src,
                 "work_per_launch": absdiff, "ms_per_launch": kms["coarse_centers"]}
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
@@ -1468,15 +1504,17 @@ def run_ours(args, wl, dist):
                              "frac": b / (kt * 1e-3) / 1e9 / pk["hbm_gbs"], "bytes_per_launch": b}
         kernels["bilateral"]["ex2_per_s"] = 25 * wl.px / (kms["bilateral"] * 1e-3)
         dom = max(kms, key=kms.get)
+        pp = NCU_TRAFFIC_PER_PX["batched_uneven"]
         roof = dict(kernels[dom], bound="hbm", kernel=dom, peak=pk["hbm_gbs"],
-                    traffic=NCU_TRAFFIC_PER_PX["batched_uneven"] * wl.px if dom == "cost_volume" else None,
+                    **traffic_fields((pp[0] * wl.px, pp[1] * wl.px) if dom == "cost_volume" else None,
+                                     256 * wl.px if dom == "cost_volume" else None),
                     peak_source=pk["source"])
     else:
         ach = hbm_bytes / (kms["filter3x3_f32"] * 1e-3) / 1e9
         cg = copy_gbs(dev, hbm_bytes)
         roof = {"bound": "hbm", "kernel": "filter3x3_f32", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": ach / pk["hbm_gbs"], "traffic": NCU_TRAFFIC[wl.name], "peak_source": pk["source"],
-                "bytes_per_launch": hbm_bytes, "ms_per_launch": kms["filter3x3_f32"],
+                "frac": ach / pk["hbm_gbs"], **traffic_fields(NCU_TRAFFIC[wl.name], hbm_bytes // 2),
+                "peak_source": pk["source"], "bytes_per_launch": hbm_bytes, "ms_per_launch": kms["filter3x3_f32"],
                 "size_matched_copy_gbs": cg, "frac_of_size_matched_copy": ach / cg}
 
     line = {

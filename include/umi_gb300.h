@@ -186,13 +186,19 @@ umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w
  * (1 MiB) per GPU, held until the process exits; frames whose tile sums
  * (int32 per row per 256-column tile, per column per 64-row tile and per
  * tile, each array rounded up to 256 bytes) exceed it are rejected with
- * UMI_ERR_NO_MEMORY (3840x2160 and 4096x2160 fit); at most 4096 rows.  The first call on a
- * device looks up the scratch address (cudaGetSymbolAddress) with that
- * device current: make it before any stream capture.  All calls share the
- * scratch: calls that overlap on the GPU race and must be serialised by the
- * caller.  Allocates nothing. */
+ * UMI_ERR_NO_MEMORY; at most 4096 rows.  The int32 limit of
+ * umi_iimg_u8_i32 applies too (h*w*255 < 2^31: about 8.42 Mpx, so 3840x2160
+ * is served and 4096x2160 is refused with UMI_ERR_UNSUPPORTED).  The first
+ * call in a CUDA context looks up the scratch address (cudaGetSymbolAddress)
+ * with that context current and caches it per context: make it before any
+ * stream capture.  All calls share the scratch: calls that overlap on the
+ * GPU race and must be serialised by the caller.  Allocates nothing. */
 #define UMI_IIMG_NOALLOC_SCRATCH_BYTES (1u << 20)
 umi_status umi_iimg_u8_i32_noalloc(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* stream);
+/* Drops the cached scratch addresses of umi_iimg_u8_i32_noalloc: call it
+ * after a context it served was destroyed (cudaDeviceReset), before the next
+ * call.  No counterpart in the reference. */
+void umi_iimg_noalloc_forget(void);
 
 /* Full-search block motion estimation with fused argmin, uint8 frames.
  * For every b x b block of `cur` (blocks truncated at the frame edge:
@@ -334,6 +340,19 @@ umi_status umi_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int3
                          void* stream);
 umi_status umi_gemm_f16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t* err,
                         void* stream);
+/* Failure-path hook, no counterpart in the reference: umi_gemm_bf16 with the
+ * epilogue's bounded wait for each finished accumulator limited to
+ * epilogue_wait_ns nanoseconds instead of 1 s.  A limit shorter than one
+ * tile's MMAs makes that wait give up: the kernel records error bit 4 in
+ * *err, every role stops, the producer's copies and the issued MMAs drain,
+ * TMEM is freed and the kernel returns (C is then unspecified), leaving the
+ * context usable.  Used by the tests of the timeout path. */
+umi_status umi_gemm_bf16_wait_limit(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K,
+                                    int32_t* err, unsigned long long epilogue_wait_ns, void* stream);
+/* Maps the error bits a kernel left in its `err` word (read back by the
+ * caller after the stream finished) to a status: UMI_OK for 0, else
+ * UMI_ERR_TIMEOUT with the bits named in umi_last_error_string(). */
+umi_status umi_err_status(int32_t err_bits);
 /* FP32 GEMM emulated on the bf16 tensor cores by operand splitting (bf16x3:
  * A = A_hi + A_lo, B = B_hi + B_lo, C = A_hi B_hi + A_lo B_hi + A_hi B_lo, fp32
  * accumulation; Henry, Tang & Heinecke, ARITH 2019).  A is (M,K), B is (N,K),

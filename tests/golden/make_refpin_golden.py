@@ -1,7 +1,7 @@
 """Generate tests/golden/refpin.json from the reference's own example programs.
 
-Run in a checkout where the reference sources are available (default
-/root/reference, override with UMI_REFERENCE):
+Run in a checkout where the reference sources are available (the directory
+named by UMI_REFERENCE, else `reference` beside this repository):
 
     python tests/golden/make_refpin_golden.py
 
@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 
-REF = os.environ.get("UMI_REFERENCE", "/root/reference")
+REF = os.environ.get("UMI_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 # Parameters and inputs of each example program (main/<app>.cu).
 APPS = {

@@ -9,7 +9,7 @@ from concurrent.futures import ThreadPoolExecutor
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("UMI_REFERENCE", "/root/reference")
+REF = os.environ.get("UMI_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 APPS = ["filter3x3", "wfilter3x3", "bilateral", "cost_volume", "full_me", "iimg", "gemm", "fprop"]
 
 

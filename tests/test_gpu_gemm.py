@@ -94,3 +94,81 @@ def test_conv2d_fprop_bf16_benchmark_shape_sampled(umi, dev):
     scale = torch.nn.functional.conv2d(xd.double().abs(), wd.double().abs(), padding=1)
     rel = ((got.double() - want).abs() / scale.clamp_min(1e-30)).max().item()
     assert rel <= 1e-5, rel
+
+
+# ---------------------------------------------------------------- config size: the persistent multi-tile path
+def _sampled_rows_cols(orc, a, b, C, tol, nsample=64, seed=0):
+    """Complete rows and columns of C (nsample of each, plus the first and last
+    of each) against the FP64 product of the same inputs."""
+    M, N = C.shape
+    g = np.random.default_rng(seed)
+    rows = np.unique(np.concatenate([[0, M - 1], g.choice(M, nsample, replace=False)]))
+    cols = np.unique(np.concatenate([[0, N - 1], g.choice(N, nsample, replace=False)]))
+    want_r = orc.gemm_f64(a[rows], b, b_is_nk=True)
+    scale_r = orc.gemm_f64(np.abs(a[rows]), np.abs(b), b_is_nk=True)
+    _check(C[rows], want_r, scale_r, tol)
+    want_c = orc.gemm_f64(a, b[cols], b_is_nk=True)
+    scale_c = orc.gemm_f64(np.abs(a), np.abs(b[cols]), b_is_nk=True)
+    _check(C[:, cols], want_c, scale_c, tol)
+    return want_r, rows
+
+
+@pytest.mark.parametrize("dt", ["bf16", "f16"])
+def test_gemm_half_4096_cubed(umi, orc, dev, dt):
+    """M = N = K = 4096: 512 tiles of 128 x 256 over the persistent CTAs, so
+    every CTA reuses both TMEM accumulators several times (the ping-pong
+    between the MMA issuer and the epilogue)."""
+    import torch
+    M = N = K = 4096
+    g = torch.Generator(device="cpu").manual_seed(4096 + (dt == "f16"))
+    tdt = torch.bfloat16 if dt == "bf16" else torch.float16
+    A = torch.randn(M, K, generator=g).to(tdt)
+    B = torch.randn(N, K, generator=g).to(tdt)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    C = umi.gemm(A.to(dev), B.to(dev), err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    assert np.isfinite(C).all()
+    _sampled_rows_cols(orc, A.float().numpy(), B.float().numpy(), C, 1e-5)
+
+
+def test_gemm_f32_bf16x3_2048(umi, orc, dev):
+    import torch
+    M = N = K = 2048
+    g = np.random.default_rng(2048)
+    a = g.standard_normal((M, K)).astype(np.float32)
+    b = g.standard_normal((N, K)).astype(np.float32)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    C = umi.gemm_f32_bf16x3(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev), err=err).cpu().numpy()
+    assert int(err.item()) == 0
+    _sampled_rows_cols(orc, a, b, C, 1e-4)
+
+
+# ---------------------------------------------------------------- the bounded-wait timeout path
+def test_gemm_epilogue_wait_times_out_and_context_stays_usable(umi, orc, dev):
+    """A 1 us limit on the epilogue's wait for the first finished accumulator
+    (one 128 x 256 tile with K = 4096 takes ~20 us of MMAs) makes that bounded
+    wait give up: the error bit 4 comes back, umi_err_status maps it to
+    UMI_ERR_TIMEOUT, the kernel returns (its copies and MMAs drained, TMEM
+    freed), and the next normal call on the same stream is correct."""
+    import torch
+    M = N = K = 4096
+    g = torch.Generator(device="cpu").manual_seed(77)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).to(dev)
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).to(dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    umi.gemm_bf16_wait_limit(A, B, 1000, err=err)
+    torch.cuda.synchronize()
+    bits = int(err.item())
+    assert bits & 4, bits
+    assert bits & ~15 == 0, bits
+    with pytest.raises(umi.UmiError) as ei:
+        umi.check_err(err, "umi_gemm_bf16_wait_limit")
+    assert "UMI_ERR_TIMEOUT" in str(ei.value)
+    # the same stream, a normal call: no error bits, correct rows
+    err.zero_()
+    C = umi.gemm(A, B, err=err)
+    umi.check_err(err, "umi_gemm_bf16")
+    rows = [0, 1234, 4095]
+    a, b = A[rows].float().cpu().numpy(), B.float().cpu().numpy()
+    _check(C[rows].cpu().numpy(), orc.gemm_f64(a, b, b_is_nk=True), orc.gemm_f64(np.abs(a), np.abs(b), b_is_nk=True),
+           1e-5)

@@ -55,7 +55,7 @@ def test_fprop_input_stream(orc):
 
 
 REFPIN = os.path.join(ROOT, "oracle", "_ref")
-REF_SRC = os.environ.get("UMI_REFERENCE", "/root/reference")
+REF_SRC = os.environ.get("UMI_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF_SRC, "main")), reason="reference sources not present")

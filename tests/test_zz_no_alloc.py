@@ -41,3 +41,19 @@ def test_noalloc_rejects_frames_beyond_the_scratch(umi, dev):
     out = torch.empty((4096, 4096), dtype=torch.int32, device=dev)
     assert _call(umi, x, out) == 5  # UMI_ERR_NO_MEMORY
     assert b"scratch" in umi.lib().umi_last_error_string()
+
+
+def test_noalloc_refuses_what_the_int32_limit_refuses(umi, dev):
+    """4096x2160 tile sums fit the 1 MiB scratch, but h*w*255 >= 2^31: the
+    same int32 limit as umi_iimg_u8_i32 refuses it (UMI_ERR_UNSUPPORTED);
+    3840x2160 (just under the limit) is served."""
+    import torch
+    x = torch.zeros((2160, 4096), dtype=torch.uint8, device=dev)
+    out = torch.empty((2160, 4096), dtype=torch.int32, device=dev)
+    assert _call(umi, x, out) == 3  # UMI_ERR_UNSUPPORTED
+    assert b"int32" in umi.lib().umi_last_error_string()
+    x = torch.full((2160, 3840), 255, dtype=torch.uint8, device=dev)
+    got = torch.empty((2160, 3840), dtype=torch.int32, device=dev)
+    assert _call(umi, x, got) == 0
+    torch.cuda.synchronize()
+    assert int(got[-1, -1].item()) == 2160 * 3840 * 255

@@ -62,6 +62,7 @@ SIGNATURES = {
     "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
     "umi_iimg_u8_i32": ([_vp, _vp, _i32, _i32, _vp, _sz, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_noalloc": ([_vp, _vp, _i32, _i32, _vp], ctypes.c_int),
+    "umi_iimg_noalloc_forget": ([], None),
     "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_full_me_u8_list": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp], ctypes.c_int),
@@ -81,6 +82,8 @@ SIGNATURES = {
     "umi_cost_volume_dot_f32": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
     "umi_gemm_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_gemm_f16": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_gemm_bf16_wait_limit": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, ctypes.c_ulonglong, _vp], ctypes.c_int),
+    "umi_err_status": ([_i32], ctypes.c_int),
     "umi_gemm_f32_bf16x3_workspace_bytes": ([_i32, _i32, _i32], _sz),
     "umi_gemm_f32_bf16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _sz, _vp, _vp], ctypes.c_int),
     "umi_conv2d_fprop_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
@@ -648,6 +651,28 @@ def gemm(A, B, out=None, err=None, stream=None):
     _need(out, torch.float32, "out")
     fn = lib().umi_gemm_bf16 if A.dtype == torch.bfloat16 else lib().umi_gemm_f16
     check(fn(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(err), _stream_ptr(stream)), fn.__name__)
+    return out
+
+
+def check_err(err, fn: str = "kernel") -> None:
+    """Raise UmiError(UMI_ERR_TIMEOUT) if a kernel left error bits in the
+    device word `err` (synchronises with the word's stream first)."""
+    import torch
+    torch.cuda.synchronize(err.device)
+    check(lib().umi_err_status(int(err.item())), fn)
+
+
+def gemm_bf16_wait_limit(A, B, epilogue_wait_ns, out=None, err=None, stream=None):
+    """umi_gemm_bf16 with the epilogue's accumulator wait limited to
+    epilogue_wait_ns (the timeout path's test hook)."""
+    import torch
+    _need(A, torch.bfloat16, "A")
+    _need(B, torch.bfloat16, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    out = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    check(lib().umi_gemm_bf16_wait_limit(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(err), int(epilogue_wait_ns),
+                                         _stream_ptr(stream)), "umi_gemm_bf16_wait_limit")
     return out
 
 

@@ -76,11 +76,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     _link(LIB, objs)
-    build_probe(verbose)
     return LIB
 
 
-PROBE_LIB = os.path.join(PKG, "libumi_probe.so")
+PROBE_DIR = os.path.join(ROOT, "probe")
+PROBE_LIB = os.path.join(PROBE_DIR, "libumi_probe.so")
 
 
 def _link(lib: str, objs: list[str]) -> None:
@@ -93,9 +93,10 @@ def _link(lib: str, objs: list[str]) -> None:
 
 
 def build_probe(verbose: bool = False) -> str:
-    """Benchmark helper library (instruction-throughput probes), separate from the operator ABI."""
+    """The benchmark's instruction-throughput probes (probe/ beside bench.py),
+    a library of their own, separate from the operator ABI."""
     os.makedirs(BUILD, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(PKG, "probe", "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(PROBE_DIR, "*.cu")))
     objs = [_compile(s, verbose) for s in srcs]
     _link(PROBE_LIB, objs)
     return PROBE_LIB

@@ -40,6 +40,7 @@ struct GemmArgs {
 	int M, N, K, ldc;
 	int vec;   // C 16-byte aligned and ldc % 4 == 0: stores through the C tensor map
 	int* err;  // optional: error bits of bounded waits that gave up
+	unsigned long long acc_wait_ns;  // limit of the epilogue's wait for a finished accumulator (kWaitNs)
 };
 
 // C[M,N] = A[M,K] B[N,K]^T: grid (N/BN, M/BM).
@@ -53,6 +54,7 @@ struct GemmPolicy {
 	static constexpr bool EPI_TMA = true;  // epilogue through shared memory + TMA tile stores
 	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
 	template <class A> __device__ static int dil(const A&) { return 1; }
+	__device__ static unsigned long long acc_wait_ns(const GemmArgs& g) { return g.acc_wait_ns; }
 	using Args = GemmArgs;
 	struct Tile { int m0, n0; };
 	// tiles in row-major order of (m-block, n-block): CTAs working at the same
@@ -108,6 +110,7 @@ struct ConvPolicy {
 	static constexpr bool EPI_TMA = false;
 	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
 	template <class A> __device__ static int dil(const A&) { return 1; }
+	template <class A> __device__ static unsigned long long acc_wait_ns(const A&) { return kWaitNs; }
 	using Args = ConvArgs;
 	struct Tile { int n, y, x0, k0; };
 	// tile id = ((n*h + y)*xtiles + xt)*ktiles + kt
@@ -244,6 +247,7 @@ struct MenetConvPolicy {
 	static constexpr int R = 3, MAXD = 8;
 	static constexpr uint32_t STRIP_BYTES = 0;  // per layer: strip_bytes()
 	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * BK * 2 + 1023) & ~1023u;  // 18 432
+	template <class A> __device__ static unsigned long long acc_wait_ns(const A&) { return kWaitNs; }
 	using Args = MenetArgs;
 	struct Tile { int y, x0; };
 	__host__ __device__ static int ntiles(const Args& g) { return g.h * g.xtiles; }
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		for (int id = blockIdx.x; id < ntiles; id += gridDim.x, ++i) {
 			const int a = i & 1;
 			const uint32_t use = (uint32_t)(i >> 1);
-			if (!mbar_wait(&accfull[a], use & 1, abort_flag, g.err, kErrTimeoutAccum)) break;
+			if (!mbar_wait(&accfull[a], use & 1, abort_flag, g.err, kErrTimeoutAccum, P::acc_wait_ns(g))) break;
 			tc_fence_after();
 			const typename P::Tile t = P::tile(g, id);
 #pragma unroll 1
@@ -556,7 +560,7 @@ umi_status map_kmajor(CUtensorMap* m, const void* ptr, CUtensorMapDataType dt, i
 }
 
 umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int K, int ab_type, int* err,
-                       cudaStream_t st) {
+                       cudaStream_t st, unsigned long long acc_wait_ns = kWaitNs) {
 	if (M < 0 || N < 0 || K < 0) return umi::fail(UMI_ERR_INVALID_ARG, "gemm: negative size");
 	if (M == 0 || N == 0) return UMI_OK;
 	if (!A || !B || !C) return umi::fail(UMI_ERR_INVALID_ARG, "gemm: null pointer");
@@ -568,7 +572,7 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 	CUtensorMap ta, tb;
 	UMI_TRY(map_kmajor(&ta, A, dt, M, K, BM));
 	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
-	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err};
+	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err, acc_wait_ns};
 	CUtensorMap tc;
 	std::memset(&tc, 0, sizeof(tc));
 	if (g.vec) {
@@ -604,6 +608,20 @@ extern "C" umi_status umi_gemm_f16(const void* A, const void* B, float* C, int32
                                    void* stream) {
 	const umi_status s = gemm_launch(A, B, C, M, N, K, 0, err, umi::as_stream(stream));
 	return s == UMI_OK ? umi::ok() : s;
+}
+
+extern "C" umi_status umi_gemm_bf16_wait_limit(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K,
+                                               int32_t* err, unsigned long long epilogue_wait_ns, void* stream) {
+	const umi_status s = gemm_launch(A, B, C, M, N, K, 1, err, umi::as_stream(stream), epilogue_wait_ns);
+	return s == UMI_OK ? umi::ok() : s;
+}
+
+extern "C" umi_status umi_err_status(int32_t err_bits) {
+	if (err_bits == 0) return umi::ok();
+	return umi::fail(UMI_ERR_TIMEOUT,
+	                 "a bounded device wait gave up (error bits 0x%x: 1 slice not loaded, 2 ring slot not released, "
+	                 "4 accumulator not finished, 8 accumulator not released)",
+	                 (unsigned)err_bits);
 }
 
 extern "C" size_t umi_gemm_f32_bf16x3_workspace_bytes(int32_t M, int32_t N, int32_t K) {

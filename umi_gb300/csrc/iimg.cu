@@ -23,6 +23,8 @@
 // griddepcontrol.wait, so everything before it overlaps kernel 1), adds the
 // carries (at most nty + ntx + nty*ntx small-array reads per tile, issued as
 // independent loads) and writes the tile with 16-byte stores.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.h"
@@ -506,36 +508,69 @@ extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h
 // frame and the output.
 //
 // The scratch is a file-scope __device__ array of kNoAllocScratchBytes
-// (1 MiB: enough for frames up to 3840x2160 and 4096x2160); every GPU that
+// (1 MiB: the tile sums of every frame the int32 limit accepts, up to 4096
+// rows; the largest accepted frame has h*w*255 < 2^31, about 8.42 Mpx, so
+// 3840x2160 is served and 4096x2160 is refused by that limit); every GPU that
 // loads the library holds it until the process exits.  Host code cannot use
-// the array's name as a device address, so the first call on each device
-// (with that device current) looks the address up with cudaGetSymbolAddress
-// and caches it; make that first call before any stream capture.  All calls
-// share the one array: calls that overlap on the GPU (different streams,
-// different host threads) race on it and must be serialised by the caller.
-// Nothing in the scratch needs to start at zero: kernel 1 writes every entry
-// kernel 2 reads.
+// the array's name as a device address, so the first call in each CUDA
+// context (with that context current) looks the address up with
+// cudaGetSymbolAddress and caches it under the context handle; make that
+// first call before any stream capture.  A context destroyed and re-created
+// while the library stays loaded (cudaDeviceReset) can come back with the
+// same handle: such a caller calls umi_iimg_noalloc_forget() after the reset.
+// All calls share the one array: calls that overlap on the GPU (different
+// streams, different host threads) race on it and must be serialised by the
+// caller.  Nothing in the scratch needs to start at zero: kernel 1 writes
+// every entry kernel 2 reads.
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(1) << 20;
 static_assert(kNoAllocScratchBytes == UMI_IIMG_NOALLOC_SCRATCH_BYTES, "header and library disagree");
 static __device__ __align__(256) unsigned char g_iimg_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
+// Scratch address per CUDA context (the module, and so the array, is loaded
+// once per context: the primary context of each device, or a context the
+// caller made current through the driver API).
+constexpr int kMaxContexts = 64;
 std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchEntry { void* ctx; void* addr; };
+ScratchEntry g_scratch[kMaxContexts] = {};
+int g_scratch_n = 0;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn ctx_get_current_fn() {
+	static CtxGetCurrentFn fn = nullptr;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		cudaDriverEntryPointQueryResult q;
+		void* p = nullptr;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<CtxGetCurrentFn>(p);
+	});
+	return fn;
+}
 
 umi_status scratch_address(void** out) {
 	int dev = 0;
 	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
-	if (dev < 0 || dev >= kMaxDevices) return umi::fail(UMI_ERR_UNSUPPORTED, "iimg_noalloc: device %d", dev);
+	// the runtime makes the device's primary context current if none is yet
+	UMI_TRY(umi::cuda_status(cudaFree(nullptr), "cudaFree(0) (context initialisation)"));
+	auto get = ctx_get_current_fn();
+	if (!get) return umi::fail(UMI_ERR_CUDA, "iimg_noalloc: cuCtxGetCurrent unavailable");
+	CUcontext ctx = nullptr;
+	if (get(&ctx) != CUDA_SUCCESS || !ctx) return umi::fail(UMI_ERR_CUDA, "iimg_noalloc: no current CUDA context");
 	std::lock_guard<std::mutex> lock(g_scratch_mu);
-	if (!g_scratch_addr[dev]) {
-		void* p = nullptr;
-		UMI_TRY(umi::cuda_status(cudaGetSymbolAddress(&p, g_iimg_scratch), "cudaGetSymbolAddress"));
-		g_scratch_addr[dev] = p;
-	}
-	*out = g_scratch_addr[dev];
+	for (int i = 0; i < g_scratch_n; ++i)
+		if (g_scratch[i].ctx == ctx) {
+			*out = g_scratch[i].addr;
+			return UMI_OK;
+		}
+	if (g_scratch_n == kMaxContexts) return umi::fail(UMI_ERR_UNSUPPORTED, "iimg_noalloc: more than %d contexts", kMaxContexts);
+	void* p = nullptr;
+	UMI_TRY(umi::cuda_status(cudaGetSymbolAddress(&p, g_iimg_scratch), "cudaGetSymbolAddress"));
+	g_scratch[g_scratch_n++] = {reinterpret_cast<void*>(ctx), p};
+	*out = p;
 	return UMI_OK;
 }
 
@@ -575,4 +610,9 @@ extern "C" umi_status umi_iimg_u8_i32_noalloc(const uint8_t* in, int32_t* out, i
 	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tile_sums, in, g), "iimg_tile_sums"));
 	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_tiles, in, out, g), "iimg_tiles"));
 	return umi::ok();
+}
+
+extern "C" void umi_iimg_noalloc_forget(void) {
+	std::lock_guard<std::mutex> lock(g_scratch_mu);
+	g_scratch_n = 0;
 }

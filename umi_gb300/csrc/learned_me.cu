@@ -742,7 +742,9 @@ AuxStream* aux_stream(cudaStream_t st) {
 
 umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, int full_r, int audit_stride,
                           const MeFinishBuffers& b, cudaStream_t st, MeAudit* audit) {
-	*audit = MeAudit{};
+	audit->active = audit->combined = audit->forked = audit->joined = false;
+	audit->done = nullptr;
+	audit->st = st;
 	const int nblk = (h / 16) * (w / 16);
 	if (audit_stride <= 0 || nblk == 0) return UMI_OK;
 	audit->active = true;
@@ -765,14 +767,22 @@ umi_status me_audit_begin(const uint8_t* cur, const uint8_t* ref, int h, int w, 
 		as = aux->s;
 	}
 	audit_list_kernel<<<grid_for(na), NT, 0, as>>>(b.alist, b.count + 2, nblk, audit_stride);
-	UMI_TRY(launch_status("audit_list_kernel"));
-	UMI_TRY(umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 2, na, b.amv, as));
+	umi_status rc = launch_status("audit_list_kernel");
+	if (rc == UMI_OK)
+		rc = umi_full_me_u8_list(cur, ref, h, w, 16, full_r, nullptr, b.alist, b.count + 2, na, b.amv, as);
 	if (aux) {
-		UMI_TRY(cuda_status(cudaEventRecord(aux->join, aux->s), "cudaEventRecord"));
-		audit->forked = true;
-		audit->done = aux->join;
+		// recorded on every path once the fork happened: whatever was issued on
+		// the second stream is joined back into the caller's stream
+		const umi_status jr = cuda_status(cudaEventRecord(aux->join, aux->s), "cudaEventRecord");
+		if (jr == UMI_OK) {
+			audit->forked = true;
+			audit->done = aux->join;
+		} else {
+			cudaStreamSynchronize(aux->s);  // no join event: the second stream's work ends here
+			if (rc == UMI_OK) rc = jr;
+		}
 	}
-	return UMI_OK;
+	return rc;
 }
 
 // Refine around the proposal's centres, exhaustive search for every
@@ -797,7 +807,10 @@ umi_status me_refine_fallback_finish(const uint8_t* cur, const uint8_t* ref, int
 		audit_sum_kernel<<<grid_for(ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, nblk, audit_stride, audit_sums);
 		UMI_TRY(launch_status("audit_sum_kernel"));
 	} else if (audit.active && !audit.combined) {
-		if (audit.forked) UMI_TRY(cuda_status(cudaStreamWaitEvent(st, audit.done, 0), "cudaStreamWaitEvent"));
+		if (audit.forked) {
+			UMI_TRY(cuda_status(cudaStreamWaitEvent(st, audit.done, 0), "cudaStreamWaitEvent"));
+			audit.joined = true;
+		}
 		audit_merge_kernel<<<grid_for(ceil_div(nblk, audit_stride)), NT, 0, st>>>(mv, b.amv, nblk, audit_stride,
 		                                                                          audit_sums);
 		UMI_TRY(launch_status("audit_merge_kernel"));

@@ -25,11 +25,27 @@ struct MeFinishBuffers {
 // proposal, so that it can run beside it: `forked` when it went to the
 // calling thread's second stream on this device (joined by `done`), else
 // in order on the caller's stream.
+// Once forked, the caller's stream waits for `done` on every return path:
+// me_refine_fallback_finish joins it before the merge, and the destructor
+// joins it if an error returned earlier, so that no audit kernel can still be
+// writing the caller's workspace after the entry point has returned.
 struct MeAudit {
 	bool active = false;
 	bool combined = false;
 	bool forked = false;
 	cudaEvent_t done = nullptr;
+	cudaStream_t st = nullptr;    // the caller's stream (joined to `done`)
+	mutable bool joined = false;
+	MeAudit() = default;
+	MeAudit(const MeAudit&) = delete;
+	MeAudit& operator=(const MeAudit&) = delete;
+	void join() const {
+		if (forked && !joined) {
+			cudaStreamWaitEvent(st, done, 0);
+			joined = true;
+		}
+	}
+	~MeAudit() { join(); }
 };
 
 // Audit: every audit_stride-th block (0: none) is searched exhaustively in

@@ -50,11 +50,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Waits for the phase with the given parity.  Returns false (after raising
 // *abort and recording `code` in *err) when the limit passes or another role
 // has aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* err, int code,
+                                          unsigned long long limit_ns = kWaitNs) {
 	const unsigned long long t0 = gtimer();
 	while (!mbar_try_wait(bar, parity)) {
 		if (*abort) return false;
-		if (gtimer() - t0 > kWaitNs) {
+		if (gtimer() - t0 > limit_ns) {
 			*abort = 1;
 			if (err) atomicOr(err, code);
 			return false;
