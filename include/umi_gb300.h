@@ -220,6 +220,14 @@ umi_status umi_full_me_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 umi_status umi_full_me_u8_list(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,
                                const int32_t* centers, const int32_t* blocks, const int32_t* n_blocks,
                                int32_t max_blocks, int32_t* mv, void* stream);
+/* Error word of the full-search kernels, no counterpart in the reference
+ * (whose kernels have no bounded waits).  The searches of umi_full_me_u8 and
+ * umi_full_me_u8_list at 16x16 blocks and r = 32 or 64 run a warp-specialised
+ * kernel whose mbarrier waits are bounded (1 s); a wait that gives up ORs an
+ * error bit into a library-wide device word and the blocks it did not finish
+ * get sad = -1.  This call synchronises `stream`, stores the word in *bits
+ * (if non-NULL), clears it and returns UMI_ERR_TIMEOUT if it was set. */
+umi_status umi_full_me_error(int32_t* bits, void* stream);
 /* The same search without the argmin: writes the whole SAD volume
  * (h/b, w/b, 2r+1, 2r+1) int32, the output layout of main/full_me.cu:55-62. */
 umi_status umi_full_me_sad_u8(const uint8_t* cur, const uint8_t* ref, int32_t h, int32_t w, int32_t b, int32_t r,

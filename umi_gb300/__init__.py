@@ -65,6 +65,7 @@ SIGNATURES = {
     "umi_iimg_noalloc_forget": ([], None),
     "umi_full_me_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "umi_full_me_sad_u8": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "umi_full_me_error": ([_vp, _vp], ctypes.c_int),
     "umi_full_me_u8_list": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp], ctypes.c_int),
     "umi_menet_param_count": ([], _i32),
     "umi_menet_workspace_bytes": ([_i32, _i32], _sz),

@@ -21,10 +21,11 @@
 //    first displacement in raster order (the reference's output order
 //    (..., sy, sx), main/full_me.cu:70-71).
 //  * the argmin search runs persistent CTAs with two window buffers: the
-//    next macroblocks' windows are copied (one TMA box per window for large
-//    search ranges, else 4-byte cp.async by all threads) while the current
-//    ones are searched (full_me_pipe_kernel); the SAD-volume output keeps
-//    one CTA per group of macroblocks (full_me_kernel).
+//    next macroblocks' windows are copied (4-byte cp.async by all threads)
+//    while the current ones are searched (full_me_pipe_kernel); the
+//    SAD-volume output keeps one CTA per group of macroblocks
+//    (full_me_kernel).  The benchmark shapes (16x16 blocks, r = 32 and 64,
+//    argmin) go to the warp-specialised kernel of full_me_ws.cu instead.
 #include <algorithm>
 #include <cstring>
 
@@ -34,7 +35,10 @@
 #include "tc_common.cuh"
 
 namespace umi {
-void* tma_encode_fn();  // cuTensorMapEncodeTiled (gemm_tc.cu)
+// Warp-specialised search for 16x16 blocks at r = 32, 64 (full_me_ws.cu);
+// UMI_ERR_UNSUPPORTED (nothing launched) for other shapes.
+umi_status full_me_ws(const uint8_t* cur, const uint8_t* ref, int h, int w, int b, int r, const int32_t* centers,
+                      int32_t* out, const int32_t* list, const int32_t* list_count, int max_slots, cudaStream_t st);
 }
 
 namespace {
@@ -53,7 +57,7 @@ struct MeGeom {
 	int ndx;          // 2r + 1 displacements per axis
 	int ng;           // groups of G vertical displacements
 	int win_rows;     // rows staged per window (ng*G + b - 1)
-	int win_words;    // 32-bit words per staged row (a multiple of 4 when `tma`)
+	int win_words;    // 32-bit words per staged row
 	int win_need;     // words of a row the search reads: (2r + b + 3) / 4 + 1
 	int copy_stride;  // words between the four shifted copies
 	int mb_stride;    // words per macroblock (4 copies + current block)
@@ -61,7 +65,6 @@ struct MeGeom {
 	int tasks_per_mb; // ndx * ng
 	int vec_ok;       // ref and cur are 4-byte aligned and w % 4 == 0: word loads / 4-byte cp.async allowed
 	int nx32;         // largest multiple of 32 <= ndx: displacements served by whole warps
-	int tma;          // argmin search: windows inside the frame with a 16-byte-aligned left edge arrive by TMA
 	int ng2;          // argmin search: groups of G2 vertical displacements for the ndx - nx32 leftover columns (0: none)
 	int tasks_pipe;   // argmin search tasks per macroblock: ng*nx32 + ng2*(ndx - nx32), or ndx*ng when ng2 == 0
 	const int32_t* list;        // optional: search only these blocks (slot i -> block list[i])
@@ -322,86 +325,6 @@ __device__ __forceinline__ bool me_window(const MeGeom& g, const int32_t* __rest
 	return true;
 }
 
-// The window lies inside the frame (no edge replication) and starts on a
-// 16-byte boundary: one TMA box of win_words * 4 bytes x win_rows rows.
-__device__ __forceinline__ bool me_tma_window(const MeGeom& g, bool tma, int gy0, int gx0) {
-	return tma && gy0 >= 0 && gy0 + g.win_rows <= g.h && gx0 >= 0 && gx0 + 4 * g.win_need <= g.w && (gx0 & 15) == 0;
-}
-
-// Bounded wait for the TMA windows of a buffer (1 s of %globaltimer; the
-// boxes are in bounds by construction, so the limit only keeps a failing
-// GPU from hanging the kernel).
-__device__ __forceinline__ void me_tma_wait(uint64_t* bar, uint32_t parity) {
-	const unsigned long long t0 = umi_tc::gtimer();
-	while (!umi_tc::mbar_try_wait(bar, parity))
-		if (umi_tc::gtimer() - t0 > umi_tc::kWaitNs) break;
-}
-
-template <int B>
-__device__ __forceinline__ void me_stage_group_tma(const MeGeom& g, uint32_t* buf, int gi, const uint8_t* __restrict__ cur,
-                                               const uint8_t* __restrict__ ref, const int32_t* __restrict__ centers,
-                                               int tid, int row0, int wd0, int rstep, bool stager, bool tma,
-                                               const CUtensorMap* tref, uint64_t* tbar) {
-	constexpr int BW = B / 4;
-	if (tma && tid == 0) {
-		// arm the buffer's barrier with the bytes of every TMA window, then issue them
-		uint32_t bytes = 0;
-		int blk, gy0, gx0;
-		for (int m = 0; m < g.m && me_window<B>(g, centers, gi * g.m + m, blk, gy0, gx0); ++m)
-			if (me_tma_window(g, tma, gy0, gx0)) bytes += (uint32_t)(4 * g.win_words * g.win_rows);
-		umi_tc::mbar_arrive_expect_tx(tbar, bytes);
-		for (int m = 0; m < g.m && me_window<B>(g, centers, gi * g.m + m, blk, gy0, gx0); ++m)
-			if (me_tma_window(g, tma, gy0, gx0)) umi_tc::tma_load_2d(buf + m * g.mb_stride, tref, tbar, gx0, gy0);
-	}
-	for (int m = 0; m < g.m; ++m) {
-		int blk, gy0, gx0;
-		if (!me_window<B>(g, centers, gi * g.m + m, blk, gy0, gx0)) break;
-		const int by = blk / g.nbx, bx = blk - by * g.nbx;
-		uint32_t* win = buf + m * g.mb_stride;
-		const bool inside = g.vec_ok && gy0 >= 0 && gy0 + g.win_rows <= g.h && gx0 >= 0 &&
-		                    gx0 + 4 * g.win_need <= g.w && (gx0 & 3) == 0;
-		if (stager && wd0 < g.win_need && !me_tma_window(g, tma, gy0, gx0)) {
-			if (inside) {
-				const uint8_t* src = ref + (size_t)gy0 * g.w + gx0 + 4 * wd0;
-				for (int row = row0; row < g.win_rows; row += rstep)
-					cp_async4(win + row * g.win_words + wd0, src + (size_t)row * g.w);
-			} else {
-				const int gx = gx0 + 4 * wd0;
-				const bool vec = g.vec_ok && gx >= 0 && gx + 3 < g.w && (gx & 3) == 0;
-				int xs[4];
-#pragma unroll
-				for (int k = 0; k < 4; ++k) xs[k] = min(max(gx + k, 0), g.w - 1);
-				for (int row = row0; row < g.win_rows; row += rstep) {
-					const int gy = min(max(gy0 + row, 0), g.h - 1);
-					const uint8_t* src = ref + (size_t)gy * g.w;
-					uint32_t v;
-					if (vec) {
-						v = __ldg(reinterpret_cast<const uint32_t*>(src + gx));
-					} else {
-						v = 0;
-#pragma unroll
-						for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + xs[k]) << (8 * k);
-					}
-					win[row * g.win_words + wd0] = v;
-				}
-			}
-		}
-		uint32_t* cb = win + 4 * g.copy_stride;
-		if (tid < B * BW) {
-			const int row = tid / BW, wd = tid - row * BW;
-			const uint8_t* src = cur + (size_t)(by * B + row) * g.w + bx * B + 4 * wd;
-			if (g.vec_ok) {
-				cp_async4(cb + tid, src);
-			} else {
-				uint32_t v = 0;
-#pragma unroll
-				for (int k = 0; k < 4; ++k) v |= (uint32_t)__ldg(src + k) << (8 * k);
-				cb[tid] = v;
-			}
-		}
-	}
-}
-
 // Copies 1..3 of every window of group gi (word k of copy s holds bytes
 // [4k+s, 4k+s+4) of the row).
 __device__ __forceinline__ void me_shift_group(const MeGeom& g, uint32_t* buf, int gi, int row0, int wd0, int rstep,
@@ -468,15 +391,12 @@ __device__ __forceinline__ uint32_t me_task(const MeGeom& g, const uint32_t* win
 // few lanes active.
 constexpr int G2 = 5;
 
-template <int B, int G, bool TMA>
+template <int B, int G>
 __global__ void __launch_bounds__(512) __maxnreg__((MeRegs<B, G>::value))
 full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__ ref,
-                    const int32_t* __restrict__ centers, int32_t* __restrict__ out, const MeGeom g,
-                    const __grid_constant__ CUtensorMap tref) {
+                    const int32_t* __restrict__ centers, int32_t* __restrict__ out, const MeGeom g) {
 	extern __shared__ __align__(128) uint32_t smem[];
 	__shared__ uint32_t best[2][64];
-	__shared__ __align__(8) uint64_t tbar[2];  // TMA windows landed, one per buffer
-	__shared__ int tma_sh;
 	const int tid = threadIdx.x;
 	const int ngroups = (g.slots + g.m - 1) / g.m;
 	const int rstep = blockDim.x / g.win_words;  // host guarantees blockDim >= win_words
@@ -487,26 +407,8 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 	int gi = blockIdx.x;
 	if (gi >= ngroups || slot_block(g, gi * g.m) < 0) return;  // uniform over the CTA
 	if (tid < 64) best[0][tid] = best[1][tid] = 0xffffffffu;
-	if (TMA && tid == 0) {
-		// TMA destinations must be 128-byte aligned: otherwise every window is thread-staged
-		tma_sh = (umi_tc::smem_u32(smem) & 127u) == 0;
-		if (tma_sh) {
-			umi_tc::mbar_init(&tbar[0], 1);
-			umi_tc::mbar_init(&tbar[1], 1);
-			umi_tc::fence_mbar_init();
-		}
-	}
-	if (TMA) __syncthreads();
-	const bool tma = TMA && tma_sh != 0;
-	// staging j (0 = this first group) fills buffer j & 1; that buffer's barrier
-	// then completes its phase j >> 1
-	uint32_t j = 0;
-	if constexpr (TMA)
-		me_stage_group_tma<B>(g, smem, gi, cur, ref, centers, tid, row0, wd0, rstep, stager, tma, &tref, &tbar[0]);
-	else
-		me_stage_group<B>(g, smem, gi, cur, ref, centers, tid, row0, wd0, rstep, stager);
+	me_stage_group<B>(g, smem, gi, cur, ref, centers, tid, row0, wd0, rstep, stager);
 	cp_async_wait_all();
-	if (TMA && tma) me_tma_wait(&tbar[0], 0);
 	__syncthreads();
 	me_shift_group(g, smem, gi, row0, wd0, rstep, stager);
 	__syncthreads();
@@ -517,13 +419,7 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 		const bool has_next = ngi < ngroups && slot_block(g, ngi * g.m) >= 0;
 		uint32_t* cur_buf = smem + cbuf * buf_words;
 		uint32_t* next_buf = smem + (cbuf ^ 1) * buf_words;
-		if (has_next) {
-			if constexpr (TMA)
-				me_stage_group_tma<B>(g, next_buf, ngi, cur, ref, centers, tid, row0, wd0, rstep, stager, tma, &tref,
-				                      &tbar[cbuf ^ 1]);
-			else
-				me_stage_group<B>(g, next_buf, ngi, cur, ref, centers, tid, row0, wd0, rstep, stager);
-		}
+		if (has_next) me_stage_group<B>(g, next_buf, ngi, cur, ref, centers, tid, row0, wd0, rstep, stager);
 		// Search group gi: tasks [0, ng*nx32) are whole-warp columns with G
 		// vertical displacements each; the leftover columns follow in tasks of G2.
 		for (int t = tid; t < total; t += blockDim.x) {
@@ -546,10 +442,6 @@ full_me_pipe_kernel(const uint8_t* __restrict__ cur, const uint8_t* __restrict__
 			atomicMin(&best[cbuf][m], key);
 		}
 		cp_async_wait_all();
-		if constexpr (TMA) {
-			++j;  // the staging of ngi
-			if (has_next && tma) me_tma_wait(&tbar[cbuf ^ 1], (j >> 1) & 1);
-		}
 		__syncthreads();  // search of gi done; this thread's copies for ngi landed (all threads: barrier)
 		if (tid < g.m) {
 			const int blk = slot_block(g, gi * g.m + tid);
@@ -742,8 +634,8 @@ umi_status launch_g(const uint8_t* cur, const uint8_t* ref, const int32_t* cente
 
 template <int B, int G>
 umi_status launch_pipe_g(const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out, const MeGeom& g,
-                         const CUtensorMap& tref, int threads, size_t smem, cudaStream_t st) {
-	auto kern = g.tma ? full_me_pipe_kernel<B, G, true> : full_me_pipe_kernel<B, G, false>;
+                         int threads, size_t smem, cudaStream_t st) {
+	auto kern = full_me_pipe_kernel<B, G>;
 	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
 	                         "cudaFuncSetAttribute"));
 	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -756,18 +648,18 @@ umi_status launch_pipe_g(const uint8_t* cur, const uint8_t* ref, const int32_t* 
 	if (per_sm < 1) return umi::fail(UMI_ERR_UNSUPPORTED, "full_me: %zu bytes of shared memory per CTA do not fit", smem);
 	const int ngroups = (g.slots + g.m - 1) / g.m;
 	const int grid = std::min(ngroups, per_sm * sms);
-	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g, tref);
+	kern<<<grid, threads, smem, st>>>(cur, ref, centers, out, g);
 	return umi::launch_status("full_me_pipe_kernel");
 }
 
 template <int B>
 umi_status launch_pipe_b(int G, const uint8_t* cur, const uint8_t* ref, const int32_t* centers, int32_t* out,
-                         const MeGeom& g, const CUtensorMap& tref, int threads, size_t smem, cudaStream_t st) {
+                         const MeGeom& g, int threads, size_t smem, cudaStream_t st) {
 	switch (G) {
-		case 5: return launch_pipe_g<B, 5>(cur, ref, centers, out, g, tref, threads, smem, st);
-		case 9: return launch_pipe_g<B, 9>(cur, ref, centers, out, g, tref, threads, smem, st);
-		case 13: return launch_pipe_g<B, 13>(cur, ref, centers, out, g, tref, threads, smem, st);
-		default: return launch_pipe_g<B, 15>(cur, ref, centers, out, g, tref, threads, smem, st);
+		case 5: return launch_pipe_g<B, 5>(cur, ref, centers, out, g, threads, smem, st);
+		case 9: return launch_pipe_g<B, 9>(cur, ref, centers, out, g, threads, smem, st);
+		case 13: return launch_pipe_g<B, 13>(cur, ref, centers, out, g, threads, smem, st);
+		default: return launch_pipe_g<B, 15>(cur, ref, centers, out, g, threads, smem, st);
 	}
 }
 
@@ -804,21 +696,20 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	g.win_rows = g.ng * G + b - 1;
 	g.win_need = (2 * r + b + 3) / 4 + 1;
 	g.vec_ok = umi::aligned(ref, 4) && umi::aligned(cur, 4) && (w % 4) == 0;
+	if (!volume) {  // the benchmark ranges: warp-specialised kernel (full_me_ws.cu)
+		const umi_status rc = umi::full_me_ws(cur, ref, h, w, b, r, centers, out, list, list_count, max_slots,
+		                                      umi::as_stream(stream));
+		if (rc != UMI_ERR_UNSUPPORTED) return rc == UMI_OK ? umi::ok() : rc;
+	}
 	if (!volume && !list && b == 16 && r <= 7 && g.vec_ok) {  // small windows: registers only
 		const umi_status rc = launch_small(cur, ref, centers, out, g, umi::as_stream(stream));
 		return rc == UMI_OK ? umi::ok() : rc;
 	}
-	// TMA windows (argmin search, 16x16 blocks, r >= 48): 16-byte-aligned frame rows and box rows.
-	// Measured on GB300: at +-64 one TMA box per window beats the thread-staged
-	// copies (2.76 vs 2.81 ms at 4K); at +-32 the row padding to 16 bytes costs
-	// more in the shift pass than the copies save, and +-4 windows are too small.
-	g.tma = !volume && b == 16 && r >= 48 && umi::aligned(ref, 16) && (w % 16) == 0 && umi::tma_encode_fn() != nullptr;
-	g.win_words = g.tma ? (g.win_need + 3) & ~3 : g.win_need;
+	g.win_words = g.win_need;
 	const int copy = g.win_rows * g.win_words;
 	g.copy_stride = ((copy + 31) / 32) * 32 + 8;  // copies land 8 banks apart
 	g.mb_stride = 4 * g.copy_stride + b * b / 4 + 4;
-	g.mb_stride = g.tma ? (g.mb_stride + 31) & ~31   // each window starts on 128 bytes (TMA destination)
-	                    : (g.mb_stride + 3) & ~3;    // current block 16-byte aligned
+	g.mb_stride = (g.mb_stride + 3) & ~3;  // current block 16-byte aligned
 	g.tasks_per_mb = g.ndx * g.ng;
 	g.nx32 = (g.ndx / 32) * 32;
 	g.ng2 = (g.nx32 > 0 && g.ndx > g.nx32) ? (g.ndx + G2 - 1) / G2 : 0;
@@ -850,21 +741,8 @@ umi_status full_me_common(const uint8_t* cur, const uint8_t* ref, int32_t h, int
 	umi_status rc;
 	if (!volume && 2 * smem <= 200 * 1024) {  // double-buffered persistent search
 		const int tp = threads_for(m * g.tasks_pipe);
-		CUtensorMap tref;
-		std::memset(&tref, 0, sizeof(tref));
-		if (g.tma) {
-			auto enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(umi::tma_encode_fn());
-			const cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
-			const cuuint64_t strides[1] = {(cuuint64_t)w};
-			const cuuint32_t box[2] = {(cuuint32_t)(4 * g.win_words), (cuuint32_t)g.win_rows};
-			const cuuint32_t es[2] = {1, 1};
-			const CUresult cr = enc(&tref, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(ref), dims, strides, box,
-			                        es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-			                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-			if (cr != CUDA_SUCCESS) g.tma = 0;  // thread-staged windows only
-		}
-		rc = b == 16 ? launch_pipe_b<16>(G, cur, ref, centers, out, g, tref, tp, 2 * smem, st)
-		             : launch_pipe_b<8>(G, cur, ref, centers, out, g, tref, tp, 2 * smem, st);
+		rc = b == 16 ? launch_pipe_b<16>(G, cur, ref, centers, out, g, tp, 2 * smem, st)
+		             : launch_pipe_b<8>(G, cur, ref, centers, out, g, tp, 2 * smem, st);
 	} else if (b == 16)
 		rc = volume ? launch_b<16, true>(G, cur, ref, centers, out, g, threads, smem, st)
 		            : launch_b<16, false>(G, cur, ref, centers, out, g, threads, smem, st);
