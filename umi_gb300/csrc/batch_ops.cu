@@ -419,7 +419,9 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 	using namespace umi_tc;
 	using namespace cvtc;
 	extern __shared__ uint8_t smem_raw[];
-	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	// 1024-byte aligned start (128-byte swizzled TMA tiles), formed by indexing
+	// the shared array so that the compiler keeps shared-memory accesses
+	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* outbuf = base + 2 * STAGE_BYTES;
 	uint64_t* full = reinterpret_cast<uint64_t*>(outbuf + 8 * OUT_WARP_BYTES);  // [2]
 	uint64_t* empty = full + 2;     // [2]

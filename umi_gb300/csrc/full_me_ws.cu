@@ -40,6 +40,8 @@
 //    key (sad << 15) | raster index goes to a shared atomicMin per macroblock;
 //    the producer writes (mv_y, mv_x, sad) when it recycles the buffer.
 //
+// Waits sleep in hardware between tests (mbarrier.try_wait with a suspend-
+// time hint), so a warp that ran ahead takes no issue slots from the SADs.
 // Every mbarrier wait is bounded (1 s of %globaltimer).  A wait that gives up
 // raises the CTA's abort flag and ORs an error bit into a library-wide device
 // word (read and cleared by umi_full_me_error); the producer then lets its
@@ -167,8 +169,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 	using Gm = WsGeom<R>;
 	constexpr int NB = Gm::NB, PD = Gm::PD, S = Gm::S, TPM = Gm::TPM;
-	extern __shared__ uint8_t smem_raw[];
-	uint32_t* bufs = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+	extern __shared__ __align__(128) uint8_t smem_raw[];
+	// 128-byte aligned start (TMA destinations), formed by indexing the shared
+	// array so that the compiler keeps shared-memory loads and stores
+	uint32_t* bufs = reinterpret_cast<uint32_t*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
 	__shared__ __align__(8) uint64_t full[NB], empty[NB], tbar[NB];
 	__shared__ uint32_t best[NB];
 	__shared__ int abort_sh;
@@ -255,7 +259,7 @@ full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 			uint32_t* buf = bufs + b * Gm::BUF;
 			cp_async_wait<PD - 1>();  // one group per macroblock; PD - 1 newer ones may stay in flight
 			if (tma_pending >> b & 1u) {
-				mbar_wait(&tbar[b], tma_phase >> b & 1u, abort_flag, &g_full_me_err, kMeErrLoad);
+				mbar_wait_sleep(&tbar[b], tma_phase >> b & 1u, abort_flag, &g_full_me_err, kMeErrLoad, 2000);
 				tma_phase ^= 1u << b;
 				tma_pending &= ~(1u << b);
 			}
@@ -278,7 +282,7 @@ full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 		// Waits until every task of macroblock x is done, writes its result, resets its key.
 		auto retire = [&](int x) -> bool {
 			const int b = x % NB;
-			mbar_wait(&empty[b], (uint32_t)(x / NB) & 1u, abort_flag, &g_full_me_err, kMeErrEmpty);
+			mbar_wait_sleep(&empty[b], (uint32_t)(x / NB) & 1u, abort_flag, &g_full_me_err, kMeErrEmpty);
 			bar_producers();
 			if (*abort_flag) return false;
 			if (pt == 0) {
@@ -332,7 +336,7 @@ full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 		for (int L = c; L < total; L += kSearchThreads) {
 			const int j = L / TPM, t = L - j * TPM;
 			const int b = j % NB;
-			if (!mbar_wait(&full[b], (uint32_t)(j / NB) & 1u, abort_flag, &g_full_me_err, kMeErrFull)) break;
+			if (!mbar_wait_sleep(&full[b], (uint32_t)(j / NB) & 1u, abort_flag, &g_full_me_err, kMeErrFull, 2000)) break;
 			const int q = t / Gm::ND, ix = t - q * Gm::ND;
 			const uint32_t key = ws_task<R>(bufs + b * Gm::BUF, ix, q * Gm::G, a.mul16);
 			atomicMin(&best[b], key);

@@ -305,7 +305,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	const uint32_t load_bytes = STRIP ? P::strip_bytes(g) : STAGE_BYTES;  // bytes one ring load brings
 	static_assert(!STRIP || P::STRIP_STAGE > 0, "strip policies define their stage size");
 	extern __shared__ uint8_t smem_raw[];
-	uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+	// 1024-byte aligned start (128-byte swizzled TMA tiles), formed by indexing
+	// the shared array so that the compiler keeps shared-memory accesses
+	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* bres = base + STAGES * STAGE_BYTES;  // resident B slices (RES only)
 	uint8_t* ebuf = bres + (RES ? P::NK_RES * B_TILE : 0);  // epilogue staging, 2 x 4 KB per epilogue warp (EPI_TMA)
 	uint64_t* full = reinterpret_cast<uint64_t*>(ebuf + (P::EPI_TMA ? 8 * 4096 : 0));

@@ -47,6 +47,38 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 	return ok != 0;
 }
 
+// The same test with a suspend-time hint: a thread whose phase is not yet
+// complete sleeps until it completes or about hint_ns nanoseconds pass,
+// instead of spinning on the issue slots of the warps that do the work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+	uint32_t ok;
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t}"
+		: "=r"(ok)
+		: "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+		: "memory");
+	return ok != 0;
+}
+
+// mbar_wait that sleeps between tests (for waits that can last a whole
+// work unit, e.g. a producer that ran ahead of its consumers).
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, volatile int* abort, int* err, int code,
+                                                uint32_t hint_ns = 20000, unsigned long long limit_ns = kWaitNs) {
+	if (mbar_try_wait(bar, parity)) return true;
+	const unsigned long long t0 = gtimer();
+	while (!mbar_try_wait_sleep(bar, parity, hint_ns)) {
+		if (*abort) return false;
+		if (gtimer() - t0 > limit_ns) {
+			*abort = 1;
+			if (err) atomicOr(err, code);
+			return false;
+		}
+	}
+	return true;
+}
+
 // Waits for the phase with the given parity.  Returns false (after raising
 // *abort and recording `code` in *err) when the limit passes or another role
 // has aborted.
