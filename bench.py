@@ -519,28 +519,40 @@ class Gemm:
         return {"max_abs": float(d.max()), "rms_abs": float(np.sqrt((d ** 2).mean())),
                 "max_rel_to_scale": None, "rms_rel": float(np.sqrt(np.mean(np.minimum(rel, 1.0) ** 2)))}
 
+    @staticmethod
+    def _errors(got, ref, scale):
+        """Error of one variant against FP64: elementwise max / median of
+        |C - C64| / |C64|, normwise RMS ||C - C64||_F / ||C64||_F, and the
+        largest error over the condition scale sum_k |a b|."""
+        d = np.abs(got - ref)
+        rel = d / np.maximum(np.abs(ref), 1e-300)
+        return {"max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+                "rms_rel": float(np.sqrt((d ** 2).sum() / (ref ** 2).sum())),
+                "max_err_over_scale": float((d / scale).max())}
+
     def check(self):
+        """Max and RMS relative error against FP64 for every variant, on 32
+        complete sampled rows of C (4096 x 32 outputs), all from the same fp32
+        inputs: bf16 / f16 (inputs rounded to 16 bits), bf16x3, f16x3 (the
+        FP32-level product), and the plain FP32 UMI path (the generic operator
+        with the reference's Gemm strategy, main/gemm.cu:8-15, fp32 FMA)."""
         import torch
         rows = np.random.default_rng(0).choice(self.M, 32, replace=False)
-        a64 = self.A[0][rows].double().cpu().numpy()
-        b64 = self.B[0].double().cpu().numpy()
-        ref = a64 @ b64.T
-        scale = np.abs(a64) @ np.abs(b64).T
-        C = self.C[0][rows].double().cpu().numpy()
-        out = {"bf16_max_err_over_scale": float((np.abs(C - ref) / scale).max())}
-        # fp32-emulation variant against the fp32 inputs
         a32 = self.a32[rows].double().cpu().numpy()
         b32 = self.b32.double().cpu().numpy()
         ref32 = a32 @ b32.T
-        C3 = self.U.gemm_f32_bf16x3(self.a32, self.b32)[rows].double().cpu().numpy()
-        d3 = np.abs(C3 - ref32)
-        out["bf16x3_vs_fp32_inputs"] = {"max_abs": float(d3.max()), "rms_abs": float(np.sqrt((d3 ** 2).mean())),
-                                        "max_rel": float((d3 / np.abs(ref32)).max()),
-                                        "median_rel": float(np.median(d3 / np.abs(ref32)))}
-        Cb = self.C[0][rows].double().cpu().numpy()
-        db = np.abs(Cb - ref32)
-        out["bf16_vs_fp32_inputs"] = {"max_abs": float(db.max()), "rms_abs": float(np.sqrt((db ** 2).mean())),
-                                      "median_rel": float(np.median(db / np.abs(ref32)))}
+        scale = np.abs(a32) @ np.abs(b32).T
+        ridx = torch.from_numpy(rows).to(self.a32.device)
+        out = {"rows_checked": len(rows), "reference": "FP64 product of the fp32 inputs"}
+        variants = {
+            "bf16": lambda: self.U.gemm(self.a32.to(torch.bfloat16), self.b32.to(torch.bfloat16))[ridx],
+            "f16": lambda: self.U.gemm(self.a32.to(torch.float16), self.b32.to(torch.float16))[ridx],
+            "bf16x3": lambda: self.U.gemm_f32_bf16x3(self.a32, self.b32)[ridx],
+            "f16x3": lambda: self.U.gemm_f32_f16x3(self.a32, self.b32)[ridx],
+            "fp32_umi_generic": lambda: self.U.gemm_f32_generic(self.a32[ridx].contiguous(), self.b32),
+        }
+        for name, fn in variants.items():
+            out[name] = self._errors(fn().double().cpu().numpy(), ref32, scale)
         out["err_word"] = int(self.err.item())
         return out
 
@@ -552,11 +564,22 @@ class Gemm:
         ws = torch.empty(self.U.lib().umi_gemm_f32_bf16x3_workspace_bytes(self.M, self.N, self.K), dtype=torch.uint8,
                          device=dev)
         a32, b32 = self.a32, self.b32
+        ws16 = torch.empty(self.U.lib().umi_gemm_f32_f16x3_workspace_bytes(self.M, self.N, self.K),
+                           dtype=torch.uint8, device=dev)
         fns = {"gemm_bf16": lambda i: self.U.gemm(self.A[i % R], self.B[i % R], out=self.C[i % R], err=self.err),
                "gemm_f16": lambda i: self.U.gemm(A16[i % R], B16[i % R], out=self.C[i % R], err=self.err),
                "gemm_f32_bf16x3": lambda i: self.U.gemm_f32_bf16x3(a32, b32, out=self.C[i % R], workspace=ws,
-                                                                   err=self.err)}
-        return {k: time_launches(f, R, n) for k, f in fns.items()}, None, None
+                                                                   err=self.err),
+               "gemm_f32_f16x3": lambda i: self.U.gemm_f32_f16x3(a32, b32, out=self.C[i % R], workspace=ws16,
+                                                                 err=self.err)}
+        ms = {k: time_launches(f, R, n) for k, f in fns.items()}
+        # the plain FP32 UMI path on a 256-row slice of C (the whole product
+        # through the generic operator would take seconds)
+        rows = 256
+        a_sl = a32[:rows].contiguous()
+        c_sl = torch.empty((rows, self.N), device=dev)
+        ms["gemm_f32_umi_generic_256rows"] = time_launches(lambda i: self.U.gemm_f32_generic(a_sl, b32, out=c_sl), 1, 3)
+        return ms, None, None
 
     def cpu_setup(self):
         import oracle
@@ -598,8 +621,10 @@ class Fprop:
         import umi_gb300 as U
         self.U = U
         gen = torch.Generator(device=dev).manual_seed(self.seed)
-        x = torch.randn((self.N, self.H, self.W, self.C), generator=gen, device=dev).to(torch.bfloat16)
-        w = (torch.randn((self.K, self.R, self.R, self.C), generator=gen, device=dev) / 24.0).to(torch.bfloat16)
+        self.x32 = torch.randn((self.N, self.H, self.W, self.C), generator=gen, device=dev)
+        self.w32 = torch.randn((self.K, self.R, self.R, self.C), generator=gen, device=dev) / 24.0
+        x = self.x32.to(torch.bfloat16)
+        w = self.w32.to(torch.bfloat16)
         self.n_rot = 4
         self.x = [x.clone() for _ in range(self.n_rot)]
         self.w = w
@@ -623,17 +648,38 @@ class Fprop:
         return 2 * self.N * self.H * self.W * self.C, 4 * self.N * self.K * self.H * self.W
 
     def check(self):
+        """Max and RMS relative error against an FP64 convolution (on the GPU,
+        2 images) of the bf16 product (against its bf16 inputs) and of the
+        FP32-level split product f16x3 (against fp32 inputs)."""
         import torch
-        xd = self.x[0][:2].permute(0, 3, 1, 2).double()
-        wd = self.w.permute(0, 3, 1, 2).double()
-        ref = torch.nn.functional.conv2d(xd, wd, padding=1)
-        scale = torch.nn.functional.conv2d(xd.abs(), wd.abs(), padding=1)
-        d = (self.out[0][:2].double() - ref).abs()
-        return {"max_err_over_scale": float((d / scale.clamp_min(1e-30)).max()), "max_abs": float(d.max()),
-                "rms_abs": float(d.pow(2).mean().sqrt()), "images_checked": 2, "err_word": int(self.err.item())}
+
+        def errs(got, xd, wd):
+            ref = torch.nn.functional.conv2d(xd, wd, padding=1)
+            scale = torch.nn.functional.conv2d(xd.abs(), wd.abs(), padding=1)
+            d = (got.double() - ref).abs()
+            return {"max_rel": float((d / ref.abs().clamp_min(1e-300)).max()),
+                    "median_rel": float((d / ref.abs().clamp_min(1e-300)).median()),
+                    "rms_rel": float((d.pow(2).sum() / ref.pow(2).sum()).sqrt()),
+                    "max_err_over_scale": float((d / scale.clamp_min(1e-30)).max())}
+        out = {"images_checked": 2, "reference": "FP64 convolution of the same inputs"}
+        out["bf16"] = errs(self.out[0][:2], self.x[0][:2].permute(0, 3, 1, 2).double(),
+                           self.w.permute(0, 3, 1, 2).double())
+        x32, w32 = self.x32[:2].contiguous(), self.w32
+        got = self.U.conv2d_fprop_f32_f16x3(x32, w32)
+        out["f16x3_fp32_inputs"] = errs(got, x32.permute(0, 3, 1, 2).double(), w32.permute(0, 3, 1, 2).double())
+        out["err_word"] = int(self.err.item())
+        return out
 
     def kernels(self, dev, peaks, n=30):
-        return {"conv2d_fprop_bf16": time_launches(self.step, self.n_rot, n)}, None, None
+        import torch
+        ws = torch.empty(self.U.lib().umi_conv2d_fprop_f32_f16x3_workspace_bytes(self.N, self.C, self.H, self.W,
+                                                                               self.K, self.R), dtype=torch.uint8,
+                         device=dev)
+        o32 = torch.empty_like(self.out[0])
+        return {"conv2d_fprop_bf16": time_launches(self.step, self.n_rot, n),
+                "conv2d_fprop_f32_f16x3": time_launches(
+                    lambda i: self.U.conv2d_fprop_f32_f16x3(self.x32, self.w32, out=o32, workspace=ws, err=self.err),
+                    1, n)}, None, None
 
     def cpu_setup(self):
         import oracle
@@ -1422,12 +1468,19 @@ def run_ours(args, wl, dist):
                                   "frac_of_size_matched_copy": ig / cg}
     elif isinstance(wl, Gemm):
         for name, kt in kms.items():
-            f = wl.flops * (3 if name == "gemm_f32_bf16x3" else 1)
+            if name == "gemm_f32_umi_generic_256rows":
+                f = wl.flops * 256 / wl.M
+                kernels[name] = {"ms_per_launch": kt, "fp32_gemm_tflops": f / (kt * 1e-3) / 1e12,
+                                 "note": "plain fp32 FMA through the generic operator, 256 of the 4096 rows"}
+                continue
+            f = wl.flops * (3 if name in ("gemm_f32_bf16x3", "gemm_f32_f16x3") else 1)
             kernels[name] = {"ms_per_launch": kt, "achieved": f / (kt * 1e-3) / 1e12, "unit": "TFLOP/s",
                              "frac": f / (kt * 1e-3) / 1e12 / pk["bf16_tflops"],
-                             "note": "bf16x3 does 3 bf16 GEMMs per fp32 GEMM; achieved counts tensor FLOPs"
-                             if name == "gemm_f32_bf16x3" else None}
-        kernels["gemm_f32_bf16x3"]["fp32_gemm_tflops"] = wl.flops / (kms["gemm_f32_bf16x3"] * 1e-3) / 1e12
+                             "note": "3 half-precision products per fp32 product (plus the operand split); "
+                                     "achieved counts tensor FLOPs"
+                             if name in ("gemm_f32_bf16x3", "gemm_f32_f16x3") else None}
+        for name in ("gemm_f32_bf16x3", "gemm_f32_f16x3"):
+            kernels[name]["fp32_gemm_tflops"] = wl.flops / (kms[name] * 1e-3) / 1e12
         roof = dict(kernels["gemm_bf16"], bound="tensor", kernel="gemm_tc_kernel (bf16)", peak=pk["bf16_tflops"],
                     **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.M * wl.N), peak_source=pk["source"] + " (burst)",
                     flops_per_launch=wl.flops)
@@ -1442,6 +1495,10 @@ def run_ours(args, wl, dist):
                                         "achieved_gbs": gbs, "frac_of_hbm": gbs / pk["hbm_gbs"],
                                         "tensor_floor_ms": wl.flops / (pk["bf16_tflops"] * 1e12) * 1e3,
                                         "hbm_floor_ms": nbytes / (pk["hbm_gbs"] * 1e9) * 1e3}
+        kt3 = kms["conv2d_fprop_f32_f16x3"]
+        kernels["conv2d_fprop_f32_f16x3"] = {"ms_per_launch": kt3, "fp32_conv_tflops": wl.flops / (kt3 * 1e-3) / 1e12,
+                                             "tensor_tflops": 3 * wl.flops / (kt3 * 1e-3) / 1e12,
+                                             "note": "fp32 inputs split f16 hi/lo (3 products), fp32-level accuracy"}
         k = kernels["conv2d_fprop_bf16"]
         if k["hbm_floor_ms"] >= k["tensor_floor_ms"]:  # the fp32 output makes the launch HBM-bound
             roof = {"bound": "hbm", "kernel": "tc_kernel<conv> (bf16)", "achieved": gbs, "peak": pk["hbm_gbs"],

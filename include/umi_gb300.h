@@ -370,6 +370,21 @@ umi_status umi_err_status(int32_t err_bits);
 size_t umi_gemm_f32_bf16x3_workspace_bytes(int32_t M, int32_t N, int32_t K);
 umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float* C, int32_t M, int32_t N, int32_t K,
                                void* workspace, size_t workspace_bytes, int32_t* err, void* stream);
+/* FP32 GEMM at FP32-level accuracy on the f16 tensor cores: operand
+ * splitting with error correction (Ootomo & Yokota, IJHPCA 2022):
+ * x = x_hi + 2^-11 x_lo (x_hi = rn_f16(x), x_lo = rn_f16((x - x_hi) 2^11)),
+ * C = A_hi B_hi^T + 2^-11 (A_hi B_lo^T + A_lo B_hi^T).  The tensor core's
+ * fp32 accumulation truncates, so A_hi B_hi is accumulated in tensor memory
+ * for `chunk` K-slices of 64 only (0: default 2) and each chunk is added into
+ * fp32 registers with round-to-nearest adds.  A (M,K) and B (N,K) fp32
+ * row-major, 16-byte aligned, K a multiple of 8, |values| < 65504.  Needs a
+ * workspace of umi_gemm_f32_f16x3_workspace_bytes(M, N, K) bytes (256-byte
+ * aligned) for the split operands.  `err` as for umi_gemm_bf16.  Replaces the
+ * Execute call of main/gemm.cu:37-67 (Gemm strategy, main/gemm.cu:8-15) for
+ * fp32 operands. */
+size_t umi_gemm_f32_f16x3_workspace_bytes(int32_t M, int32_t N, int32_t K);
+umi_status umi_gemm_f32_f16x3(const float* A, const float* B, float* C, int32_t M, int32_t N, int32_t K, int32_t chunk,
+                              void* workspace, size_t workspace_bytes, int32_t* err, void* stream);
 
 /* Convolution forward pass on the tensor cores (implicit GEMM, tcgen05):
  * out[n,k,y,x] = sum_{c,dy,dx} w[k,dy,dx,c] * in[n,y+dy-r/2,x+dx-r/2,c], stride
@@ -380,6 +395,16 @@ umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float* C, int32_t
  * (N, K, OH, OW) x (C, R, S); there int32, stride 2, 7x7). */
 umi_status umi_conv2d_fprop_bf16(const void* x_nhwc, const void* w_krsc, float* out_nchw, int32_t n, int32_t c,
                                  int32_t h, int32_t w, int32_t k, int32_t r, int32_t* err, void* stream);
+/* The same convolution on fp32 input and weights at FP32-level accuracy: the
+ * split of umi_gemm_f32_f16x3 applied to the implicit GEMM (x NHWC fp32, w
+ * KRSC fp32, out NCHW fp32; c a multiple of 64; r in 1, 3, 5, 7).  Needs a
+ * workspace of umi_conv2d_fprop_f32_f16x3_workspace_bytes(...) bytes
+ * (256-byte aligned).  `chunk` and `err` as for umi_gemm_f32_f16x3.
+ * Replaces the Execute call of main/fprop.cu:49-82 for fp32 data. */
+size_t umi_conv2d_fprop_f32_f16x3_workspace_bytes(int32_t n, int32_t c, int32_t h, int32_t w, int32_t k, int32_t r);
+umi_status umi_conv2d_fprop_f32_f16x3(const float* x_nhwc, const float* w_krsc, float* out_nchw, int32_t n, int32_t c,
+                                      int32_t h, int32_t w, int32_t k, int32_t r, int32_t chunk, void* workspace,
+                                      size_t workspace_bytes, int32_t* err, void* stream);
 
 /* ---- batched launches: many images of uneven sizes in one persistent
  * launch.  The image table is copied into the launch (no device allocation);

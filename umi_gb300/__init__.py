@@ -87,6 +87,11 @@ SIGNATURES = {
     "umi_err_status": ([_i32], ctypes.c_int),
     "umi_gemm_f32_bf16x3_workspace_bytes": ([_i32, _i32, _i32], _sz),
     "umi_gemm_f32_bf16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _vp, _sz, _vp, _vp], ctypes.c_int),
+    "umi_gemm_f32_f16x3_workspace_bytes": ([_i32, _i32, _i32], _sz),
+    "umi_gemm_f32_f16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp, _sz, _vp, _vp], ctypes.c_int),
+    "umi_conv2d_fprop_f32_f16x3_workspace_bytes": ([_i32, _i32, _i32, _i32, _i32, _i32], _sz),
+    "umi_conv2d_fprop_f32_f16x3": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _sz, _vp, _vp],
+                                   ctypes.c_int),
     "umi_conv2d_fprop_bf16": ([_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_batch_variants": ([_i32], _i32),
     "umi_batch_run": ([_i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
@@ -689,6 +694,68 @@ def gemm_f32_bf16x3(A, B, out=None, workspace=None, err=None, stream=None):
     workspace = torch.empty(max(nb, 256), dtype=torch.uint8, device=A.device) if workspace is None else workspace
     check(lib().umi_gemm_f32_bf16x3(_ptr(A), _ptr(B), _ptr(out), M, N, K, _ptr(workspace), workspace.numel(),
                                     _ptr(err), _stream_ptr(stream)), "umi_gemm_f32_bf16x3")
+    return out
+
+
+def gemm_f32_f16x3(A, B, out=None, workspace=None, chunk=0, err=None, stream=None):
+    """C = A @ B.T for fp32 A (M,K), B (N,K) at fp32-level accuracy: f16 hi/lo
+    split with error correction on the tensor cores, the large product added
+    in fp32 registers every `chunk` K-slices of 64 (umi_gemm_f32_f16x3)."""
+    import torch
+    _need(A, torch.float32, "A")
+    _need(B, torch.float32, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    if B.shape[1] != K:
+        raise ValueError("B must be (N, K)")
+    out = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    _need(out, torch.float32, "out")
+    nb = int(lib().umi_gemm_f32_f16x3_workspace_bytes(M, N, K))
+    workspace = torch.empty(max(nb, 256), dtype=torch.uint8, device=A.device) if workspace is None else workspace
+    check(lib().umi_gemm_f32_f16x3(_ptr(A), _ptr(B), _ptr(out), M, N, K, int(chunk), _ptr(workspace),
+                                   workspace.numel(), _ptr(err), _stream_ptr(stream)), "umi_gemm_f32_f16x3")
+    return out
+
+
+def conv2d_fprop_f32_f16x3(x_nhwc, w_krsc, out=None, workspace=None, chunk=0, err=None, stream=None):
+    """Stride-1 'same' convolution of fp32 x (N,H,W,C) with fp32 w (K,R,R,C) ->
+    (N,K,H,W) fp32 at fp32-level accuracy (umi_conv2d_fprop_f32_f16x3)."""
+    import torch
+    _need(x_nhwc, torch.float32, "x")
+    _need(w_krsc, torch.float32, "w")
+    n, h, w, c = x_nhwc.shape
+    k, r = w_krsc.shape[0], w_krsc.shape[1]
+    out = torch.empty((n, k, h, w), dtype=torch.float32, device=x_nhwc.device) if out is None else out
+    _need(out, torch.float32, "out")
+    nb = int(lib().umi_conv2d_fprop_f32_f16x3_workspace_bytes(n, c, h, w, k, r))
+    workspace = torch.empty(max(nb, 256), dtype=torch.uint8, device=x_nhwc.device) if workspace is None else workspace
+    check(lib().umi_conv2d_fprop_f32_f16x3(_ptr(x_nhwc), _ptr(w_krsc), _ptr(out), n, c, h, w, k, r, int(chunk),
+                                           _ptr(workspace), workspace.numel(), _ptr(err), _stream_ptr(stream)),
+          "umi_conv2d_fprop_f32_f16x3")
+    return out
+
+
+def gemm_f32_generic(A, B, out=None, stream=None):
+    """C = A @ B.T in plain fp32 through the generic UMI operator with the
+    reference's Gemm strategy (main/gemm.cu:8-15: accum += a * b over a
+    blocked K loop, fp32 FMA), for A (M,K) and B (N,K) fp32: the plain FP32
+    UMI path that the split-precision products are measured against."""
+    import torch
+    _need(A, torch.float32, "A")
+    _need(B, torch.float32, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    out = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    _need(out, torch.float32, "out")
+    # P = (row m, column n), A = K; A row-major (M,K), B row-major (N,K): both read along K
+    d = make_desc(p=[(1, 1, 1, 1), (1, 1, 1, 1), (M, 16, 2, 1), (N, 16, 16, 1)], a=[(1, 1), (1, 1), (1, 1), (K, 16)],
+                  mems=[dict(p_view=[(), (), (2, 0, 1), ()], a_view=[(), (), (), (3, 0, 1)],
+                             phys=[(1, PAD), (1, PAD), (M, PAD), (K, PAD)], stage=1),
+                        dict(p_view=[(), (), (), (2, 0, 1)], a_view=[(), (), (), (3, 0, 1)],
+                             phys=[(1, PAD), (1, PAD), (N, PAD), (K, PAD)], stage=1),
+                        dict(p_view=[(), (), (2, 0, 1), (3, 0, 1)], phys=[(), (), (M, PAD), (N, PAD)], stage=2,
+                             out=True)])
+    launch(d, STRATEGY_DOT_F32, [A, B], [out], stream=stream)
     return out
 
 

@@ -17,6 +17,7 @@
 // records an error bit in *err, drains its own copies and MMAs, frees TMEM
 // and returns.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -514,6 +515,308 @@ umi_status persistent_grid(K kern, size_t smem, int ntiles, int tmem_cols, int* 
 	return UMI_OK;
 }
 
+// ---- FP32 products at FP32-level accuracy on the FP16 tensor cores.
+//
+// Operand splitting with error correction (Ootomo & Yokota, "Recovering
+// single precision accuracy from Tensor Cores while surpassing the FP32
+// theoretical peak performance", IJHPCA 2022): x = x_hi + 2^-11 x_lo with
+// x_hi = rn_f16(x), x_lo = rn_f16((x - x_hi) 2^11), and
+//   a b ~= a_hi b_hi + 2^-11 (a_hi b_lo + a_lo b_hi)       (a_lo b_lo dropped).
+// Measured on GB300, the tensor core's fp32 accumulation truncates (the
+// error of a bf16 GEMM with exact products is biased toward zero and grows
+// with K: median 4.2e-6 relative at K = 4096 against 4.4e-7 for a plain
+// fp32 sum), so, as the paper prescribes, the large term is not accumulated
+// over all of K in the tensor core: a_hi b_hi of every `kc` K-slices goes to
+// a fresh TMEM chunk (two, ping-ponged) that the epilogue warps add into fp32
+// registers with round-to-nearest adds while the MMAs fill the other chunk.
+// The correction terms (2^-11 smaller) accumulate over all of K in a third
+// TMEM accumulator; their truncation is scaled down by 2^-11.
+//
+// Tile 128 x 128, K-slices of 64 fp16: a stage holds a_hi, a_lo, b_hi, b_lo
+// (16 KB each, 128-byte swizzle), three stages.  TMEM: chunks at columns
+// 0 and 128, correction accumulators (per tile parity) at 256 and 384.
+// Roles as in tc_kernel: warp 0 TMA producer, warp 1 MMA issuer (3 MMAs per
+// K-step of 16), warps 2..5 epilogue (each owns 32 rows: 128 fp32 running
+// sums per thread).  Every wait is bounded; on a timeout every role stops,
+// copies and MMAs drain, TMEM is freed.
+struct SplitMaps {
+	CUtensorMap ah, al, bh, bl;
+};
+constexpr uint32_t SPLIT_TILE = BM * BK * 2;      // 16 KB: 128 rows x 64 fp16
+constexpr uint32_t SPLIT_STAGE = 4 * SPLIT_TILE;  // a_hi, a_lo, b_hi, b_lo
+constexpr int SPLIT_STAGES = 3, SPLIT_BN = 128;
+constexpr float kSplitLoScale = 1.0f / 2048.0f;
+
+struct GemmSplitPolicy {
+	static constexpr bool EPI_TMA = true;
+	using Args = GemmArgs;
+	using Tile = GemmPolicy::Tile;
+	__host__ __device__ static int ntiles(const Args& g) {
+		return ((g.M + BM - 1) / BM) * ((g.N + SPLIT_BN - 1) / SPLIT_BN);
+	}
+	__device__ static Tile tile(const Args& g, int id) {
+		const int nt = (g.N + SPLIT_BN - 1) / SPLIT_BN;
+		return {(id / nt) * BM, (id % nt) * SPLIT_BN};
+	}
+	__device__ static int nk(const Args& g) { return (g.K + BK - 1) / BK; }
+	__device__ static void load4(const SplitMaps& m, const Args&, const Tile& t, int ks, uint8_t* dst, uint64_t* bar) {
+		tma_load_2d(dst, &m.ah, bar, ks * BK, t.m0);
+		tma_load_2d(dst + SPLIT_TILE, &m.al, bar, ks * BK, t.m0);
+		tma_load_2d(dst + 2 * SPLIT_TILE, &m.bh, bar, ks * BK, t.n0);
+		tma_load_2d(dst + 3 * SPLIT_TILE, &m.bl, bar, ks * BK, t.n0);
+	}
+	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
+		GemmPolicy::store(g, t, rl, c, v);
+	}
+};
+
+// The convolution (ConvPolicy's tiles: 128 pixels of a row x 128 output
+// channels, K-slices (tap, 64 input channels)) with split operands.
+struct ConvSplitPolicy {
+	static constexpr bool EPI_TMA = false;
+	using Args = ConvArgs;
+	using Tile = ConvPolicy::Tile;
+	static_assert(ConvPolicy::BN == SPLIT_BN, "tile width");
+	__host__ __device__ static int ntiles(const Args& g) { return ConvPolicy::ntiles(g); }
+	__device__ static Tile tile(const Args& g, int id) { return ConvPolicy::tile(g, id); }
+	__device__ static int nk(const Args& g) { return ConvPolicy::nk(g); }
+	__device__ static void load4(const SplitMaps& m, const Args& g, const Tile& t, int ks, uint8_t* dst, uint64_t* bar) {
+		const int cs = g.c / BK;
+		const int tap = ks / cs, c0 = (ks - tap * cs) * BK;
+		const int dy = tap / g.r, dx = tap - dy * g.r, pad = g.r / 2;
+		tma_load_4d(dst, &m.ah, bar, c0, t.x0 + dx - pad, t.y + dy - pad, t.n);
+		tma_load_4d(dst + SPLIT_TILE, &m.al, bar, c0, t.x0 + dx - pad, t.y + dy - pad, t.n);
+		tma_load_2d(dst + 2 * SPLIT_TILE, &m.bh, bar, tap * g.c + c0, t.k0);
+		tma_load_2d(dst + 3 * SPLIT_TILE, &m.bl, bar, tap * g.c + c0, t.k0);
+	}
+	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
+		ConvPolicy::store(g, t, rl, c, v);
+	}
+};
+
+template <class P>
+__global__ void __launch_bounds__(NTHREADS, 1)
+	tc_split_kernel(const __grid_constant__ SplitMaps maps, const __grid_constant__ CUtensorMap tcm,
+	                const typename P::Args g, const uint32_t idesc, const int kc) {
+	extern __shared__ __align__(1024) uint8_t smem_raw[];
+	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+	uint8_t* ebuf = base + SPLIT_STAGES * SPLIT_STAGE;  // epilogue staging, 2 x 4 KB per epilogue warp (EPI_TMA)
+	uint64_t* full = reinterpret_cast<uint64_t*>(ebuf + (P::EPI_TMA ? 8 * 4096 : 0));
+	uint64_t* empty = full + SPLIT_STAGES;
+	uint64_t* hifull = empty + SPLIT_STAGES;  // [2] chunk of a_hi b_hi complete
+	uint64_t* hiempty = hifull + 2;           // [2] chunk added into the registers
+	uint64_t* accfull = hiempty + 2;          // [2] correction accumulator complete
+	uint64_t* accempty = accfull + 2;         // [2] correction accumulator read
+	uint64_t* drain = accempty + 2;
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int ntiles = P::ntiles(g);
+	const int nk = P::nk(g);
+	const int nchunk = (nk + kc - 1) / kc;
+
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < SPLIT_STAGES; ++s) {
+			mbar_init(&full[s], 1);
+			mbar_init(&empty[s], 1);
+		}
+		for (int a = 0; a < 2; ++a) {
+			mbar_init(&hifull[a], 1);
+			mbar_init(&hiempty[a], 4);
+			mbar_init(&accfull[a], 1);
+			mbar_init(&accempty[a], 4);
+		}
+		mbar_init(drain, 1);
+		*abort_flag = 0;
+		fence_mbar_init();
+		tma_prefetch(&maps.ah);
+		tma_prefetch(&maps.al);
+		tma_prefetch(&maps.bh);
+		tma_prefetch(&maps.bl);
+	}
+	if (warp == 1) {
+		tmem_alloc(tmem_slot, 512);
+		tmem_relinquish();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = *tmem_slot;
+
+	if (warp == 0 && lane == 0) {
+		// ---- producer
+		int armed[SPLIT_STAGES];
+		for (int s = 0; s < SPLIT_STAGES; ++s) armed[s] = -1;
+		uint32_t q = 0;
+		for (int id = blockIdx.x; id < ntiles && !*abort_flag; id += gridDim.x) {
+			const typename P::Tile t = P::tile(g, id);
+			for (int ks = 0; ks < nk; ++ks, ++q) {
+				const int s = (int)(q % SPLIT_STAGES);
+				const uint32_t round = q / SPLIT_STAGES;
+				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
+				mbar_arrive_expect_tx(&full[s], SPLIT_STAGE);
+				armed[s] = (int)round;
+				P::load4(maps, g, t, ks, base + s * SPLIT_STAGE, &full[s]);
+			}
+		}
+		if (*abort_flag) {
+			volatile int own = 0;
+			for (int s = 0; s < SPLIT_STAGES; ++s)
+				if (armed[s] >= 0) mbar_wait(&full[s], (uint32_t)armed[s] & 1, &own, g.err, kErrTimeoutFull);
+		}
+	} else if (warp == 1 && lane == 0) {
+		// ---- MMA issuer
+		uint32_t q = 0, cq = 0;
+		int i = 0;
+		bool ok = true;
+		for (int id = blockIdx.x; ok && id < ntiles && !*abort_flag; id += gridDim.x, ++i) {
+			const int a = i & 1;
+			if (!mbar_wait(&accempty[a], ((uint32_t)(i >> 1) & 1) ^ 1, abort_flag, g.err, kErrTimeoutAccEmpty)) break;
+			tc_fence_after();
+			const uint32_t cacc = tmem + 256u + (uint32_t)(a * SPLIT_BN);
+			uint32_t hacc = 0;
+			for (int ks = 0; ks < nk; ++ks, ++q) {
+				const bool first = ks % kc == 0;
+				if (first) {
+					const uint32_t hb = cq & 1;
+					if (!mbar_wait(&hiempty[hb], ((cq >> 1) & 1) ^ 1, abort_flag, g.err, kErrTimeoutAccEmpty)) {
+						ok = false;
+						break;
+					}
+					tc_fence_after();
+					hacc = tmem + hb * (uint32_t)SPLIT_BN;
+				}
+				const int s = (int)(q % SPLIT_STAGES);
+				if (!mbar_wait(&full[s], (q / SPLIT_STAGES) & 1, abort_flag, g.err, kErrTimeoutFull)) {
+					ok = false;
+					break;
+				}
+				tc_fence_after();
+				const uint32_t sa = smem_u32(base + s * SPLIT_STAGE);
+				const uint64_t dah = desc_kmajor_sw128(sa), dal = desc_kmajor_sw128(sa + SPLIT_TILE);
+				const uint64_t dbh = desc_kmajor_sw128(sa + 2 * SPLIT_TILE), dbl = desc_kmajor_sw128(sa + 3 * SPLIT_TILE);
+#pragma unroll
+				for (int kk = 0; kk < BK / 16; ++kk) {
+					mma_f16(hacc, dah + 2 * kk, dbh + 2 * kk, idesc, !first || kk > 0);
+					mma_f16(cacc, dah + 2 * kk, dbl + 2 * kk, idesc, ks > 0 || kk > 0);
+					mma_f16(cacc, dal + 2 * kk, dbh + 2 * kk, idesc, true);
+				}
+				mma_commit(&empty[s]);
+				if (ks % kc == kc - 1 || ks == nk - 1) {
+					mma_commit(&hifull[cq & 1]);
+					++cq;
+				}
+			}
+			if (!ok) break;
+			mma_commit(&accfull[a]);
+		}
+		mma_commit(drain);
+		volatile int own = 0;
+		mbar_wait(drain, 0, &own, g.err, kErrTimeoutAccum);
+	} else if (warp >= 2) {
+		// ---- epilogue: warp w owns TMEM lanes 32*(w%4) .. +31 (rows of the tile)
+		const int qd = warp & 3;
+		const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
+		uint32_t cq = 0, nst = 0;
+		int i = 0;
+		bool ok = true;
+		for (int id = blockIdx.x; ok && id < ntiles; id += gridDim.x, ++i) {
+			const int a = i & 1;
+			float run[SPLIT_BN];
+#pragma unroll
+			for (int c = 0; c < SPLIT_BN; ++c) run[c] = 0.0f;
+			for (int ch = 0; ch < nchunk; ++ch, ++cq) {
+				const uint32_t hb = cq & 1;
+				if (!mbar_wait(&hifull[hb], (cq >> 1) & 1, abort_flag, g.err, kErrTimeoutAccum)) {
+					ok = false;
+					break;
+				}
+				tc_fence_after();
+#pragma unroll
+				for (int c = 0; c < SPLIT_BN; c += 32) {
+					float v[32];
+					tmem_ld32(tmem + lane_base + hb * (uint32_t)SPLIT_BN + (uint32_t)c, v);
+#pragma unroll
+					for (int j = 0; j < 32; ++j) run[c + j] += v[j];
+				}
+				tc_fence_before();
+				__syncwarp();
+				if (lane == 0) mbar_arrive(&hiempty[hb]);
+			}
+			if (!ok) break;
+			if (!mbar_wait(&accfull[a], ((uint32_t)i >> 1) & 1, abort_flag, g.err, kErrTimeoutAccum)) break;
+			tc_fence_after();
+			const typename P::Tile t = P::tile(g, id);
+#pragma unroll
+			for (int c = 0; c < SPLIT_BN; c += 32) {
+				float v[32];
+				tmem_ld32(tmem + lane_base + 256u + (uint32_t)(a * SPLIT_BN + c), v);
+#pragma unroll
+				for (int j = 0; j < 32; ++j) v[j] = fmaf(v[j], kSplitLoScale, run[c + j]);  // exact scaling, one rounding
+				if constexpr (P::EPI_TMA) {
+					if (g.vec) {
+						const int row0 = t.m0 + 32 * qd, col0 = t.n0 + c;
+						if (row0 < g.M && col0 < g.N) {
+							uint8_t* sb = ebuf + (qd * 2 + (nst & 1)) * 4096;
+							if (lane == 0) bulk_wait_read_1();
+							__syncwarp();
+#pragma unroll
+							for (int j = 0; j < 8; ++j)
+								*reinterpret_cast<float4*>(sb + lane * 128 + ((j ^ (lane & 7)) << 4)) =
+									make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+							fence_proxy_async_smem();
+							__syncwarp();
+							if (lane == 0) {
+								tma_store_2d(&tcm, sb, col0, row0);
+								bulk_commit();
+							}
+							++nst;
+						}
+						continue;
+					}
+				}
+				P::store(g, t, 32 * qd + lane, c, v);
+			}
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&accempty[a]);
+		}
+		if constexpr (P::EPI_TMA) {
+			if (lane == 0) bulk_wait_all();
+			__syncwarp();
+		}
+	}
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 1) {
+		tc_fence_after();
+		tmem_dealloc(tmem, 512);
+	}
+}
+
+template <class P>
+constexpr size_t split_smem_bytes() {
+	return (size_t)SPLIT_STAGES * SPLIT_STAGE + (P::EPI_TMA ? 8 * 4096 : 0) + 1024 + 256;
+}
+
+// x (rows x K fp32) -> hi = rn_f16(x), lo = rn_f16((x - hi) 2^11), both (rows x K) fp16.
+__global__ void split_f16_kernel(const float4* __restrict__ X, uint2* __restrict__ Hi, uint2* __restrict__ Lo, size_t n4) {
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 x = X[i];
+		const float xs[4] = {x.x, x.y, x.z, x.w};
+		__half h[4], l[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			h[k] = __float2half_rn(xs[k]);
+			l[k] = __float2half_rn((xs[k] - __half2float(h[k])) * 2048.0f);
+		}
+		Hi[i] = make_uint2((uint32_t)__half_as_ushort(h[0]) | ((uint32_t)__half_as_ushort(h[1]) << 16),
+		                   (uint32_t)__half_as_ushort(h[2]) | ((uint32_t)__half_as_ushort(h[3]) << 16));
+		Lo[i] = make_uint2((uint32_t)__half_as_ushort(l[0]) | ((uint32_t)__half_as_ushort(l[1]) << 16),
+		                   (uint32_t)__half_as_ushort(l[2]) | ((uint32_t)__half_as_ushort(l[3]) << 16));
+	}
+}
+
 // ---- split of fp32 operands into bf16 hi/lo parts, concatenated along K:
 // A' = [A_hi | A_lo | A_hi], B' = [B_hi | B_hi | B_lo]  =>  A' B'^T =
 // A_hi B_hi^T + A_lo B_hi^T + A_hi B_lo^T  (bf16x3 of Henry, Tang & Heinecke,
@@ -649,6 +952,152 @@ extern "C" umi_status umi_gemm_f32_bf16x3(const float* A, const float* B, float*
 	split_bf16x3_kernel<<<1024, 256, 0, st>>>(B, Bs, N, K, 2);
 	UMI_TRY(umi::launch_status("split_bf16x3_kernel"));
 	const umi_status s = gemm_launch(As, Bs, C, M, N, 3 * K, 1, err, st);
+	return s == UMI_OK ? umi::ok() : s;
+}
+
+namespace {
+
+constexpr int kSplitChunkDefault = 2;  // K-slices of 64 per TMEM chunk of a_hi b_hi
+
+size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+umi_status split_operand(const float* X, size_t n, __half* hi, __half* lo, cudaStream_t st) {
+	const size_t n4 = n / 4;
+	const int blocks = (int)std::min<size_t>(4096, std::max<size_t>(1, (n4 + 255) / 256));
+	split_f16_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const float4*>(X), reinterpret_cast<uint2*>(hi),
+	                                          reinterpret_cast<uint2*>(lo), n4);
+	return umi::launch_status("split_f16_kernel");
+}
+
+template <class P>
+umi_status split_launch(const SplitMaps& maps, const CUtensorMap& tc, const typename P::Args& g, int kc,
+                        cudaStream_t st, const char* what) {
+	constexpr size_t SMEM = split_smem_bytes<P>();
+	auto kern = tc_split_kernel<P>;
+	int grid = 0;
+	UMI_TRY(persistent_grid(kern, SMEM, P::ntiles(g), 512, &grid));
+	kern<<<grid, NTHREADS, SMEM, st>>>(maps, tc, g, idesc_f16(0u, BM, SPLIT_BN), kc);
+	return umi::launch_status(what);
+}
+
+umi_status check_chunk(int32_t chunk, int* kc) {
+	if (chunk < 0 || chunk > 64) return umi::fail(UMI_ERR_INVALID_ARG, "split: chunk of %d K-slices (0..64)", chunk);
+	*kc = chunk == 0 ? kSplitChunkDefault : chunk;
+	return UMI_OK;
+}
+
+}  // namespace
+
+extern "C" size_t umi_gemm_f32_f16x3_workspace_bytes(int32_t M, int32_t N, int32_t K) {
+	if (M <= 0 || N <= 0 || K <= 0) return 0;
+	return 2 * al256((size_t)M * K * 2) + 2 * al256((size_t)N * K * 2);
+}
+
+extern "C" umi_status umi_gemm_f32_f16x3(const float* A, const float* B, float* C, int32_t M, int32_t N, int32_t K,
+                                         int32_t chunk, void* workspace, size_t workspace_bytes, int32_t* err,
+                                         void* stream) {
+	if (M < 0 || N < 0 || K < 0) return umi::fail(UMI_ERR_INVALID_ARG, "gemm_f16x3: negative size");
+	const cudaStream_t st = umi::as_stream(stream);
+	int kc = 0;
+	UMI_TRY(check_chunk(chunk, &kc));
+	if (M == 0 || N == 0) return umi::ok();
+	if (!A || !B || !C) return umi::fail(UMI_ERR_INVALID_ARG, "gemm_f16x3: null pointer");
+	if (K == 0) {
+		const umi_status s = umi::cuda_status(cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st), "cudaMemsetAsync");
+		return s == UMI_OK ? umi::ok() : s;
+	}
+	if (K % 8 != 0) return umi::fail(UMI_ERR_UNSUPPORTED, "gemm_f16x3: K = %d must be a multiple of 8", K);
+	if (!umi::aligned(A, 16) || !umi::aligned(B, 16))
+		return umi::fail(UMI_ERR_INVALID_ARG, "gemm_f16x3: A and B must be 16-byte aligned");
+	if (!workspace) return umi::fail(UMI_ERR_INVALID_ARG, "gemm_f16x3: null workspace");
+	if (!umi::aligned(workspace, 256)) return umi::fail(UMI_ERR_INVALID_ARG, "gemm_f16x3: workspace not 256-byte aligned");
+	if (workspace_bytes < umi_gemm_f32_f16x3_workspace_bytes(M, N, K))
+		return umi::fail(UMI_ERR_NO_MEMORY, "gemm_f16x3: workspace of %zu bytes, need %zu", workspace_bytes,
+		                 umi_gemm_f32_f16x3_workspace_bytes(M, N, K));
+	if ((int64_t)umi::ceil_div(M, BM) * umi::ceil_div(N, SPLIT_BN) > INT32_MAX)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "gemm_f16x3: too many tiles");
+	char* ws = static_cast<char*>(workspace);
+	__half* ah = reinterpret_cast<__half*>(ws);
+	__half* al = reinterpret_cast<__half*>(ws + al256((size_t)M * K * 2));
+	__half* bh = reinterpret_cast<__half*>(ws + 2 * al256((size_t)M * K * 2));
+	__half* bl = reinterpret_cast<__half*>(ws + 2 * al256((size_t)M * K * 2) + al256((size_t)N * K * 2));
+	UMI_TRY(split_operand(A, (size_t)M * K, ah, al, st));
+	UMI_TRY(split_operand(B, (size_t)N * K, bh, bl, st));
+	SplitMaps maps;
+	UMI_TRY(map_kmajor(&maps.ah, ah, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, M, K, BM));
+	UMI_TRY(map_kmajor(&maps.al, al, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, M, K, BM));
+	UMI_TRY(map_kmajor(&maps.bh, bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, N, K, SPLIT_BN));
+	UMI_TRY(map_kmajor(&maps.bl, bl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, N, K, SPLIT_BN));
+	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err, kWaitNs};
+	CUtensorMap tc;
+	std::memset(&tc, 0, sizeof(tc));
+	if (g.vec) {
+		auto enc = encode_fn();
+		const cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)M};
+		const cuuint64_t strides[1] = {(cuuint64_t)N * 4};
+		const cuuint32_t box[2] = {32, 32};
+		const cuuint32_t es[2] = {1, 1};
+		const CUresult r = enc(&tc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, es,
+		                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                       CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "gemm_f16x3: C tensor map (%d)", (int)r);
+	}
+	const umi_status s = split_launch<GemmSplitPolicy>(maps, tc, g, kc, st, "tc_split_kernel<gemm>");
+	return s == UMI_OK ? umi::ok() : s;
+}
+
+extern "C" size_t umi_conv2d_fprop_f32_f16x3_workspace_bytes(int32_t n, int32_t c, int32_t h, int32_t w, int32_t k,
+                                                             int32_t r) {
+	if (n <= 0 || c <= 0 || h <= 0 || w <= 0 || k <= 0 || r <= 0) return 0;
+	return 2 * al256((size_t)n * h * w * c * 2) + 2 * al256((size_t)k * r * r * c * 2);
+}
+
+extern "C" umi_status umi_conv2d_fprop_f32_f16x3(const float* x_nhwc, const float* w_krsc, float* out_nchw, int32_t n,
+                                                 int32_t c, int32_t h, int32_t w, int32_t k, int32_t r, int32_t chunk,
+                                                 void* workspace, size_t workspace_bytes, int32_t* err, void* stream) {
+	if (n < 0 || c < 0 || h < 0 || w < 0 || k < 0) return umi::fail(UMI_ERR_INVALID_ARG, "conv_f16x3: negative size");
+	int kc = 0;
+	UMI_TRY(check_chunk(chunk, &kc));
+	if (n == 0 || h == 0 || w == 0 || k == 0) return umi::ok();
+	if (!x_nhwc || !w_krsc || !out_nchw || !workspace) return umi::fail(UMI_ERR_INVALID_ARG, "conv_f16x3: null pointer");
+	if (r != 1 && r != 3 && r != 5 && r != 7)
+		return umi::fail(UMI_ERR_UNSUPPORTED, "conv_f16x3: filter %dx%d (1, 3, 5, 7)", r, r);
+	if (c % BK != 0) return umi::fail(UMI_ERR_UNSUPPORTED, "conv_f16x3: %d input channels (a multiple of %d)", c, BK);
+	if (!umi::aligned(x_nhwc, 16) || !umi::aligned(w_krsc, 16))
+		return umi::fail(UMI_ERR_INVALID_ARG, "conv_f16x3: misaligned input");
+	if (!umi::aligned(workspace, 256)) return umi::fail(UMI_ERR_INVALID_ARG, "conv_f16x3: workspace not 256-byte aligned");
+	if (workspace_bytes < umi_conv2d_fprop_f32_f16x3_workspace_bytes(n, c, h, w, k, r))
+		return umi::fail(UMI_ERR_NO_MEMORY, "conv_f16x3: workspace too small");
+	auto enc = encode_fn();
+	if (!enc) return umi::fail(UMI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+	const cudaStream_t st = umi::as_stream(stream);
+	const size_t nx = (size_t)n * h * w * c, nw = (size_t)k * r * r * c;
+	char* ws = static_cast<char*>(workspace);
+	__half* xh = reinterpret_cast<__half*>(ws);
+	__half* xl = reinterpret_cast<__half*>(ws + al256(nx * 2));
+	__half* wh = reinterpret_cast<__half*>(ws + 2 * al256(nx * 2));
+	__half* wl = reinterpret_cast<__half*>(ws + 2 * al256(nx * 2) + al256(nw * 2));
+	UMI_TRY(split_operand(x_nhwc, nx, xh, xl, st));
+	UMI_TRY(split_operand(w_krsc, nw, wh, wl, st));
+	SplitMaps maps;
+	for (int part = 0; part < 2; ++part) {
+		const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+		const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)BM, 1, 1};
+		const cuuint32_t es[4] = {1, 1, 1, 1};
+		const CUresult rr = enc(part ? &maps.al : &maps.ah, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, part ? xl : xh, dims,
+		                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "conv_f16x3: input tensor map (%d)", (int)rr);
+	}
+	UMI_TRY(map_kmajor(&maps.bh, wh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, k, r * r * c, SPLIT_BN));
+	UMI_TRY(map_kmajor(&maps.bl, wl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, k, r * r * c, SPLIT_BN));
+	ConvArgs g{out_nchw, n, c, h, w, k, r, umi::ceil_div(w, BM), umi::ceil_div(k, SPLIT_BN),
+	           umi::aligned(out_nchw, 16) && w % 4 == 0, err};
+	if ((int64_t)n * h * g.xtiles * g.ktiles > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "conv_f16x3: too many tiles");
+	CUtensorMap unused;
+	std::memset(&unused, 0, sizeof(unused));
+	const umi_status s = split_launch<ConvSplitPolicy>(maps, unused, g, kc, st, "tc_split_kernel<conv>");
 	return s == UMI_OK ? umi::ok() : s;
 }
 
