@@ -449,6 +449,28 @@ typedef struct umi_batch_graph umi_batch_graph;
 umi_status umi_batch_graph_create(umi_batch_graph** graph);
 umi_status umi_batch_graph_add(umi_batch_graph* graph, int32_t op, const umi_batch_image* images, int32_t n_images,
                                const umi_batch_params* params, int32_t variant);
+/* One launch for a whole batch step, no counterpart in the reference (which
+ * runs one Execute per image and operator): up to one job per operator
+ * (bilateral, per-pixel-weight filter, dot-product cost volume), each with its
+ * images, parameters and, per image, the variant that serves it (tile shape
+ * and pixels per thread; NULL: variant 0 for every image; see
+ * umi_batch_fused_variants).  One persistent kernel walks every CTA's share of
+ * the cost-volume tiles (tensor cores), then of one queue holding the two
+ * filters' tiles of all images.  The cost-volume job must use nd = 64, 1..32
+ * channels and 16-byte aligned outputs (else UMI_ERR_UNSUPPORTED: use
+ * umi_batch_run per operator); at most UMI_BATCH_MAX_IMAGES images in each
+ * job and in the filters' queue together.  Allocates nothing. */
+typedef struct {
+	int32_t op; /* umi_batch_op */
+	const umi_batch_image* images;
+	int32_t n_images;
+	umi_batch_params params;
+	const int32_t* variants; /* n_images host ints, or NULL */
+} umi_batch_job;
+int32_t umi_batch_fused_variants(int32_t op);
+umi_status umi_batch_run_fused(const umi_batch_job* jobs, int32_t n_jobs, void* stream);
+/* Records one umi_batch_run_fused launch as the next node of `graph`. */
+umi_status umi_batch_graph_add_fused(umi_batch_graph* graph, const umi_batch_job* jobs, int32_t n_jobs);
 umi_status umi_batch_graph_launch(umi_batch_graph* graph, void* stream);
 void umi_batch_graph_destroy(umi_batch_graph* graph);
 

@@ -153,3 +153,120 @@ def test_batch_rejects_bad_arguments(umi, dev):
         umi.batch_run(umi.OP_COST_VOLUME, [(x.view(1, 4, 4), x.view(1, 4, 4), x)], umi.BatchParams(0, 0, 0, 1, 48))
     with pytest.raises(umi.UmiError):
         umi.batch_run(umi.OP_WFILTER_PP, [(x, None, x)])  # missing weights
+
+
+# ---------------------------------------------------------------- one fused launch for a batch step
+def _fused_case(seed, n, lo, hi):
+    sizes = _uneven_sizes(seed, n, lo, hi)
+    g = np.random.default_rng(seed + 100)
+    xs = [g.random(s, dtype=np.float32) for s in sizes]
+    ws = [g.random(s + (3, 3), dtype=np.float32) for s in sizes]
+    Ls = [g.standard_normal((32,) + s).astype(np.float32) for s in sizes]
+    Rs = [g.standard_normal((32,) + s).astype(np.float32) for s in sizes]
+    return sizes, xs, ws, Ls, Rs
+
+
+def _fused_check(outs_b, outs_w, outs_c, xs, ws, Ls, Rs, want_b, want_w, want_c, tag):
+    for o, wv in zip(outs_b, want_b):
+        if wv is not None:
+            assert _bil_rel(o.cpu().numpy(), wv) <= TOL, ("bilateral", tag)
+    for o, wv, x, wt in zip(outs_w, want_w, xs, ws):
+        if wv is not None:
+            got = o.cpu().numpy()
+            assert np.max(np.abs(got - wv) / np.maximum(np.abs(wv), _wf_scale(x, wt))) <= TOL, ("wfilter", tag)
+    for o, wv, L, R in zip(outs_c, want_c, Ls, Rs):
+        if wv is not None:
+            got = o.cpu().numpy()
+            err = np.max(np.abs(got - wv) / np.maximum(np.maximum(np.abs(wv), _cv_scale(L, R, 64)), 1e-30))
+            assert err <= TOL, ("cost volume", tag)
+
+
+def test_batch_fused_all_operators_every_variant(umi, orc, dev):
+    """The three operators of an uneven batch (an empty and a 1x1 image
+    included) in ONE fused launch, against the FP64 oracle, for every fused
+    variant of the filters, and with a different variant per image."""
+    import torch
+    sizes, xs, ws, Ls, Rs = _fused_case(11, 7, 1, 150)
+    want_b = [orc.bilateral_f64(x, 2, 2.0, 0.1) if x.size else None for x in xs]
+    want_w = [orc.wfilter_pp_f64(x, wt) if x.size else None for x, wt in zip(xs, ws)]
+    want_c = [orc.cost_volume_dot_f64(L, R, 64) if L.size else None for L, R in zip(Ls, Rs)]
+    dx, dw, dL, dR = ([_t(a, dev) for a in arr] for arr in (xs, ws, Ls, Rs))
+    nb, nw = umi.batch_fused_variants(umi.OP_BILATERAL), umi.batch_fused_variants(umi.OP_WFILTER_PP)
+    assert nb >= 2 and nw >= 2
+    plans = [([v] * len(sizes), [v % nw] * len(sizes)) for v in range(max(nb, nw))]
+    plans.append(([i % nb for i in range(len(sizes))], [(i + 1) % nw for i in range(len(sizes))]))
+    for vb, vw in plans:
+        outs_b = [torch.full(s, -7.0, device=dev) for s in sizes]
+        outs_w = [torch.full(s, -7.0, device=dev) for s in sizes]
+        outs_c = [torch.full(s + (64,), -7.0, device=dev) for s in sizes]
+        vb = [v % nb for v in vb]
+        umi.batch_run_fused([(umi.OP_COST_VOLUME, list(zip(dL, dR, outs_c)), umi.BatchParams(0, 0.0, 0.0, 32, 64), None),
+                             (umi.OP_WFILTER_PP, list(zip(dx, dw, outs_w)), None, vw),
+                             (umi.OP_BILATERAL, [(x, None, o) for x, o in zip(dx, outs_b)],
+                              umi.BatchParams(2, 2.0, 0.1, 0, 0), vb)])
+        _fused_check(outs_b, outs_w, outs_c, xs, ws, Ls, Rs, want_b, want_w, want_c, (vb, vw))
+
+
+@pytest.mark.parametrize("radius", [1, 3])
+def test_batch_fused_filters_only_and_graph_replay(umi, orc, dev, radius):
+    """Without a cost-volume job (filters only), other radii, and the fused
+    launch recorded in a batch graph and replayed twice."""
+    import torch
+    sizes, xs, ws, _, _ = _fused_case(20 + radius, 5, 3, 260)
+    want_b = [orc.bilateral_f64(x, radius, 1.5, 0.2) if x.size else None for x in xs]
+    want_w = [orc.wfilter_pp_f64(x, wt) if x.size else None for x, wt in zip(xs, ws)]
+    dx, dw = [_t(a, dev) for a in xs], [_t(a, dev) for a in ws]
+    outs_b = [torch.full(s, -7.0, device=dev) for s in sizes]
+    outs_w = [torch.full(s, -7.0, device=dev) for s in sizes]
+    jobs = [(umi.OP_BILATERAL, [(x, None, o) for x, o in zip(dx, outs_b)], umi.BatchParams(radius, 1.5, 0.2, 0, 0),
+             [i % umi.batch_fused_variants(umi.OP_BILATERAL) for i in range(len(sizes))]),
+            (umi.OP_WFILTER_PP, list(zip(dx, dw, outs_w)), None, None)]
+    g = umi.BatchGraph()
+    g.add_fused(jobs)
+    for _ in range(2):
+        for o in outs_b + outs_w:
+            o.fill_(-7.0)
+        g.launch()
+        torch.cuda.synchronize()
+        _fused_check(outs_b, outs_w, [], xs, ws, [], [], want_b, want_w, [], radius)
+    g.close()
+
+
+def test_batch_fused_autotune_per_size_class(umi, dev, tmp_path, monkeypatch):
+    """The autotuner picks one variant per operator and size class and fills
+    every image's variant from its class."""
+    import torch
+    from umi_gb300 import autotune
+    monkeypatch.setenv("UMI_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    sizes = [(64, 64), (700, 600), (1100, 1000), (100, 90)]
+    ins = [torch.rand(s, device=dev) for s in sizes]
+    wts = [torch.rand(s + (3, 3), device=dev) for s in sizes]
+    outs = [torch.empty(s, device=dev) for s in sizes]
+    jobs = [(umi.OP_BILATERAL, [(i, None, o) for i, o in zip(ins, outs)], umi.BatchParams(2, 2.0, 0.1, 0, 0), None),
+            (umi.OP_WFILTER_PP, list(zip(ins, wts, outs)), None, None)]
+    tuned, report = autotune.tuned_fused_variants(jobs, reps=1)
+    assert set(report) == {"bilateral", "wfilter_pp"}
+    for (op, imgs, _, var), name in zip(tuned, ("bilateral", "wfilter_pp")):
+        assert len(var) == len(imgs)
+        for (inp, _, _), v in zip(imgs, var):
+            cls = autotune.image_class(*inp.shape)
+            assert report[name][cls]["variant"] == v
+            assert len(report[name][cls]["candidates_ms"]) == umi.batch_fused_variants(op)
+    # a second call is served from the cache
+    tuned2, report2 = autotune.tuned_fused_variants(jobs, reps=1)
+    assert [j[3] for j in tuned2] == [j[3] for j in tuned]
+
+
+def test_batch_fused_rejects(umi, dev):
+    import torch
+    x = torch.zeros((8, 8), device=dev)
+    cv_bad = (umi.OP_COST_VOLUME, [(x.view(1, 8, 8), x.view(1, 8, 8), torch.zeros((8, 8, 32), device=dev))],
+              umi.BatchParams(0, 0, 0, 1, 32), None)  # nd 32: not the tensor-core form
+    with pytest.raises(umi.UmiError) as e:
+        umi.batch_run_fused([cv_bad])
+    assert e.value.status == 3
+    job = (umi.OP_BILATERAL, [(x, None, x.clone())], umi.BatchParams(2, 2.0, 0.1, 0, 0), None)
+    with pytest.raises(umi.UmiError):
+        umi.batch_run_fused([job, job])  # two jobs of one operator
+    with pytest.raises(umi.UmiError):
+        umi.batch_run_fused([(umi.OP_BILATERAL, [(x, None, x.clone())], umi.BatchParams(2, 2.0, 0.1, 0, 0), [9])])

@@ -57,6 +57,9 @@ SIGNATURES = {
     "umi_batch_graph_create": ([_vp], ctypes.c_int),
     "umi_batch_graph_add": ([_vp, _i32, _vp, _i32, _vp, _i32], ctypes.c_int),
     "umi_batch_graph_launch": ([_vp, _vp], ctypes.c_int),
+    "umi_batch_fused_variants": ([_i32], _i32),
+    "umi_batch_run_fused": ([_vp, _i32, _vp], ctypes.c_int),
+    "umi_batch_graph_add_fused": ([_vp, _vp, _i32], ctypes.c_int),
     "umi_batch_graph_destroy": ([_vp], None),
     "umi_filter3x3_f32": ([_vp, _vp, _i32, _i32, _vp, _f32, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
@@ -231,6 +234,12 @@ class BatchGraph:
         check(lib().umi_batch_graph_add(self._h, op, table, len(images), ctypes.byref(prm), variant),
               "umi_batch_graph_add")
         self._keep.append((table, prm))
+
+    def add_fused(self, jobs):
+        """Record one fused launch (batch_run_fused's job list)."""
+        arr, keep = _fused_jobs(jobs)
+        check(lib().umi_batch_graph_add_fused(self._h, arr, len(jobs)), "umi_batch_graph_add_fused")
+        self._keep.append((arr, keep))
 
     def launch(self, stream=None):
         check(lib().umi_batch_graph_launch(self._h, _stream_ptr(stream)), "umi_batch_graph_launch")
@@ -627,6 +636,40 @@ def batch_run(op, images, params=None, variant=-1, stream=None):
 
 def batch_variants(op):
     return int(lib().umi_batch_variants(op))
+
+
+class BatchJob(ctypes.Structure):
+    _fields_ = [("op", _i32), ("images", _vp), ("n_images", _i32), ("params", BatchParams), ("variants", _vp)]
+
+
+def batch_fused_variants(op):
+    """Variants (tile shape, pixels per thread) of `op` inside the fused launch."""
+    return int(lib().umi_batch_fused_variants(op))
+
+
+def _fused_jobs(jobs):
+    """jobs: [(op, images, params_or_None, variants_or_None), ...] -> (BatchJob array, objects to keep alive)."""
+    arr = (BatchJob * max(len(jobs), 1))()
+    keep = []
+    for k, (op, images, params, variants) in enumerate(jobs):
+        tab = _batch_table(images)
+        var = None
+        if variants is not None:
+            if len(variants) != len(images):
+                raise ValueError("one variant per image")
+            var = (_i32 * max(len(variants), 1))(*[int(v) for v in variants])
+        prm = params if params is not None else BatchParams()
+        arr[k] = BatchJob(op, ctypes.cast(tab, _vp), len(images), prm, ctypes.cast(var, _vp) if var is not None else None)
+        keep += [tab, var]
+    return arr, keep
+
+
+def batch_run_fused(jobs, stream=None):
+    """One persistent launch for a whole batch step (umi_batch_run_fused):
+    jobs = [(op, [(in, aux_or_None, out), ...], params_or_None, per-image variants_or_None), ...],
+    at most one job per operator."""
+    arr, keep = _fused_jobs(jobs)
+    check(lib().umi_batch_run_fused(arr, len(jobs), _stream_ptr(stream)), "umi_batch_run_fused")
 
 
 def autotune_batch(op, images, params=None, reps=3, stream=None):

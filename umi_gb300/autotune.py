@@ -60,3 +60,79 @@ def tuned_variant(op: int, images, params=None, reps: int = 3, refresh: bool = F
     cache[key] = {"variant": v, "ms": ms, "variants": U.batch_variants(op)}
     _store(cache)
     return v, ms, False
+
+
+# ---- the fused launch: one variant per operator and image size class
+
+SIZE_CLASSES = ((18, "px<2^18"), (20, "2^18<=px<2^20"), (99, "px>=2^20"))
+
+
+def image_class(h: int, w: int) -> str:
+    """Size class of one image by its pixel count (log2 buckets)."""
+    lg = math.log2(max(1, h * w))
+    for bound, name in SIZE_CLASSES:
+        if lg < bound:
+            return name
+    return SIZE_CLASSES[-1][1]
+
+
+def _time_fused(jobs, reps: int) -> float:
+    import torch
+    U.batch_run_fused(jobs)  # warm-up
+    st = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        U.batch_run_fused(jobs)
+    b.record(st)
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def tuned_fused_variants(jobs, reps: int = 3, refresh: bool = False):
+    """Per-image variants for batch_run_fused, chosen per operator and size class.
+
+    jobs: batch_run_fused's list [(op, images, params, variants_or_None), ...].
+    For each filter operator (bilateral, per-pixel wfilter) and each size
+    class present in its images, every fused variant of the operator (tile
+    width x height = the P block, pixels per thread = Expand) is timed on that
+    class's images alone (one fused launch per candidate, CUDA events) and the
+    fastest wins; winners are cached per (GPU, operator, radius, class).  The
+    cost volume has one fused form (tensor-core tiles of 128 pixels x 64
+    disparities).  Returns (jobs with their variants filled in, report) with
+    report[op_name][class] = {"variant", "ms", "images", "candidates_ms"}.
+    """
+    import torch
+    cache = _load()
+    gpu = torch.cuda.get_device_name()
+    out_jobs, report = [], {}
+    for op, images, params, _ in jobs:
+        nvar = U.batch_fused_variants(op)
+        if op == U.OP_COST_VOLUME or nvar <= 1:
+            out_jobs.append((op, images, params, None))
+            continue
+        classes = {}
+        for i, (inp, _, _) in enumerate(images):
+            classes.setdefault(image_class(inp.shape[-2], inp.shape[-1]), []).append(i)
+        variants = [0] * len(images)
+        rep = {}
+        radius = params.radius if params is not None else 0
+        for cls, idx in sorted(classes.items()):
+            key = f"{gpu}|fused|{OP_NAMES[op]}|r{radius}|{cls}"
+            hit = cache.get(key)
+            if not refresh and hit and hit.get("variants") == nvar:
+                best, ms, cand = hit["variant"], hit["ms"], hit.get("candidates_ms")
+            else:
+                sub = [images[i] for i in idx]
+                cand = {v: _time_fused([(op, sub, params, [v] * len(sub))], reps) for v in range(nvar)}
+                best = min(cand, key=cand.get)
+                ms = cand[best]
+                cache[key] = {"variant": best, "ms": ms, "variants": nvar,
+                              "candidates_ms": {str(k): v for k, v in cand.items()}}
+            for i in idx:
+                variants[i] = best
+            rep[cls] = {"variant": best, "ms": ms, "images": len(idx), "candidates_ms": cand}
+        report[OP_NAMES[op]] = rep
+        out_jobs.append((op, images, params, variants))
+    _store(cache)
+    return out_jobs, report

@@ -30,7 +30,8 @@ struct Img {
 	const float* aux;
 	float* out;
 	int h, w, tiles_x;
-	int vec;  // all pointers 16-byte aligned and w % 4 == 0
+	int vec;   // all pointers 16-byte aligned and w % 4 == 0
+	int kind;  // batch_fused_kernel's filter phase: which operator variant serves this image
 };
 
 struct Table {
@@ -66,17 +67,17 @@ struct BilParams {
 	float lsw[7][7];
 };
 
-template <int R, int TW, int TH, int PPT>
+template <int R, int TW, int TH, int PPT, int NTH = NT>
 struct Bilateral {
 	static constexpr int SW = TW + 2 * R, SH = TH + 2 * R;
-	static_assert(TW * TH / PPT == NT, "one pixel column of PPT per thread");
+	static_assert(TW * TH / PPT == NTH && TH % PPT == 0, "one pixel column of PPT per thread");
 	static constexpr size_t smem = sizeof(float) * SW * SH;
 	static int tiles_x(int w) { return umi::ceil_div(w, TW); }
 	static int tiles(int h, int w) { return tiles_x(w) * umi::ceil_div(h, TH); }
 	__device__ static void tile(const Img& im, int t, const BilParams& p, float* sm) {
 		const int ty = t / im.tiles_x, tx = t - ty * im.tiles_x;
 		const int X0 = tx * TW, Y0 = ty * TH;
-		for (int i = threadIdx.x; i < SW * SH; i += NT) {
+		for (int i = threadIdx.x; i < SW * SH; i += NTH) {
 			const int sy = i / SW, sx = i - sy * SW;
 			const int gy = Y0 + sy - R, gx = X0 + sx - R;
 			sm[i] = (gy >= 0 && gy < im.h && gx >= 0 && gx < im.w) ? __ldg(im.in + (size_t)gy * im.w + gx) : 0.0f;
@@ -123,9 +124,9 @@ __device__ __forceinline__ float4 row4(const Img& im, int y, int x) {
 	return v;
 }
 
-template <int RY>
+template <int RY, int NTH = NT>
 struct WFilter {
-	static constexpr int WARPS = NT / 32;
+	static constexpr int WARPS = NTH / 32;
 	static constexpr int TH = WARPS * RY;
 	static constexpr size_t smem = 0;
 	static int tiles_x(int w) { return umi::ceil_div(w, 128); }
@@ -415,12 +416,15 @@ struct CostVolumeTc {  // tiles of 128 pixels of one row
 	static int tiles(int h, int w) { return tiles_x(w) * h; }
 };
 
-__global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Table t, const cvtc::Params prm, int* err) {
+// The whole cost-volume pass of one CTA (every role), used by
+// cost_volume_tc_kernel and as the first phase of batch_fused_kernel.
+// Returns after every role has finished and TMEM is freed (ends with a CTA
+// barrier), so the caller may reuse the shared memory.
+__device__ __forceinline__ void cv_tc_phase(const Table& t, const cvtc::Params& prm, int* err, uint8_t* smem_raw) {
 	using namespace umi_tc;
 	using namespace cvtc;
-	extern __shared__ uint8_t smem_raw[];
-	// 1024-byte aligned start (128-byte swizzled TMA tiles), formed by indexing
-	// the shared array so that the compiler keeps shared-memory accesses
+	// 1024-byte aligned start (128-byte swizzled operand tiles), formed by
+	// indexing the shared array so that the compiler keeps shared-memory accesses
 	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* outbuf = base + 2 * STAGE_BYTES;
 	uint64_t* full = reinterpret_cast<uint64_t*>(outbuf + 8 * OUT_WARP_BYTES);  // [2]
@@ -553,6 +557,12 @@ __global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Tabl
 		tc_fence_after();
 		tmem_dealloc(tmem, TMEM_COLS);
 	}
+	__syncthreads();
+}
+
+__global__ void __launch_bounds__(cvtc::NTH, 1) cost_volume_tc_kernel(const Table t, const cvtc::Params prm, int* err) {
+	extern __shared__ __align__(1024) uint8_t smem_raw[];
+	cv_tc_phase(t, prm, err, smem_raw);
 }
 
 // ------------------------------------------------------------------ launcher
@@ -637,6 +647,163 @@ umi_status launch_cv_tc(const umi_batch_image* images, int n, int channels, cuda
 	return umi::launch_status("cost_volume_tc_kernel");
 }
 
+// ------------------------------------------------------------------ one launch for a whole batch step
+// batch_fused_kernel serves the three operators of a batch step in one
+// persistent launch (one CTA per SM, the 480 threads of the tensor-core cost
+// volume): every CTA first takes its share of the cost-volume tiles (the
+// warp-specialised pass of cost_volume_tc_kernel, static round robin), then,
+// with all 15 warps, its share of one queue that holds the per-pixel-weight
+// filter's and the bilateral filter's tiles of every image.  Each image of
+// that queue carries its own variant (tile shape = P block, pixels per
+// thread = Expand), chosen per operator and size class by the autotuner.
+constexpr int FNT = cvtc::NTH;
+enum : int { kKindBil = 0, kKindWf = 8 };
+constexpr int kFusedBilVariants = 4, kFusedWfVariants = 3;
+template <int R> using FBil0 = Bilateral<R, 32, 30, 2, FNT>;
+template <int R> using FBil1 = Bilateral<R, 32, 60, 4, FNT>;
+template <int R> using FBil2 = Bilateral<R, 96, 20, 4, FNT>;
+template <int R> using FBil3 = Bilateral<R, 32, 15, 1, FNT>;
+using FWf0 = WFilter<4, FNT>;
+using FWf1 = WFilter<2, FNT>;
+using FWf2 = WFilter<1, FNT>;
+constexpr size_t kFusedSimtSmem = sizeof(float) * (96 + 6) * (60 + 6);  // covers every bilateral variant at r <= 3
+
+template <int R>
+__global__ void __launch_bounds__(FNT, 1)
+batch_fused_kernel(const Table cv, const cvtc::Params cvp, const Table q, const BilParams bp, int* err) {
+	extern __shared__ __align__(1024) uint8_t smem_raw[];
+	if (cv.start[cv.n] > 0) cv_tc_phase(cv, cvp, err, smem_raw);  // uniform over the CTA
+	float* sm = reinterpret_cast<float*>(smem_raw);
+	const int total = q.start[q.n];
+	for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+		const int i = find_image(q, tile);
+		const Img& im = q.img[i];
+		const int lt = tile - q.start[i];
+		switch (im.kind) {  // uniform over the CTA: every thread serves the same tile
+			case kKindBil + 0: FBil0<R>::tile(im, lt, bp, sm); break;
+			case kKindBil + 1: FBil1<R>::tile(im, lt, bp, sm); break;
+			case kKindBil + 2: FBil2<R>::tile(im, lt, bp, sm); break;
+			case kKindBil + 3: FBil3<R>::tile(im, lt, bp, sm); break;
+			case kKindWf + 0: FWf0::tile(im, lt, NoParams{}, sm); break;
+			case kKindWf + 1: FWf1::tile(im, lt, NoParams{}, sm); break;
+			default: FWf2::tile(im, lt, NoParams{}, sm); break;
+		}
+	}
+}
+
+// tiles_x and tile count of an image under a fused kind
+void fused_tiles(int kind, int h, int w, int* tx, int64_t* nt) {
+	switch (kind) {
+		case kKindBil + 0: *tx = FBil0<1>::tiles_x(w); *nt = FBil0<1>::tiles(h, w); return;
+		case kKindBil + 1: *tx = FBil1<1>::tiles_x(w); *nt = FBil1<1>::tiles(h, w); return;
+		case kKindBil + 2: *tx = FBil2<1>::tiles_x(w); *nt = FBil2<1>::tiles(h, w); return;
+		case kKindBil + 3: *tx = FBil3<1>::tiles_x(w); *nt = FBil3<1>::tiles(h, w); return;
+		case kKindWf + 0: *tx = FWf0::tiles_x(w); *nt = FWf0::tiles(h, w); return;
+		case kKindWf + 1: *tx = FWf1::tiles_x(w); *nt = FWf1::tiles(h, w); return;
+		default: *tx = FWf2::tiles_x(w); *nt = FWf2::tiles(h, w); return;
+	}
+}
+
+umi_status fused_queue(const umi_batch_job* const jobs[2], Table& t) {
+	t.n = 0;
+	t.start[0] = 0;
+	for (int jb = 0; jb < 2; ++jb) {
+		const umi_batch_job* j = jobs[jb];
+		if (!j) continue;
+		const bool wf = j->op == UMI_OP_WFILTER_PP;
+		const int nvar = wf ? kFusedWfVariants : kFusedBilVariants;
+		for (int i = 0; i < j->n_images; ++i) {
+			const umi_batch_image& b = j->images[i];
+			if (b.h < 0 || b.w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: negative size");
+			if (b.h == 0 || b.w == 0) continue;
+			if (!b.in || !b.out || (wf && !b.aux)) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: null pointer");
+			if (t.n == MAXIMG) return umi::fail(UMI_ERR_UNSUPPORTED, "fused batch: more than %d filter images", MAXIMG);
+			const int v = j->variants ? j->variants[i] : 0;
+			if (v < 0 || v >= nvar) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: variant %d (0..%d)", v, nvar - 1);
+			Img& m = t.img[t.n];
+			m.in = b.in; m.aux = b.aux; m.out = b.out; m.h = b.h; m.w = b.w;
+			m.vec = umi::aligned(b.in, 16) && umi::aligned(b.out, 16) && (!b.aux || umi::aligned(b.aux, 16)) &&
+			        (b.w % 4) == 0;
+			m.kind = (wf ? kKindWf : kKindBil) + v;
+			int64_t nt = 0;
+			fused_tiles(m.kind, b.h, b.w, &m.tiles_x, &nt);
+			if (t.start[t.n] + nt > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "fused batch too large");
+			t.start[t.n + 1] = t.start[t.n] + (int)nt;
+			++t.n;
+		}
+	}
+	return UMI_OK;
+}
+
+template <int R>
+umi_status launch_fused_r(const Table& cv, const cvtc::Params& cvp, const Table& q, const BilParams& bp, cudaStream_t st) {
+	auto kern = batch_fused_kernel<R>;
+	const bool has_cv = cv.start[cv.n] > 0;
+	const size_t smem = has_cv ? cvtc::SMEM : kFusedSimtSmem;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cvtc::SMEM),
+	                         "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	const int tiles = std::max(cv.start[cv.n], q.start[q.n]);
+	const int grid = std::max(1, std::min(tiles, sms));  // 480 threads x 128 registers: one CTA per SM
+	kern<<<grid, FNT, smem, st>>>(cv, cvp, q, bp, nullptr);
+	return umi::launch_status("batch_fused_kernel");
+}
+
+umi_status bil_params(const umi_batch_params& bp, BilParams& p) {
+	if (bp.radius < 1 || bp.radius > 3) return umi::fail(UMI_ERR_UNSUPPORTED, "bilateral: radius %d (1..3)", bp.radius);
+	if (!(bp.sigma_s > 0.0f) || !(bp.sigma_r > 0.0f)) return umi::fail(UMI_ERR_INVALID_ARG, "bilateral: sigmas must be > 0");
+	const double log2e = 1.4426950408889634;
+	p.k = (float)(-log2e / (2.0 * (double)bp.sigma_r * (double)bp.sigma_r));
+	const int r = bp.radius;
+	for (int dy = 0; dy <= 2 * r; ++dy)
+		for (int dx = 0; dx <= 2 * r; ++dx) {
+			const double a = (double)((dy - r) * (dy - r) + (dx - r) * (dx - r));
+			p.lsw[dy][dx] = (float)(-a / (2.0 * (double)bp.sigma_s * (double)bp.sigma_s) * log2e);
+		}
+	return UMI_OK;
+}
+
+umi_status run_fused(const umi_batch_job* jobs, int n_jobs, cudaStream_t st) {
+	if (n_jobs < 0 || (n_jobs > 0 && !jobs)) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: bad job list");
+	const umi_batch_job* by_op[3] = {nullptr, nullptr, nullptr};
+	for (int k = 0; k < n_jobs; ++k) {
+		const int op = jobs[k].op;
+		if (op < 0 || op > 2) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: unknown op %d", op);
+		if (by_op[op]) return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: two jobs of op %d", op);
+		if (jobs[k].n_images < 0 || jobs[k].n_images > MAXIMG || (jobs[k].n_images > 0 && !jobs[k].images))
+			return umi::fail(UMI_ERR_INVALID_ARG, "fused batch: job of op %d has a bad image list", op);
+		by_op[op] = &jobs[k];
+	}
+	Table cv;
+	cv.n = 0;
+	cv.start[0] = 0;
+	cvtc::Params cvp{0};
+	if (const umi_batch_job* j = by_op[UMI_OP_COST_VOLUME]) {
+		if (!cv_tc_eligible(j->images, j->n_images, j->params))
+			return umi::fail(UMI_ERR_UNSUPPORTED,
+			                 "fused batch: the cost volume needs nd = 64, 1..32 channels and 16-byte aligned outputs");
+		UMI_TRY(make_table<CostVolumeTc>(j->images, j->n_images, true, cv));
+		cvp.channels = j->params.channels;
+	}
+	Table q;
+	const umi_batch_job* const simt[2] = {by_op[UMI_OP_WFILTER_PP], by_op[UMI_OP_BILATERAL]};
+	UMI_TRY(fused_queue(simt, q));
+	BilParams bp{};
+	int r = 1;
+	if (const umi_batch_job* j = by_op[UMI_OP_BILATERAL]) {
+		UMI_TRY(bil_params(j->params, bp));
+		r = j->params.radius;
+	}
+	if (cv.start[cv.n] == 0 && q.start[q.n] == 0) return UMI_OK;
+	switch (r) {
+		case 1: return launch_fused_r<1>(cv, cvp, q, bp, st);
+		case 2: return launch_fused_r<2>(cv, cvp, q, bp, st);
+		default: return launch_fused_r<3>(cv, cvp, q, bp, st);
+	}
+}
+
 // Variant tables.
 constexpr int kBilVariants = 4;
 template <int R>
@@ -652,18 +819,9 @@ constexpr int kWfVariants = 3;
 constexpr int kCvVariants = 2;  // tensor cores (where eligible), FP32
 
 umi_status run_bilateral(const umi_batch_image* im, int n, const umi_batch_params& bp, int v, cudaStream_t st) {
-	if (bp.radius < 1 || bp.radius > 3) return umi::fail(UMI_ERR_UNSUPPORTED, "bilateral: radius %d (1..3)", bp.radius);
-	if (!(bp.sigma_s > 0.0f) || !(bp.sigma_r > 0.0f)) return umi::fail(UMI_ERR_INVALID_ARG, "bilateral: sigmas must be > 0");
 	BilParams p{};
-	const double log2e = 1.4426950408889634;
-	p.k = (float)(-log2e / (2.0 * (double)bp.sigma_r * (double)bp.sigma_r));
-	const int r = bp.radius;
-	for (int dy = 0; dy <= 2 * r; ++dy)
-		for (int dx = 0; dx <= 2 * r; ++dx) {
-			const double a = (double)((dy - r) * (dy - r) + (dx - r) * (dx - r));
-			p.lsw[dy][dx] = (float)(-a / (2.0 * (double)bp.sigma_s * (double)bp.sigma_s) * log2e);
-		}
-	switch (r) {
+	UMI_TRY(bil_params(bp, p));
+	switch (bp.radius) {
 		case 1: return run_bilateral_r<1>(im, n, p, v, st);
 		case 2: return run_bilateral_r<2>(im, n, p, v, st);
 		default: return run_bilateral_r<3>(im, n, p, v, st);
@@ -776,6 +934,20 @@ extern "C" umi_status umi_autotune_batch(int32_t op, const umi_batch_image* imag
 	return umi::ok();
 }
 
+extern "C" int32_t umi_batch_fused_variants(int32_t op) {
+	switch (op) {
+		case UMI_OP_BILATERAL: return kFusedBilVariants;
+		case UMI_OP_WFILTER_PP: return kFusedWfVariants;
+		case UMI_OP_COST_VOLUME: return 1;
+		default: return 0;
+	}
+}
+
+extern "C" umi_status umi_batch_run_fused(const umi_batch_job* jobs, int32_t n_jobs, void* stream) {
+	const umi_status st = run_fused(jobs, n_jobs, umi::as_stream(stream));
+	return st == UMI_OK ? umi::ok() : st;
+}
+
 // ---- batch graphs: a sequence of persistent batched launches recorded once
 // into a CUDA graph and replayed with one cudaGraphLaunch.
 struct umi_batch_graph {
@@ -819,6 +991,32 @@ extern "C" umi_status umi_batch_graph_add(umi_batch_graph* g, int32_t op, const 
 		cudaGraphAddChildGraphNode(&node, g->graph, g->last ? &g->last : nullptr, g->last ? 1 : 0, sub),
 		"cudaGraphAddChildGraphNode");
 	cudaGraphDestroy(sub);  // the child node holds its own copy
+	UMI_TRY(ac);
+	g->last = node;
+	++g->n_ops;
+	if (g->exec) {
+		cudaGraphExecDestroy(g->exec);
+		g->exec = nullptr;
+	}
+	return umi::ok();
+}
+
+extern "C" umi_status umi_batch_graph_add_fused(umi_batch_graph* g, const umi_batch_job* jobs, int32_t n_jobs) {
+	if (!g) return umi::fail(UMI_ERR_INVALID_ARG, "batch graph: null graph");
+	UMI_TRY(umi::cuda_status(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal),
+	                         "cudaStreamBeginCapture"));
+	const umi_status rc = run_fused(jobs, n_jobs, g->capture);
+	cudaGraph_t sub = nullptr;
+	const umi_status ec = umi::cuda_status(cudaStreamEndCapture(g->capture, &sub), "cudaStreamEndCapture");
+	if (rc != UMI_OK || ec != UMI_OK) {
+		if (sub) cudaGraphDestroy(sub);
+		return rc != UMI_OK ? rc : ec;
+	}
+	cudaGraphNode_t node = nullptr;
+	const umi_status ac = umi::cuda_status(
+		cudaGraphAddChildGraphNode(&node, g->graph, g->last ? &g->last : nullptr, g->last ? 1 : 0, sub),
+		"cudaGraphAddChildGraphNode");
+	cudaGraphDestroy(sub);
 	UMI_TRY(ac);
 	g->last = node;
 	++g->n_ops;

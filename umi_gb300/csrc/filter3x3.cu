@@ -4,13 +4,24 @@
 // 3x3 neighbourhood, PAD value outside the image) and main/wfilter3x3.cu:39-69
 // (WFilter3x3: the same with a 3x3 weight memory) for float images.
 //
-// HBM-bound: 4 bytes read + 4 bytes written per pixel.  A warp owns a
+// HBM-bound: 4 bytes read + 4 bytes written per pixel.  Zero padding on
+// 16-byte aligned rows takes TMA-staged halo tiles (filter3x3_tma_kernel,
+// below); any other padding value or alignment takes the register kernel: a warp owns a
 // 128-column strip and RY output rows; each lane keeps 4 adjacent columns of
 // three input rows in registers, loads every input row once with one 128-bit
 // load, takes the x-1 / x+4 neighbours from the adjacent lanes by shuffle
 // (the strip's edge lanes load one extra float), and writes 4 outputs with
 // one 128-bit store.  Accumulation order per output: (dy, dx) row-major, FMA.
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
 #include "common.h"
+#include "tc_common.cuh"
+
+namespace umi {
+void* tma_encode_fn();  // cuTensorMapEncodeTiled (gemm_tc.cu)
+}
 
 namespace {
 
@@ -108,6 +119,83 @@ __global__ void __launch_bounds__(WARPS * 32) filter3x3_f32_kernel(const float* 
 	}
 }
 
+// ---- TMA-staged halo tiles (zero padding, 16-byte aligned rows).
+// A CTA computes a TW x TH output tile.  One TMA box brings the input tile
+// with its halo, (TW + 8) x (TH + 2) floats from (x0 - 4, y0 - 1): the box's
+// x is kept on a 16-byte boundary (4 floats left of the tile instead of 1),
+// and the tensor map's zero fill outside the image is the reference's PAD 0.
+// Thread t owns column t % TW and TH / 2 rows: a 3 x 3 register window slides
+// down its column (three shared loads per row).  The output tile is written
+// to shared memory and leaves by one TMA tile store (clipped at the image
+// edge by the tensor map).  The wait for the box is bounded (1 s): a CTA
+// whose box never lands writes NaN into its tile and returns after a second
+// bounded wait for the copy.
+constexpr int TTW = 128, TTH = 32, TNT = 256;
+constexpr int TIN_W = TTW + 8, TIN_H = TTH + 2;
+constexpr int TROWS = TTH / (TNT / TTW);  // output rows per thread
+constexpr int TIN_WORDS = (TIN_W * TIN_H + 31) & ~31;  // input tile, rounded to 128 bytes
+constexpr size_t TSMEM = (size_t)4 * (TIN_WORDS + TTW * TTH) + 128;
+static_assert(TIN_WORDS % 32 == 0, "TMA tiles in shared memory start on 128-byte boundaries");
+
+__global__ void __launch_bounds__(TNT) filter3x3_tma_kernel(const __grid_constant__ CUtensorMap tin,
+                                                             const __grid_constant__ CUtensorMap tout, float* __restrict__ out,
+                                                             const FilterGeom g, const Weights9 wt) {
+	using namespace umi_tc;
+	extern __shared__ __align__(128) uint8_t smem_raw[];
+	float* sin = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+	float* sout = sin + TIN_WORDS;  // 128-byte aligned (TMA store source)
+	__shared__ __align__(8) uint64_t bar;
+	__shared__ int abort_sh;
+	const int x0 = blockIdx.x * TTW, y0 = blockIdx.y * TTH;
+	if (threadIdx.x == 0) {
+		mbar_init(&bar, 1);
+		abort_sh = 0;
+		fence_mbar_init();
+	}
+	__syncthreads();
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+	asm volatile("griddepcontrol.launch_dependents;");
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+	if (threadIdx.x == 0) {
+		mbar_arrive_expect_tx(&bar, (uint32_t)(4 * TIN_W * TIN_H));
+		tma_load_2d(sin, &tin, &bar, x0 - 4, y0 - 1);
+	}
+	mbar_wait(&bar, 0, &abort_sh, nullptr, 0);
+	__syncthreads();  // every thread sees the same abort flag
+	const int c = threadIdx.x % TTW, r0 = (threadIdx.x / TTW) * TROWS;
+	if (abort_sh) {  // the box never landed: mark the tile, let the copy finish, return (uniform)
+		for (int r = r0; r < r0 + TROWS; ++r)
+			if (y0 + r < g.h && x0 + c < g.w) out[(size_t)(y0 + r) * g.w + x0 + c] = __int_as_float(0x7fc00000);
+		volatile int own = 0;
+		mbar_wait(&bar, 0, &own, nullptr, 0);
+		return;
+	}
+	// input column of output column c, dx = -1: tile column c + 3
+	const float* col = sin + c + 3;
+	float a0 = col[r0 * TIN_W], a1 = col[r0 * TIN_W + 1], a2 = col[r0 * TIN_W + 2];
+	float b0 = col[(r0 + 1) * TIN_W], b1 = col[(r0 + 1) * TIN_W + 1], b2 = col[(r0 + 1) * TIN_W + 2];
+#pragma unroll
+	for (int k = 0; k < TROWS; ++k) {
+		const float* rr = col + (r0 + k + 2) * TIN_W;
+		const float c0 = rr[0], c1 = rr[1], c2 = rr[2];
+		float s = 0.0f;
+		s = fmaf(wt.w[0], a0, s); s = fmaf(wt.w[1], a1, s); s = fmaf(wt.w[2], a2, s);
+		s = fmaf(wt.w[3], b0, s); s = fmaf(wt.w[4], b1, s); s = fmaf(wt.w[5], b2, s);
+		s = fmaf(wt.w[6], c0, s); s = fmaf(wt.w[7], c1, s); s = fmaf(wt.w[8], c2, s);
+		sout[(r0 + k) * TTW + c] = s;
+		a0 = b0; a1 = b1; a2 = b2;
+		b0 = c0; b1 = c1; b2 = c2;
+	}
+	fence_proxy_async_smem();  // the tile's generic stores before the async-proxy store reads them
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		tma_store_2d(&tout, sout, x0, y0);
+		bulk_commit();
+		bulk_wait_all();
+	}
+}
+
 }  // namespace
 
 extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, int32_t w, const float* w9, float pad,
@@ -119,6 +207,41 @@ extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, 
 	FilterGeom g{h, w, pad, umi::aligned(in, 16) && umi::aligned(out, 16) && (w % 4) == 0};
 	Weights9 wt;
 	for (int i = 0; i < 9; ++i) wt.w[i] = w9[i];
+	uint32_t pad_bits;
+	std::memcpy(&pad_bits, &pad, 4);
+	auto enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(umi::tma_encode_fn());
+	if (g.vec && pad_bits == 0 && enc) {
+		// zero padding on aligned rows: TMA-staged halo tiles
+		CUtensorMap tin, tout;
+		const cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
+		const cuuint64_t strides[1] = {(cuuint64_t)w * 4};
+		const cuuint32_t es[2] = {1, 1};
+		const cuuint32_t bin[2] = {(cuuint32_t)TIN_W, (cuuint32_t)TIN_H};
+		const cuuint32_t bout[2] = {(cuuint32_t)TTW, (cuuint32_t)TTH};
+		CUresult r = enc(&tin, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(in), dims, strides, bin, es,
+		                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+		                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r == CUDA_SUCCESS)
+			r = enc(&tout, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, out, dims, strides, bout, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+			        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (r == CUDA_SUCCESS) {
+			UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(filter3x3_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                                              (int)TSMEM), "cudaFuncSetAttribute"));
+			cudaLaunchConfig_t cfg{};
+			cfg.gridDim = dim3(umi::ceil_div(w, TTW), umi::ceil_div(h, TTH));
+			cfg.blockDim = dim3(TNT);
+			cfg.dynamicSmemBytes = TSMEM;
+			cfg.stream = umi::as_stream(stream);
+			cudaLaunchAttribute attr[1];
+			attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+			attr[0].val.programmaticStreamSerializationAllowed = 1;
+			cfg.attrs = attr;
+			cfg.numAttrs = 1;
+			UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_tma_kernel, tin, tout, out, g, wt),
+			                         "filter3x3_tma_kernel"));
+			return umi::ok();
+		}
+	}
 	cudaLaunchConfig_t cfg{};
 	cfg.gridDim = dim3(umi::ceil_div(w, TWC), umi::ceil_div(h, WARPS * RY));
 	cfg.blockDim = dim3(WARPS * 32);
