@@ -443,6 +443,15 @@ class Batched:
     def kernels(self, dev, peaks, n=3):
         ms = {name: time_launches(lambda i, f=fn: f(), 1, n) for name, fn in self._ops()}
         ms["fused_step"] = time_launches(self.step, 1, n)
+        # the same step as three persistent launches (one per operator, their own kernels and tuned tile shapes)
+        from umi_gb300 import autotune
+        U = self.U
+        sep = []
+        for op, imgs, prm in ((U.OP_BILATERAL, self.bil, self.pb), (U.OP_WFILTER_PP, self.wf, None),
+                              (U.OP_COST_VOLUME, self.cv, self.pc)):
+            v, _, _ = autotune.tuned_variant(op, imgs, prm)
+            sep.append(lambda op=op, imgs=imgs, prm=prm, v=v: U.batch_run(op, imgs, prm, v))
+        ms["three_launches_step"] = time_launches(lambda i: [f() for f in sep], 1, n)
         return ms, None, None
 
     def cpu_setup(self):
@@ -1559,11 +1568,12 @@ def run_ours(args, wl, dist):
                 "work_per_launch": absdiff, "ms_per_launch": kms["coarse_centers"]}
     elif isinstance(wl, Batched):
         for name, kt in kms.items():
-            b = (sum(wl.BYTES.values()) if name == "fused_step" else wl.BYTES[name]) * wl.px
+            b = (sum(wl.BYTES.values()) if name.endswith("_step") else wl.BYTES[name]) * wl.px
             kernels[name] = {"ms_per_launch": kt, "achieved": b / (kt * 1e-3) / 1e9, "unit": "GB/s",
                              "frac": b / (kt * 1e-3) / 1e9 / pk["hbm_gbs"], "bytes_per_launch": b}
         kernels["bilateral"]["ex2_per_s"] = 25 * wl.px / (kms["bilateral"] * 1e-3)
         kernels["fused_step"]["note"] = "the three operators in one launch; the others are each operator alone"
+        kernels["three_launches_step"]["note"] = "the same step as three launches (one kernel per operator)"
         roof = dict(kernels["fused_step"], bound="hbm", kernel="batch_fused_kernel (all three operators)",
                     peak=pk["hbm_gbs"], **traffic_fields(NCU_TRAFFIC.get("batched_uneven_fused")),
                     peak_source=pk["source"])

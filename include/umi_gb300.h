@@ -168,6 +168,15 @@ umi_status umi_launch(const umi_plan* plan, int32_t strategy, const void* const*
  * (their Execute calls) for float images. */
 umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, int32_t w, const float* w9, float pad,
                              void* stream);
+/* The same filter with zero padding (PAD 0) through TMA-staged halo tiles:
+ * one tensor-map box per 128 x 16 tile (the map's zero fill is the padding),
+ * double-buffered in shared memory, TMA tile stores.  16-byte aligned in/out
+ * and w % 4 == 0 (else UMI_ERR_UNSUPPORTED).  The staged form of the
+ * reference's FillShm halo tile (src/UMI_gpu.h:33-83); measured slower than
+ * umi_filter3x3_f32 on GB300 (which already reads each input once from HBM),
+ * so it is not the default.  Same FMA order: results equal umi_filter3x3_f32
+ * with pad 0 bit for bit. */
+umi_status umi_filter3x3_f32_tma(const float* in, float* out, int32_t h, int32_t w, const float* w9, void* stream);
 
 /* Integral image, uint8 -> int32: out[y,x] = sum_{y'<=y, x'<=x} in[y',x'].
  * Replaces the two Execute calls of main/iimg.cu:37-82 (row prefix through a

@@ -40,16 +40,16 @@ def test_filter3x3_f32(umi, orc, dev, h, w, pad):
     assert rel.max() <= FILTER_REL_TOL, rel.max()
 
 
-@pytest.mark.parametrize("h,w", [(100, 260), (32, 128), (35, 132), (2000, 8), (1, 4), (97, 1028)])
+@pytest.mark.parametrize("h,w", [(100, 260), (32, 128), (35, 132), (2000, 8), (1, 4), (97, 1028), (4096, 1024)])
 def test_filter3x3_tma_tiles_match_register_kernel(umi, orc, dev, h, w):
-    """Zero padding on aligned rows runs the TMA-staged halo tiles; a pad of
-    -0.0 (the same values, other bits) runs the register kernel: both use the
-    same (dy, dx) FMA order, so they agree exactly, and both match FP64."""
+    """The TMA-staged halo tiles (umi_filter3x3_f32_tma: ragged edge tiles,
+    several tiles per persistent CTA at 2000 rows) and the register kernel use
+    the same (dy, dx) FMA order: they agree exactly, and both match FP64."""
     from umi_gb300 import workloads
     x, w9 = workloads.filter_image(seed=h + w, h=h, w=w)
     xt = _t(x, dev)
-    tma = umi.filter3x3_f32(xt, w9, pad=0.0).cpu().numpy()
-    reg = umi.filter3x3_f32(xt, w9, pad=-0.0).cpu().numpy()
+    tma = umi.filter3x3_f32_tma(xt, w9).cpu().numpy()
+    reg = umi.filter3x3_f32(xt, w9, pad=0.0).cpu().numpy()
     assert np.array_equal(tma, reg)
     want = orc.filter3x3_f64(x, w9, pad=0.0)
     rel = np.abs(tma - want) / np.maximum(np.abs(want), _filter_scale(x, w9, 0.0))
@@ -61,6 +61,8 @@ def test_filter3x3_rejects_alias(umi, dev):
     x = torch.zeros(8, 8, device=dev)
     with pytest.raises(umi.UmiError):
         umi.filter3x3_f32(x, [0.0] * 9, out=x)
+    with pytest.raises(umi.UmiError):
+        umi.filter3x3_f32_tma(torch.zeros(8, 6, device=dev), [0.0] * 9)  # w % 4 != 0
 
 
 # ---------------------------------------------------------------- iimg

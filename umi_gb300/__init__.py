@@ -62,6 +62,7 @@ SIGNATURES = {
     "umi_batch_graph_add_fused": ([_vp, _vp, _i32], ctypes.c_int),
     "umi_batch_graph_destroy": ([_vp], None),
     "umi_filter3x3_f32": ([_vp, _vp, _i32, _i32, _vp, _f32, _vp], ctypes.c_int),
+    "umi_filter3x3_f32_tma": ([_vp, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_workspace_bytes": ([_i32, _i32], _sz),
     "umi_iimg_u8_i32": ([_vp, _vp, _i32, _i32, _vp, _sz, _vp], ctypes.c_int),
     "umi_iimg_u8_i32_noalloc": ([_vp, _vp, _i32, _i32, _vp], ctypes.c_int),
@@ -315,6 +316,19 @@ def filter3x3_f32(inp, w9, pad: float = 0.0, out=None, stream=None):
     wv = (ctypes.c_float * 9)(*[float(v) for v in list(w9)])
     check(lib().umi_filter3x3_f32(_ptr(inp), _ptr(out), h, w, wv, float(pad), _stream_ptr(stream)),
           "umi_filter3x3_f32")
+    return out
+
+
+def filter3x3_f32_tma(inp, w9, out=None, stream=None):
+    """The zero-padded 3x3 filter through TMA-staged halo tiles (umi_filter3x3_f32_tma)."""
+    import torch
+    _need(inp, torch.float32, "inp")
+    h, w = inp.shape
+    if out is None:
+        out = torch.empty_like(inp)
+    _need(out, torch.float32, "out")
+    wv = (ctypes.c_float * 9)(*[float(v) for v in list(w9)])
+    check(lib().umi_filter3x3_f32_tma(_ptr(inp), _ptr(out), h, w, wv, _stream_ptr(stream)), "umi_filter3x3_f32_tma")
     return out
 
 

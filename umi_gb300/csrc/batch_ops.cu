@@ -83,6 +83,29 @@ struct Bilateral {
 			sm[i] = (gy >= 0 && gy < im.h && gx >= 0 && gx < im.w) ? __ldg(im.in + (size_t)gy * im.w + gx) : 0.0f;
 		}
 		__syncthreads();
+		compute(im, t, p, sm);
+		__syncthreads();
+	}
+	// The halo tile of tile t by 4-byte cp.async (zero fill outside the image),
+	// committed as one group of this thread: lets the next tile's loads run
+	// while the current one is computed (batch_fused_kernel).
+	__device__ static void stage_async(const Img& im, int t, float* sm) {
+		const int ty = t / im.tiles_x, tx = t - ty * im.tiles_x;
+		const int X0 = tx * TW, Y0 = ty * TH;
+		for (int i = threadIdx.x; i < SW * SH; i += NTH) {
+			const int sy = i / SW, sx = i - sy * SW;
+			const int gy = Y0 + sy - R, gx = X0 + sx - R;
+			const bool in = gy >= 0 && gy < im.h && gx >= 0 && gx < im.w;
+			const unsigned d = (unsigned)__cvta_generic_to_shared(sm + i);
+			const float* src = in ? im.in + (size_t)gy * im.w + gx : im.in;
+			asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(in ? 4 : 0) : "memory");
+		}
+		asm volatile("cp.async.commit_group;" ::: "memory");
+	}
+	// Outputs of tile t from its staged halo tile.
+	__device__ static void compute(const Img& im, int t, const BilParams& p, const float* sm) {
+		const int ty = t / im.tiles_x, tx = t - ty * im.tiles_x;
+		const int X0 = tx * TW, Y0 = ty * TH;
 		const int lx = threadIdx.x % TW, ly0 = (threadIdx.x / TW) * PPT;
 #pragma unroll
 		for (int q = 0; q < PPT; ++q) {
@@ -102,7 +125,6 @@ struct Bilateral {
 			const int gy = Y0 + ly, gx = X0 + lx;
 			if (gy < im.h && gx < im.w) im.out[(size_t)gy * im.w + gx] = wx / ws;
 		}
-		__syncthreads();
 	}
 };
 
@@ -666,29 +688,66 @@ template <int R> using FBil3 = Bilateral<R, 32, 15, 1, FNT>;
 using FWf0 = WFilter<4, FNT>;
 using FWf1 = WFilter<2, FNT>;
 using FWf2 = WFilter<1, FNT>;
-constexpr size_t kFusedSimtSmem = sizeof(float) * (96 + 6) * (60 + 6);  // covers every bilateral variant at r <= 3
+constexpr size_t kFusedSimtSmem = sizeof(float) * (96 + 6) * (60 + 6);  // one halo buffer, any bilateral variant at r <= 3
 
 template <int R>
 __global__ void __launch_bounds__(FNT, 1)
 batch_fused_kernel(const Table cv, const cvtc::Params cvp, const Table q, const BilParams bp, int* err) {
 	extern __shared__ __align__(1024) uint8_t smem_raw[];
 	if (cv.start[cv.n] > 0) cv_tc_phase(cv, cvp, err, smem_raw);  // uniform over the CTA
+	// Filter phase.  Bilateral halo tiles are double-buffered: the next
+	// bilateral tile's cp.async loads run while the current one is computed.
 	float* sm = reinterpret_cast<float*>(smem_raw);
+	constexpr int BUFW = (int)(kFusedSimtSmem / sizeof(float));
 	const int total = q.start[q.n];
+	auto stage = [&](const Img& im, int lt, float* b) {
+		switch (im.kind) {
+			case kKindBil + 0: FBil0<R>::stage_async(im, lt, b); break;
+			case kKindBil + 1: FBil1<R>::stage_async(im, lt, b); break;
+			case kKindBil + 2: FBil2<R>::stage_async(im, lt, b); break;
+			default: FBil3<R>::stage_async(im, lt, b); break;
+		}
+	};
+	int buf = 0;
+	bool staged = false;  // the current tile's halo is already in sm[buf]
 	for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
 		const int i = find_image(q, tile);
 		const Img& im = q.img[i];
 		const int lt = tile - q.start[i];
-		switch (im.kind) {  // uniform over the CTA: every thread serves the same tile
-			case kKindBil + 0: FBil0<R>::tile(im, lt, bp, sm); break;
-			case kKindBil + 1: FBil1<R>::tile(im, lt, bp, sm); break;
-			case kKindBil + 2: FBil2<R>::tile(im, lt, bp, sm); break;
-			case kKindBil + 3: FBil3<R>::tile(im, lt, bp, sm); break;
-			case kKindWf + 0: FWf0::tile(im, lt, NoParams{}, sm); break;
-			case kKindWf + 1: FWf1::tile(im, lt, NoParams{}, sm); break;
-			default: FWf2::tile(im, lt, NoParams{}, sm); break;
+		if (im.kind >= kKindWf) {  // uniform over the CTA: every thread serves the same tile
+			switch (im.kind) {
+				case kKindWf + 0: FWf0::tile(im, lt, NoParams{}, sm); break;
+				case kKindWf + 1: FWf1::tile(im, lt, NoParams{}, sm); break;
+				default: FWf2::tile(im, lt, NoParams{}, sm); break;
+			}
+			staged = false;
+			continue;
 		}
+		float* cur = sm + buf * BUFW;
+		if (!staged) stage(im, lt, cur);
+		const int next = tile + (int)gridDim.x;
+		bool prefetched = false;
+		if (next < total) {
+			const int ni = find_image(q, next);
+			if (q.img[ni].kind < kKindWf) {
+				stage(q.img[ni], next - q.start[ni], sm + (buf ^ 1) * BUFW);
+				prefetched = true;
+			}
+		}
+		if (prefetched) asm volatile("cp.async.wait_group 1;" ::: "memory");
+		else asm volatile("cp.async.wait_group 0;" ::: "memory");
+		__syncthreads();  // the current halo tile is complete for every thread
+		switch (im.kind) {
+			case kKindBil + 0: FBil0<R>::compute(im, lt, bp, cur); break;
+			case kKindBil + 1: FBil1<R>::compute(im, lt, bp, cur); break;
+			case kKindBil + 2: FBil2<R>::compute(im, lt, bp, cur); break;
+			default: FBil3<R>::compute(im, lt, bp, cur); break;
+		}
+		__syncthreads();  // sm[buf] is free for the tile after next
+		buf ^= 1;
+		staged = prefetched;
 	}
+	asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // tiles_x and tile count of an image under a fused kind
@@ -739,7 +798,8 @@ template <int R>
 umi_status launch_fused_r(const Table& cv, const cvtc::Params& cvp, const Table& q, const BilParams& bp, cudaStream_t st) {
 	auto kern = batch_fused_kernel<R>;
 	const bool has_cv = cv.start[cv.n] > 0;
-	const size_t smem = has_cv ? cvtc::SMEM : kFusedSimtSmem;
+	const size_t smem = has_cv ? cvtc::SMEM : 2 * kFusedSimtSmem;
+	static_assert(2 * kFusedSimtSmem <= cvtc::SMEM, "two halo buffers fit the cost volume's shared memory");
 	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cvtc::SMEM),
 	                         "cudaFuncSetAttribute"));
 	int dev = 0, sms = 0;

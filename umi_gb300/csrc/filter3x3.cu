@@ -4,17 +4,24 @@
 // 3x3 neighbourhood, PAD value outside the image) and main/wfilter3x3.cu:39-69
 // (WFilter3x3: the same with a 3x3 weight memory) for float images.
 //
-// HBM-bound: 4 bytes read + 4 bytes written per pixel.  Zero padding on
-// 16-byte aligned rows takes TMA-staged halo tiles (filter3x3_tma_kernel,
-// below); any other padding value or alignment takes the register kernel: a warp owns a
+// HBM-bound: 4 bytes read + 4 bytes written per pixel.  A warp owns a
 // 128-column strip and RY output rows; each lane keeps 4 adjacent columns of
 // three input rows in registers, loads every input row once with one 128-bit
 // load, takes the x-1 / x+4 neighbours from the adjacent lanes by shuffle
 // (the strip's edge lanes load one extra float), and writes 4 outputs with
 // one 128-bit store.  Accumulation order per output: (dy, dx) row-major, FMA.
+// This form reaches the HBM copy rate on large frames (7.0 TB/s at 8192^2).
+//
+// umi_filter3x3_f32_tma is the same filter with TMA-staged halo tiles
+// (filter3x3_tma_kernel: one box per tile with the tensor map's zero fill as
+// the padding, double-buffered, TMA tile stores).  Measured on GB300 it is
+// slower than the register form at every size from 1024^2 to 8192^2 (5.6 vs
+// 7.0 TB/s at 8192^2): each input is used by three rows of one warp already,
+// so staging adds shared-memory traffic without saving DRAM traffic.  It is
+// kept as a separate entry point, not the default.
 #include <cudaTypedefs.h>
 
-#include <cstring>
+#include <algorithm>
 
 #include "common.h"
 #include "tc_common.cuh"
@@ -120,35 +127,38 @@ __global__ void __launch_bounds__(WARPS * 32) filter3x3_f32_kernel(const float* 
 }
 
 // ---- TMA-staged halo tiles (zero padding, 16-byte aligned rows).
-// A CTA computes a TW x TH output tile.  One TMA box brings the input tile
-// with its halo, (TW + 8) x (TH + 2) floats from (x0 - 4, y0 - 1): the box's
-// x is kept on a 16-byte boundary (4 floats left of the tile instead of 1),
-// and the tensor map's zero fill outside the image is the reference's PAD 0.
-// Thread t owns column t % TW and TH / 2 rows: a 3 x 3 register window slides
-// down its column (three shared loads per row).  The output tile is written
-// to shared memory and leaves by one TMA tile store (clipped at the image
-// edge by the tensor map).  The wait for the box is bounded (1 s): a CTA
-// whose box never lands writes NaN into its tile and returns after a second
-// bounded wait for the copy.
-constexpr int TTW = 128, TTH = 32, TNT = 256;
+// Persistent CTAs walk tiles t = blockIdx.x, + gridDim.x, ... of TW x TH
+// outputs.  One TMA box brings a tile's input with its halo, (TW + 8) x
+// (TH + 2) floats from (x0 - 4, y0 - 1): the box's x stays on a 16-byte
+// boundary (4 floats left of the tile instead of 1), and the tensor map's
+// zero fill outside the image is the reference's PAD 0.  Two input buffers:
+// the next tile's box is in flight while this one is computed.  Thread t owns
+// column t % TW and TH / 2 rows: a 3 x 3 register window slides down its
+// column.  Outputs go to one of two shared tiles and leave by one TMA tile
+// store each (clipped at the image edge by the tensor map), overlapping the
+// next tile.  Waits are bounded (1 s): a CTA whose box never lands writes
+// NaN into that tile, lets its copies finish and returns.
+constexpr int TTW = 128, TTH = 16, TNT = 256;
 constexpr int TIN_W = TTW + 8, TIN_H = TTH + 2;
 constexpr int TROWS = TTH / (TNT / TTW);  // output rows per thread
 constexpr int TIN_WORDS = (TIN_W * TIN_H + 31) & ~31;  // input tile, rounded to 128 bytes
-constexpr size_t TSMEM = (size_t)4 * (TIN_WORDS + TTW * TTH) + 128;
-static_assert(TIN_WORDS % 32 == 0, "TMA tiles in shared memory start on 128-byte boundaries");
+constexpr int TOUT_WORDS = TTW * TTH;
+constexpr size_t TSMEM = (size_t)4 * (2 * TIN_WORDS + 2 * TOUT_WORDS) + 128;
+static_assert(TIN_WORDS % 32 == 0 && TOUT_WORDS % 32 == 0, "TMA tiles in shared memory start on 128-byte boundaries");
 
 __global__ void __launch_bounds__(TNT) filter3x3_tma_kernel(const __grid_constant__ CUtensorMap tin,
                                                              const __grid_constant__ CUtensorMap tout, float* __restrict__ out,
-                                                             const FilterGeom g, const Weights9 wt) {
+                                                             const FilterGeom g, const Weights9 wt, int tiles_x,
+                                                             int ntiles) {
 	using namespace umi_tc;
 	extern __shared__ __align__(128) uint8_t smem_raw[];
 	float* sin = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
-	float* sout = sin + TIN_WORDS;  // 128-byte aligned (TMA store source)
-	__shared__ __align__(8) uint64_t bar;
+	float* sout = sin + 2 * TIN_WORDS;  // 128-byte aligned (TMA store sources)
+	__shared__ __align__(8) uint64_t bar[2];
 	__shared__ int abort_sh;
-	const int x0 = blockIdx.x * TTW, y0 = blockIdx.y * TTH;
 	if (threadIdx.x == 0) {
-		mbar_init(&bar, 1);
+		mbar_init(&bar[0], 1);
+		mbar_init(&bar[1], 1);
 		abort_sh = 0;
 		fence_mbar_init();
 	}
@@ -157,43 +167,61 @@ __global__ void __launch_bounds__(TNT) filter3x3_tma_kernel(const __grid_constan
 	asm volatile("griddepcontrol.launch_dependents;");
 	asm volatile("griddepcontrol.wait;" ::: "memory");
 #endif
-	if (threadIdx.x == 0) {
-		mbar_arrive_expect_tx(&bar, (uint32_t)(4 * TIN_W * TIN_H));
-		tma_load_2d(sin, &tin, &bar, x0 - 4, y0 - 1);
-	}
-	mbar_wait(&bar, 0, &abort_sh, nullptr, 0);
-	__syncthreads();  // every thread sees the same abort flag
+	auto load = [&](int t, int b) {
+		const int ty = t / tiles_x, tx = t - ty * tiles_x;
+		mbar_arrive_expect_tx(&bar[b], (uint32_t)(4 * TIN_W * TIN_H));
+		tma_load_2d(sin + b * TIN_WORDS, &tin, &bar[b], tx * TTW - 4, ty * TTH - 1);
+	};
 	const int c = threadIdx.x % TTW, r0 = (threadIdx.x / TTW) * TROWS;
-	if (abort_sh) {  // the box never landed: mark the tile, let the copy finish, return (uniform)
-		for (int r = r0; r < r0 + TROWS; ++r)
-			if (y0 + r < g.h && x0 + c < g.w) out[(size_t)(y0 + r) * g.w + x0 + c] = __int_as_float(0x7fc00000);
-		volatile int own = 0;
-		mbar_wait(&bar, 0, &own, nullptr, 0);
-		return;
-	}
-	// input column of output column c, dx = -1: tile column c + 3
-	const float* col = sin + c + 3;
-	float a0 = col[r0 * TIN_W], a1 = col[r0 * TIN_W + 1], a2 = col[r0 * TIN_W + 2];
-	float b0 = col[(r0 + 1) * TIN_W], b1 = col[(r0 + 1) * TIN_W + 1], b2 = col[(r0 + 1) * TIN_W + 2];
+	int i = 0;
+	if (threadIdx.x == 0 && (int)blockIdx.x < ntiles) load(blockIdx.x, 0);
+	for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+		const int b = i & 1;
+		const int tn = t + gridDim.x;
+		if (threadIdx.x == 0) {
+			if (tn < ntiles) load(tn, b ^ 1);  // its buffer was last read in iteration i - 1 (barrier below)
+			bulk_wait_read_1();                // the store that used sout[b] (iteration i - 2) has read it
+		}
+		mbar_wait(&bar[b], (uint32_t)(i >> 1) & 1u, &abort_sh, nullptr, 0);
+		__syncthreads();  // every thread sees the same abort flag; sout[b] is free
+		const int ty = t / tiles_x, tx = t - ty * tiles_x;
+		const int x0 = tx * TTW, y0 = ty * TTH;
+		if (abort_sh) {  // a box never landed: mark the tile, let the copies finish, return (uniform)
+			for (int r = r0; r < r0 + TROWS; ++r)
+				if (y0 + r < g.h && x0 + c < g.w) out[(size_t)(y0 + r) * g.w + x0 + c] = __int_as_float(0x7fc00000);
+			if (threadIdx.x == 0) {
+				volatile int own = 0;
+				mbar_wait(&bar[b], (uint32_t)(i >> 1) & 1u, &own, nullptr, 0);
+				if (tn < ntiles) mbar_wait(&bar[b ^ 1], (uint32_t)((i + 1) >> 1) & 1u, &own, nullptr, 0);
+				bulk_wait_all();
+			}
+			return;
+		}
+		// input column of output column c, dx = -1: tile column c + 3
+		const float* col = sin + b * TIN_WORDS + c + 3;
+		float* o = sout + b * TOUT_WORDS;
+		float a0 = col[r0 * TIN_W], a1 = col[r0 * TIN_W + 1], a2 = col[r0 * TIN_W + 2];
+		float b0 = col[(r0 + 1) * TIN_W], b1 = col[(r0 + 1) * TIN_W + 1], b2 = col[(r0 + 1) * TIN_W + 2];
 #pragma unroll
-	for (int k = 0; k < TROWS; ++k) {
-		const float* rr = col + (r0 + k + 2) * TIN_W;
-		const float c0 = rr[0], c1 = rr[1], c2 = rr[2];
-		float s = 0.0f;
-		s = fmaf(wt.w[0], a0, s); s = fmaf(wt.w[1], a1, s); s = fmaf(wt.w[2], a2, s);
-		s = fmaf(wt.w[3], b0, s); s = fmaf(wt.w[4], b1, s); s = fmaf(wt.w[5], b2, s);
-		s = fmaf(wt.w[6], c0, s); s = fmaf(wt.w[7], c1, s); s = fmaf(wt.w[8], c2, s);
-		sout[(r0 + k) * TTW + c] = s;
-		a0 = b0; a1 = b1; a2 = b2;
-		b0 = c0; b1 = c1; b2 = c2;
+		for (int k = 0; k < TROWS; ++k) {
+			const float* rr = col + (r0 + k + 2) * TIN_W;
+			const float c0 = rr[0], c1 = rr[1], c2 = rr[2];
+			float s = 0.0f;
+			s = fmaf(wt.w[0], a0, s); s = fmaf(wt.w[1], a1, s); s = fmaf(wt.w[2], a2, s);
+			s = fmaf(wt.w[3], b0, s); s = fmaf(wt.w[4], b1, s); s = fmaf(wt.w[5], b2, s);
+			s = fmaf(wt.w[6], c0, s); s = fmaf(wt.w[7], c1, s); s = fmaf(wt.w[8], c2, s);
+			o[(r0 + k) * TTW + c] = s;
+			a0 = b0; a1 = b1; a2 = b2;
+			b0 = c0; b1 = c1; b2 = c2;
+		}
+		fence_proxy_async_smem();  // the tile's generic stores before the async-proxy store reads them
+		__syncthreads();           // also: every thread is done reading sin[b]
+		if (threadIdx.x == 0) {
+			tma_store_2d(&tout, o, x0, y0);
+			bulk_commit();
+		}
 	}
-	fence_proxy_async_smem();  // the tile's generic stores before the async-proxy store reads them
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		tma_store_2d(&tout, sout, x0, y0);
-		bulk_commit();
-		bulk_wait_all();
-	}
+	if (threadIdx.x == 0) bulk_wait_all();
 }
 
 }  // namespace
@@ -207,11 +235,33 @@ extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, 
 	FilterGeom g{h, w, pad, umi::aligned(in, 16) && umi::aligned(out, 16) && (w % 4) == 0};
 	Weights9 wt;
 	for (int i = 0; i < 9; ++i) wt.w[i] = w9[i];
-	uint32_t pad_bits;
-	std::memcpy(&pad_bits, &pad, 4);
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(umi::ceil_div(w, TWC), umi::ceil_div(h, WARPS * RY));
+	cfg.blockDim = dim3(WARPS * 32);
+	cfg.stream = umi::as_stream(stream);
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_f32_kernel, in, out, g, wt), "filter3x3_f32_kernel"));
+	return umi::ok();
+}
+
+extern "C" umi_status umi_filter3x3_f32_tma(const float* in, float* out, int32_t h, int32_t w, const float* w9,
+                                            void* stream) {
+	if (h < 0 || w < 0) return umi::fail(UMI_ERR_INVALID_ARG, "filter3x3_tma: negative size %dx%d", h, w);
+	if (h == 0 || w == 0) return umi::ok();
+	if (!in || !out || !w9) return umi::fail(UMI_ERR_INVALID_ARG, "filter3x3_tma: null pointer");
+	if (in == out) return umi::fail(UMI_ERR_INVALID_ARG, "filter3x3_tma: in and out alias");
+	const float pad = 0.0f;
+	FilterGeom g{h, w, pad, umi::aligned(in, 16) && umi::aligned(out, 16) && (w % 4) == 0};
+	Weights9 wt;
+	for (int i = 0; i < 9; ++i) wt.w[i] = w9[i];
 	auto enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(umi::tma_encode_fn());
-	if (g.vec && pad_bits == 0 && enc) {
-		// zero padding on aligned rows: TMA-staged halo tiles
+	if (!enc) return umi::fail(UMI_ERR_CUDA, "filter3x3_tma: cuTensorMapEncodeTiled unavailable");
+	if (!g.vec) return umi::fail(UMI_ERR_UNSUPPORTED, "filter3x3_tma: needs 16-byte aligned in/out and w %% 4 == 0");
+	{
 		CUtensorMap tin, tout;
 		const cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
 		const cuuint64_t strides[1] = {(cuuint64_t)w * 4};
@@ -227,8 +277,15 @@ extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, 
 		if (r == CUDA_SUCCESS) {
 			UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(filter3x3_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			                                              (int)TSMEM), "cudaFuncSetAttribute"));
+			int dev = 0, sms = 0, per_sm = 0;
+			UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+			UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+			                         "cudaDeviceGetAttribute"));
+			UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, filter3x3_tma_kernel, TNT, TSMEM),
+			                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
+			const int tiles_x = umi::ceil_div(w, TTW), ntiles = tiles_x * umi::ceil_div(h, TTH);
 			cudaLaunchConfig_t cfg{};
-			cfg.gridDim = dim3(umi::ceil_div(w, TTW), umi::ceil_div(h, TTH));
+			cfg.gridDim = dim3(std::max(1, std::min(ntiles, sms * std::max(per_sm, 1))));
 			cfg.blockDim = dim3(TNT);
 			cfg.dynamicSmemBytes = TSMEM;
 			cfg.stream = umi::as_stream(stream);
@@ -237,20 +294,10 @@ extern "C" umi_status umi_filter3x3_f32(const float* in, float* out, int32_t h, 
 			attr[0].val.programmaticStreamSerializationAllowed = 1;
 			cfg.attrs = attr;
 			cfg.numAttrs = 1;
-			UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_tma_kernel, tin, tout, out, g, wt),
+			UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_tma_kernel, tin, tout, out, g, wt, tiles_x, ntiles),
 			                         "filter3x3_tma_kernel"));
 			return umi::ok();
 		}
+		return umi::fail(UMI_ERR_CUDA, "filter3x3_tma: tensor map (%d)", (int)r);
 	}
-	cudaLaunchConfig_t cfg{};
-	cfg.gridDim = dim3(umi::ceil_div(w, TWC), umi::ceil_div(h, WARPS * RY));
-	cfg.blockDim = dim3(WARPS * 32);
-	cfg.stream = umi::as_stream(stream);
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-	attr[0].val.programmaticStreamSerializationAllowed = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, filter3x3_f32_kernel, in, out, g, wt), "filter3x3_f32_kernel"));
-	return umi::ok();
 }
