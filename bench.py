@@ -40,15 +40,15 @@ L2_BYTES = 129 * 2 ** 20
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # (dram__bytes_read.sum, dram__bytes_write.sum) per launch of the dominant
 # kernel, from the ncu captures summarised under profiles/ (None where not
-# captured).  batched_uneven was captured on its 8-image case (12 896 910 px):
-# the cost volume's traffic grows with the pixel count, so it is kept per
+# captured).  batched_uneven's fused launch was captured on its 4-image case
+# (8 725 530 px): its traffic grows with the pixel count, so it is kept per
 # pixel and scaled to the configured batch.
-NCU_TRAFFIC = {"int_pair_1080p": (4197632, 0), "filter3x3_1024": (4204544, 0), "gemm_4096": (76233472, 35101184),
+NCU_TRAFFIC = {"int_pair_1080p": (4178432, 0), "filter3x3_1024": (4204544, 0), "gemm_4096": (76233472, 35101184),
                "fprop_n32": (67321088, 206541312), "learned_me_4k": None,
                # the proposal: cells kernel (both frames read once) + coarse search (planes and cells)
                "coarse_me_4k": (16615680 + 2795520, 0),
                "video_y4m_1080p": None, "apps_1080p": None, "serve_bilateral_8x512": None}
-NCU_TRAFFIC_PER_PX = {"batched_uneven": (3301802000 / 12896910, 3253943000 / 12896910)}
+NCU_TRAFFIC_PER_PX = {"batched_uneven": (2616474000 / 8725530, 2272248000 / 8725530)}
 
 
 def traffic_fields(rw, alg_write_bytes=None):
@@ -1575,7 +1575,9 @@ def run_ours(args, wl, dist):
         kernels["fused_step"]["note"] = "the three operators in one launch; the others are each operator alone"
         kernels["three_launches_step"]["note"] = "the same step as three launches (one kernel per operator)"
         roof = dict(kernels["fused_step"], bound="hbm", kernel="batch_fused_kernel (all three operators)",
-                    peak=pk["hbm_gbs"], **traffic_fields(NCU_TRAFFIC.get("batched_uneven_fused")),
+                    peak=pk["hbm_gbs"],
+                    **traffic_fields(tuple(v * wl.px for v in NCU_TRAFFIC_PER_PX["batched_uneven"]),
+                                     (256 + 4 + 4) * wl.px),
                     peak_source=pk["source"])
     else:
         ach = hbm_bytes / (kms["filter3x3_f32"] * 1e-3) / 1e9
