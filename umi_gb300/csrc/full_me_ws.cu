@@ -266,14 +266,23 @@ full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 			bar_producers();
 			if (*abort_flag) return false;
 			const uint32_t m1 = a.mul[0], m2 = a.mul[1], m3 = a.mul[2];
-#pragma unroll 2
-			for (int r = pw; r < Gm::WR; r += kProdWarps) {
+			// rows pw, pw + 4, ...: fully unrolled from one base pointer, so every
+			// shared-memory offset is an immediate (no address arithmetic per word)
+			constexpr int RPW = (Gm::WR + kProdWarps - 1) / kProdWarps;
+			uint32_t* rb = buf + pw * S + lane;
 #pragma unroll
-				for (int k = lane; k < Gm::WC; k += 32) {
-					const uint32_t lo = buf[r * S + k], hi = buf[r * S + k + 1];
-					buf[Gm::COPY + r * S + k] = __umulhi(lo, m1) + hi * m1;
-					buf[2 * Gm::COPY + r * S + k] = __umulhi(lo, m2) + hi * m2;
-					buf[3 * Gm::COPY + r * S + k] = __umulhi(lo, m3) + hi * m3;
+			for (int i = 0; i < RPW; ++i) {
+				if (Gm::WR % kProdWarps == 0 || pw + kProdWarps * i < Gm::WR) {
+#pragma unroll
+					for (int kc = 0; kc < Gm::WC; kc += 32) {
+						if (lane + kc < Gm::WC) {
+							const int o = kProdWarps * i * S + kc;
+							const uint32_t lo = rb[o], hi = rb[o + 1];
+							rb[Gm::COPY + o] = __umulhi(lo, m1) + hi * m1;
+							rb[2 * Gm::COPY + o] = __umulhi(lo, m2) + hi * m2;
+							rb[3 * Gm::COPY + o] = __umulhi(lo, m3) + hi * m3;
+						}
+					}
 				}
 			}
 			mbar_arrive(&full[b]);
@@ -331,16 +340,31 @@ full_me_ws_kernel(const WsArgs a, const __grid_constant__ CUtensorMap tref) {
 		}
 	} else {
 		// ------------------------------------------------------------ search
+		// task L = c, c + 512, ...: macroblock j = L / TPM (buffer b = j % NB, its
+		// use j / NB), task t = L % TPM, kept incrementally (512 < 2 TPM)
+		static_assert(kSearchThreads < 2 * TPM, "one wrap per step");
 		const int c = tid - kProdThreads;
-		const int total = nj * TPM;
-		for (int L = c; L < total; L += kSearchThreads) {
-			const int j = L / TPM, t = L - j * TPM;
-			const int b = j % NB;
-			if (!mbar_wait_sleep(&full[b], (uint32_t)(j / NB) & 1u, abort_flag, &g_full_me_err, kMeErrFull, 2000)) break;
+		int j = c / TPM, t = c - j * TPM;
+		int b = j % NB;
+		uint32_t use = (uint32_t)(j / NB);
+		for (; j < nj;) {
+			if (!mbar_wait_sleep(&full[b], use & 1u, abort_flag, &g_full_me_err, kMeErrFull, 2000)) break;
 			const int q = t / Gm::ND, ix = t - q * Gm::ND;
 			const uint32_t key = ws_task<R>(bufs + b * Gm::BUF, ix, q * Gm::G, a.mul16);
 			atomicMin(&best[b], key);
 			mbar_arrive(&empty[b]);
+			t += kSearchThreads - TPM;  // one macroblock forward, then the remainder
+			++j;
+			if (++b == NB) { b = 0; ++use; }
+			if (t < 0) {  // the step did not reach the next macroblock
+				t += TPM;
+				--j;
+				if (--b < 0) { b = NB - 1; --use; }
+			} else if (t >= TPM) {
+				t -= TPM;
+				++j;
+				if (++b == NB) { b = 0; ++use; }
+			}
 		}
 	}
 }
