@@ -1648,7 +1648,16 @@ def run_reference(args, wl, dist):
         return None
     threads = os.cpu_count() or 1
     wl.cpu_setup()
-    per_step = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2, LearnedMe: 8, CoarseMe4k: 8, VideoY4M: 8}.get(type(wl), 16)
+    base = {IntPair: 32, Batched: 2, Gemm: 2, Fprop: 2, LearnedMe: 8, CoarseMe4k: 8, VideoY4M: 8}.get(type(wl), 16)
+    cap = {IntPair: 8040, Batched: 512, Gemm: 256, Fprop: 126, LearnedMe: 32400, CoarseMe4k: 32400,
+           VideoY4M: 8040}.get(type(wl), 1024)
+    # each step a bounded sample of the workload: calibrate on one call, then
+    # size the sample to about 0.4 s per step (at most 90 s for the whole run)
+    t0 = time.perf_counter()
+    wl.cpu_step(base, threads)
+    dt1 = max(time.perf_counter() - t0, 1e-6)
+    target = min(0.4, 90.0 / max(1, args.steps + args.warmup))
+    per_step = int(min(cap, max(base, base * target / dt1)))
     for _ in range(args.warmup):
         wl.cpu_step(per_step, threads)
     t0 = time.perf_counter()
