@@ -554,9 +554,17 @@ struct GemmSplitPolicy {
 	__host__ __device__ static int ntiles(const Args& g) {
 		return ((g.M + BM - 1) / BM) * ((g.N + SPLIT_BN - 1) / SPLIT_BN);
 	}
+	// grouped order: 8 row-blocks at a time, column by column, so that the
+	// tiles in flight at once (one per CTA) share 8 blocks of A and a short
+	// run of B in L2 instead of sweeping all of B for every row of tiles
+	static constexpr int GROUP_M = 8;
 	__device__ static Tile tile(const Args& g, int id) {
-		const int nt = (g.N + SPLIT_BN - 1) / SPLIT_BN;
-		return {(id / nt) * BM, (id % nt) * SPLIT_BN};
+		const int nt = (g.N + SPLIT_BN - 1) / SPLIT_BN, mt = (g.M + BM - 1) / BM;
+		const int per_group = GROUP_M * nt;
+		const int first_m = (id / per_group) * GROUP_M;
+		const int gsz = min(mt - first_m, GROUP_M);
+		const int r = id - (id / per_group) * per_group;
+		return {(first_m + r % gsz) * BM, (r / gsz) * SPLIT_BN};
 	}
 	__device__ static int nk(const Args& g) { return (g.K + BK - 1) / BK; }
 	__device__ static void load4(const SplitMaps& m, const Args&, const Tile& t, int ks, uint8_t* dst, uint64_t* bar) {
