@@ -223,7 +223,7 @@ class IntPair:
         self.h_ref = torch.from_numpy(self.ref).pin_memory()
         self.h_ii = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
-        self.launches_per_step = 4  # iimg: 3 kernels (column sums, carry, output), full_me: 1
+        self.launches_per_step = 3  # iimg: 2 kernels (group column sums, output pass), full_me: 1
 
     def step(self, i):
         k = i % self.n_rot
@@ -1036,8 +1036,8 @@ class Apps1080p:
         self.J = [torch.zeros((self.H + 1, self.W + 1), dtype=torch.int32, device=dev) for _ in range(self.n_rot)]
         self.ws = torch.empty(U.iimg_workspace_bytes(self.H, self.W), dtype=torch.uint8, device=dev)
         self.h_out = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
-        # census + dilate + (iimg 3 kernels + J copy + box) + gaussian 2
-        self.launches_per_step = 1 + 1 + 5 + 2
+        # census + dilate + (iimg 2 kernels + J copy + box) + gaussian 2
+        self.launches_per_step = 1 + 1 + 4 + 2
         for k in range(self.n_rot):  # constants made before any graph capture
             self.step(k)
 

@@ -180,10 +180,12 @@ umi_status umi_filter3x3_f32_tma(const float* in, float* out, int32_t h, int32_t
 
 /* Integral image, uint8 -> int32: out[y,x] = sum_{y'<=y, x'<=x} in[y',x'].
  * Replaces the two Execute calls of main/iimg.cu:37-82 (row prefix through a
- * Loop output, transposed, twice).  Needs a device workspace of
+ * Loop output, transposed, twice) with two launches: column sums per group
+ * of 128 rows, then one output pass.  Needs a device workspace of
  * umi_iimg_u8_i32_workspace_bytes(h, w) bytes (16-byte aligned; about
- * 0.75 byte per pixel).  Frames with h*w*255 >= 2^31 are rejected
- * (UMI_ERR_UNSUPPORTED: sums could overflow int32). */
+ * 0.27 byte per pixel; its content need not be initialised).  Frames with
+ * h*w*255 >= 2^31 are rejected (UMI_ERR_UNSUPPORTED: sums could overflow
+ * int32). */
 size_t umi_iimg_u8_i32_workspace_bytes(int32_t h, int32_t w);
 umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h, int32_t w, void* workspace,
                            size_t workspace_bytes, void* stream);

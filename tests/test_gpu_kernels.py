@@ -127,6 +127,43 @@ def test_iimg_repeated_calls_reuse_workspace(umi, orc, dev):
         assert np.array_equal(got, orc.iimg_u8_i32(x))
 
 
+@pytest.mark.parametrize("fill", [0x01, 0xFF])
+@pytest.mark.parametrize("h,w", [(1080, 1920), (2160, 3840), (70, 600), (129, 130)])
+def test_iimg_workspace_content_is_irrelevant(umi, orc, dev, fill, h, w):
+    """Kernel 1 writes every group sum that kernel 2 reads: whatever the
+    workspace held before the call, the result is exact."""
+    import torch
+    from umi_gb300 import workloads
+    x = workloads.iimg_frame(seed=h * 7 + w + fill, h=h, w=w)
+    ws = torch.full((umi.iimg_workspace_bytes(h, w),), fill, dtype=torch.uint8, device=dev)
+    got = umi.iimg_u8_i32(_t(x, dev), workspace=ws).cpu().numpy()
+    assert np.array_equal(got, orc.iimg_u8_i32(x))
+
+
+def test_iimg_graph_replays(umi, orc, dev):
+    """Captured once (the group sums and the dependent output launch),
+    replayed on new frames copied into the same input buffer."""
+    import torch
+    h, w = 1080, 1920
+    inp = torch.zeros((h, w), dtype=torch.uint8, device=dev)
+    out = torch.empty((h, w), dtype=torch.int32, device=dev)
+    ws = torch.empty(umi.iimg_workspace_bytes(h, w), dtype=torch.uint8, device=dev)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        umi.iimg_u8_i32(inp, out=out, workspace=ws)  # first call outside the capture
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            umi.iimg_u8_i32(inp, out=out, workspace=ws)
+    torch.cuda.current_stream().wait_stream(s)
+    for seed in range(3):
+        x = np.random.default_rng(40 + seed).integers(0, 256, (h, w), dtype=np.uint8)
+        inp.copy_(_t(x, dev))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), orc.iimg_u8_i32(x)), seed
+
+
 # ---------------------------------------------------------------- full_me
 @pytest.mark.parametrize("h,w,b,r", [(64, 64, 16, 4), (48, 80, 16, 7), (64, 96, 8, 7), (96, 128, 16, 32),
                                      (40, 56, 8, 3), (17, 33, 16, 5), (130, 70, 16, 64), (50, 70, 8, 13)])

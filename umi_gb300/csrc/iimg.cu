@@ -5,7 +5,7 @@
 // frame from HBM and one write of the int32 result.
 //
 // Two forms share this file.  umi_iimg_u8_i32 uses the band form (further
-// down: per-band column sums, a carry scan down the bands, one output pass).
+// down: column sums per group of bands, then one output pass).
 // umi_iimg_u8_i32_noalloc keeps the tile form below, whose small tile sums
 // fit the library's built-in scratch:
 // the frame is cut into TH x TW tiles (64 x 256: a 1080p frame is 136 tiles,
@@ -263,77 +263,81 @@ size_t ws_bytes(int h, int w) {
 
 // ---------------------------------------------------------------------------
 // Band form (umi_iimg_u8_i32).  The frame is cut into bands of RB rows over
-// the full width; with V[b][x] = sum of column x over all rows above band b,
-//   ii[y][x] = sum_{x'<=x} V[b][x'] + sum_{band rows y'<=y} sum_{x'<=x} in[y'][x'].
-// Kernel 1 writes per-band column sums (uint16: at most RB*255), kernel 2
-// scans them down the bands into V (one warp per band range, 32 columns per
-// CTA), kernel 3 reads each band once, scans its RB rows and its V row along
-// x with one block-wide scan of RB+1 values per thread, and writes the band.
-// The three launches are chained with programmatic dependent launch; kernel
-// 3 loads its pixels before waiting for kernel 2.  Every grid is parallel
-// over the whole frame (no chain of tiles), so a 1080p frame runs 135 CTAs of
-// 256 threads in the output pass.
+// the full width and the bands into groups of GB bands (128 rows).  With
+// V[b][x] = sum of column x over all rows above band b,
+//   ii[y][x] = sum_{x'<=x} V[b][x'] + sum_{band rows y'<=y} sum_{x'<=x} in[y'][x'],
+//   V[b][x]  = sum_{groups g' above the group of b} S[g'][x] + W[b][x],
+// where S[g][x] is the column sum of group g and W[b][x] the column sum of the
+// bands of its group above b.  Kernel 1 (one CTA per group and 128 columns)
+// reads every group once and writes W and S (uint16: at most 128 * 255).
+// Kernel 2 (one CTA per band) loads its band's pixels, waits for kernel 1
+// (programmatic dependent launch: its launch and pixel loads overlap kernel
+// 1), forms V from at most ceil(h / 128) independent loads per column, scans
+// its RB rows and its V row along x with one block-wide scan of RB + 1
+// values per thread, and writes the band.  Two launches, both parallel over
+// the whole frame; no grid-wide wait.
 constexpr int RB = 8;          // rows per band
-constexpr int SEG = NT * CPL;  // columns per CTA pass (2048)
+constexpr int GB = 16;         // bands per group
+constexpr int GCT = 16;        // kernel-1 threads across the columns of a group (x CPL = 128 columns)
+constexpr int SEG = NT * CPL;  // columns per kernel-2 pass (2048)
+static_assert(GB * GCT == NT, "kernel 1: one thread per band and 8 columns");
 
 struct BandGeom {
-	int h, w, nb, wpad, nseg;
-	int bpw;  // bands per warp in the carry scan: ceil(nb / NW)
+	int h, w, nb, ng, wpad, nseg;
 	int vec_in, vec_out;
-	uint16_t* colsum;  // [nb][wpad]
-	int32_t* vsum;     // [nb][wpad]
+	uint16_t* wsum;  // [ng * GB][wpad]  W
+	uint16_t* gsum;  // [ng][wpad]       S
 };
 
 size_t band_ws_bytes(int h, int w) {
-	const size_t nb = umi::ceil_div(h, RB), wpad = (size_t)umi::ceil_div(w, CPL) * CPL;
+	const size_t nb = umi::ceil_div(h, RB), ng = umi::ceil_div(nb, (size_t)GB), wpad = (size_t)umi::ceil_div(w, CPL) * CPL;
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-	return al(nb * wpad * 2) + al(nb * wpad * 4);
+	return al(ng * GB * wpad * 2) + al(ng * wpad * 2);
 }
 
-__global__ void __launch_bounds__(NT) iimg_band_colsums(const uint8_t* __restrict__ in, const BandGeom g) {
+__global__ void __launch_bounds__(NT) iimg_group_sums(const uint8_t* __restrict__ in, const BandGeom g) {
+	__shared__ __align__(16) uint32_t cs[GB][GCT * CPL];
 	pdl_trigger();
-	const int b = blockIdx.y;
-	const int x0 = blockIdx.x * SEG + threadIdx.x * CPL;
-	if (x0 >= g.w) return;
+	const int gi = blockIdx.y, j = threadIdx.x / GCT, c = threadIdx.x % GCT;
+	const int xs = blockIdx.x * GCT * CPL, x0 = xs + c * CPL;
 	IimgGeom ig{};
 	ig.h = g.h; ig.w = g.w; ig.vec_in = g.vec_in;
 	uint32_t s[CPL] = {};
+	if (x0 < g.w) {
+		const int y0 = (gi * GB + j) * RB;
+		uint2 raw[RB];
 #pragma unroll
-	for (int r = 0; r < RB; ++r) {
-		uint32_t v[CPL];
-		unpack8(load8(in, ig, b * RB + r, x0), v);
+		for (int r = 0; r < RB; ++r) raw[r] = load8(in, ig, y0 + r, x0);
 #pragma unroll
-		for (int k = 0; k < CPL; ++k) s[k] += v[k];
+		for (int r = 0; r < RB; ++r) {
+			uint32_t v[CPL];
+			unpack8(raw[r], v);
+#pragma unroll
+			for (int k = 0; k < CPL; ++k) s[k] += v[k];
+		}
 	}
-	uint4 o;
-	o.x = s[0] | (s[1] << 16);
-	o.y = s[2] | (s[3] << 16);
-	o.z = s[4] | (s[5] << 16);
-	o.w = s[6] | (s[7] << 16);
-	*reinterpret_cast<uint4*>(g.colsum + (size_t)b * g.wpad + x0) = o;
+	*reinterpret_cast<uint4*>(&cs[j][c * CPL]) = make_uint4(s[0], s[1], s[2], s[3]);
+	*reinterpret_cast<uint4*>(&cs[j][c * CPL + 4]) = make_uint4(s[4], s[5], s[6], s[7]);
+	__syncthreads();
+	if (threadIdx.x < GCT * CPL) {  // one column per thread: exclusive prefix over the group's bands
+		const int x = xs + threadIdx.x;
+		if (x < g.w) {
+			uint32_t run = 0;
+#pragma unroll
+			for (int k = 0; k < GB; ++k) {
+				g.wsum[(size_t)(gi * GB + k) * g.wpad + x] = (uint16_t)run;
+				run += cs[k][threadIdx.x];
+			}
+			g.gsum[(size_t)gi * g.wpad + x] = (uint16_t)run;
+		}
+	}
 }
 
-// V[b][x] = sum_{b' < b} colsum[b'][x]: lane = column, warp w = bands
-// [w*S, (w+1)*S), warp totals combined through shared memory.
-__global__ void __launch_bounds__(NT) iimg_band_carry(const BandGeom g) {
-	__shared__ uint32_t tot[NW][32];
-	pdl_trigger();
-	pdl_wait();
-	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-	const int x = blockIdx.x * 32 + lane;
-	const int b0 = wp * g.bpw, b1 = min(g.nb, b0 + g.bpw);
-	uint32_t s = 0;
-	if (x < g.wpad)
-		for (int b = b0; b < b1; ++b) s += g.colsum[(size_t)b * g.wpad + x];
-	tot[wp][lane] = s;
-	__syncthreads();
-	uint32_t pre = 0;
-	for (int k = 0; k < wp; ++k) pre += tot[k][lane];
-	if (x < g.wpad)
-		for (int b = b0; b < b1; ++b) {
-			g.vsum[(size_t)b * g.wpad + x] = (int32_t)pre;
-			pre += g.colsum[(size_t)b * g.wpad + x];
-		}
+__device__ __forceinline__ void add_u16x8(uint32_t (&v)[CPL], uint4 p) {
+	v[0] += p.x & 0xffffu; v[1] += p.x >> 16;
+	v[2] += p.y & 0xffffu; v[3] += p.y >> 16;
+	v[4] += p.z & 0xffffu; v[5] += p.z >> 16;
+	v[6] += p.w & 0xffffu; v[7] += p.w >> 16;
 }
 
 __global__ void __launch_bounds__(NT) iimg_band_out(const uint8_t* __restrict__ in, int32_t* __restrict__ out,
@@ -359,11 +363,11 @@ __global__ void __launch_bounds__(NT) iimg_band_out(const uint8_t* __restrict__ 
 			for (int r = 0; r < RB; ++r) raw[r] = live ? load8(in, ig, y0 + r, x0) : make_uint2(0, 0);
 		}
 		uint32_t vv[CPL] = {};
-		if (live) {
-			const int4* vp = reinterpret_cast<const int4*>(g.vsum + (size_t)b * g.wpad + x0);
-			const int4 a = vp[0], c = vp[1];
-			vv[0] = a.x; vv[1] = a.y; vv[2] = a.z; vv[3] = a.w;
-			vv[4] = c.x; vv[5] = c.y; vv[6] = c.z; vv[7] = c.w;
+		if (live) {  // V = W of this band + S of every group above
+			add_u16x8(vv, __ldcg(reinterpret_cast<const uint4*>(g.wsum + (size_t)b * g.wpad + x0)));
+			const int gb = b / GB;
+#pragma unroll 8
+			for (int q = 0; q < gb; ++q) add_u16x8(vv, __ldcg(reinterpret_cast<const uint4*>(g.gsum + (size_t)q * g.wpad + x0)));
 		}
 		// thread totals of each row and of the V row, scanned over the block
 		uint32_t tsum[RB + 1];
@@ -470,28 +474,26 @@ extern "C" umi_status umi_iimg_u8_i32(const uint8_t* in, int32_t* out, int32_t h
 	BandGeom g{};
 	g.h = h; g.w = w;
 	g.nb = umi::ceil_div(h, RB);
+	g.ng = umi::ceil_div(g.nb, GB);
 	g.wpad = umi::ceil_div(w, CPL) * CPL;
 	g.nseg = umi::ceil_div(w, SEG);
-	g.bpw = umi::ceil_div(g.nb, NW);
 	g.vec_in = umi::aligned(in, 8) && (w % 8) == 0;
 	g.vec_out = umi::aligned(out, 16) && (w % 4) == 0;
 	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
 	char* ws = static_cast<char*>(workspace);
-	g.colsum = reinterpret_cast<uint16_t*>(ws);
-	g.vsum = reinterpret_cast<int32_t*>(ws + al((size_t)g.nb * g.wpad * 2));
+	g.wsum = reinterpret_cast<uint16_t*>(ws);
+	g.gsum = reinterpret_cast<uint16_t*>(ws + al((size_t)g.ng * GB * g.wpad * 2));
 	const cudaStream_t st = umi::as_stream(stream);
 	// kernel 1 follows whatever the stream ran before: plain launch
-	iimg_band_colsums<<<dim3(g.nseg, g.nb), NT, 0, st>>>(in, g);
-	UMI_TRY(umi::launch_status("iimg_band_colsums"));
+	iimg_group_sums<<<dim3(umi::ceil_div(w, GCT * CPL), g.ng), NT, 0, st>>>(in, g);
+	UMI_TRY(umi::launch_status("iimg_group_sums"));
 	cudaLaunchAttribute attr[1] = {pdl_attr()};
 	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(g.nb);
 	cfg.blockDim = dim3(NT);
 	cfg.stream = st;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	cfg.gridDim = dim3(umi::ceil_div(g.wpad, 32));
-	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_band_carry, g), "iimg_band_carry"));
-	cfg.gridDim = dim3(g.nb);
 	UMI_TRY(umi::cuda_status(cudaLaunchKernelEx(&cfg, iimg_band_out, in, out, g), "iimg_band_out"));
 	return umi::ok();
 }
