@@ -22,9 +22,10 @@
 // the four cells of a row are one unaligned word, one vabsdiff4 per cell row.
 // cur's cells are four words per block.
 //
-// Search kernel: one CTA per block, one warp per plane, one lane per
-// candidate column B holding 32 candidate rows in registers; the argmin key
-// (sad << 12) | raster index is reduced per warp, then over the four warps.
+// Search kernel: one CTA per pair of vertically adjacent blocks, one warp per
+// plane, one lane per candidate column B holding 32 candidate rows of each
+// block in registers; the argmin key (sad << 12) | raster index is reduced
+// per warp, then over the four warps.
 #include <algorithm>
 #include <climits>
 
@@ -154,6 +155,7 @@ __global__ void __launch_bounds__(NT) coarse_cells_kernel(const uint8_t* __restr
 
 // Minimum of cost[a] * 32 + a over the candidate rows a whose vertical
 // displacement 2 (a - 16) + PY lies in [-m, m]: the first row wins ties.
+// Runtime range (M < 0): masks per row.
 template <int M, int PY>
 __device__ __forceinline__ uint32_t first_min_row(const uint32_t (&cost)[32], int m) {
 	uint32_t mn = 0xffffffffu;
@@ -165,20 +167,67 @@ __device__ __forceinline__ uint32_t first_min_row(const uint32_t (&cost)[32], in
 	return mn;
 }
 
-// One CTA per block, one warp per plane (py, px), one lane per candidate
-// column B = lane - 16.  The lane streams the plane's 35 window rows once:
-// one realigned word per row (two shared loads and a prmt) meets the four cell
-// rows i at the candidate rows A = row - 16 - i, so a candidate costs four
-// vabsdiff4 and about a quarter of a prmt.  M = range / 2 at compile time
-// (the default range 60), or M < 0 for any range (runtime masks).
+__device__ __forceinline__ uint32_t min_u16x2(uint32_t a, uint32_t b) {
+	uint32_t d;
+	asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+	return d;
+}
+
+// The same minimum for a range fixed at compile time, on 16-bit keys: a cost
+// is at most 16 * 255 = 4080 < 0xfff, so cost * 16 + (a & 15) fits 16 bits
+// and rows a and a + 16 share one word, reduced by 15 packed minima; a row
+// outside the range holds 0xffff, above every real key.  The words are formed
+// by multiply-adds with multipliers the compiler cannot see (k16 = 16,
+// k20 = 1 << 20), which keeps them on the FMA pipe beside the SADs.
+template <int M, int PY>
+__device__ __forceinline__ uint32_t first_min_row_packed(const uint32_t (&cost)[32], uint32_t k16, uint32_t k20) {
+	static_assert(M >= 1, "every row parity has a row inside the range");
+	auto in = [](int a) { const int dy2 = 2 * (a - 16) + PY; return dy2 >= -M && dy2 <= M; };
+	uint32_t w[16];
+#pragma unroll
+	for (int a = 0; a < 16; ++a) {
+		const bool lo = in(a), hi = in(a + 16);
+		const uint32_t c = (uint32_t)a | ((uint32_t)a << 16);
+		if (lo && hi) w[a] = cost[a] * k16 + (cost[a + 16] * k20 + c);
+		else if (lo) w[a] = cost[a] * k16 + (0xffff0000u | (uint32_t)a);
+		else if (hi) w[a] = cost[a + 16] * k20 + (((uint32_t)a << 16) | 0xffffu);
+		else w[a] = 0xffffffffu;
+	}
+#pragma unroll
+	for (int s = 8; s > 0; s >>= 1)
+#pragma unroll
+		for (int a = 0; a < s; ++a) w[a] = min_u16x2(w[a], w[a + s]);
+	const uint32_t klo = w[0] & 0xffffu, khi = w[0] >> 16;
+	const uint32_t kl = ((klo >> 4) << 5) | (klo & 15u), kh = ((khi >> 4) << 5) | 16u | (khi & 15u);
+	return min(kl, kh);  // equal costs: the row of the low half comes first
+}
+
+// Key of a lane's best candidate: (sad << 12) | raster index of (dy, dx).
+__device__ __forceinline__ uint32_t cand_key(uint32_t mn, int py, int dx2, int m) {
+	const int a = (int)(mn & 31u), dy2 = 2 * (a - 16) + py, nd = 2 * m + 1;
+	return ((mn >> 5) << 12) | (uint32_t)((dy2 + m) * nd + dx2 + m);
+}
+
+// One CTA per pair of vertically adjacent blocks (2 p, 2 p + 1) of one block
+// column, one warp per plane (py, px), one lane per candidate column
+// B = lane - 16.  The lane streams the 39 plane rows the pair's windows cover
+// once: one realigned word per row (two shared loads and a prmt) meets the
+// four cell rows i of the upper block at candidate rows A = row - 16 - i and
+// those of the lower block at A = row - 20 - i, so a candidate costs four
+// vabsdiff4 and about a fifth of a prmt; 64 costs stay in registers.
+// M = range / 2 at compile time (the default range 60: packed 16-bit argmin),
+// or M < 0 for any range (runtime masks).
+constexpr int PAIR_ROWS = WIN_ROWS + 4;
 template <int M>
 __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __restrict__ cells,
                                                             const uint32_t* __restrict__ planes, CoarseGeom g, int m_rt,
-                                                            int32_t* __restrict__ centers) {
+                                                            uint32_t k16, uint32_t k20, int32_t* __restrict__ centers) {
 	const int m = M >= 0 ? M : m_rt;
-	__shared__ uint32_t win[4][WIN_ROWS][WIN_WORDS];
-	__shared__ uint32_t best[4];
-	const int blk = blockIdx.x, by = blk / g.nbx, bx = blk - by * g.nbx;
+	__shared__ uint32_t win[4][PAIR_ROWS][WIN_WORDS];
+	__shared__ uint32_t best[2][4];
+	const int pr = blockIdx.x / g.nbx, bx = blockIdx.x - pr * g.nbx, by0 = 2 * pr;
+	const bool two = by0 + 1 < g.nby;
+	const int blk0 = by0 * g.nbx + bx, blk1 = blk0 + g.nbx;
 	const int pww = g.pw / 4;
 	const size_t plane_words = (size_t)g.pr * pww;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
@@ -186,46 +235,65 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 		constexpr int RPP = 32 / WIN_WORDS;
 		const int kk = lane % WIN_WORDS, rr = lane / WIN_WORDS;
 		if (rr < RPP) {
-			// plane row 4 by + r < 4 nby + 31 < pr; word bx + k <= nbx + 7 < pww
-			const uint32_t* src = planes + warp * plane_words + (size_t)(4 * by + rr) * pww + bx + kk;
+			// word bx + k <= nbx + 7 < pww; plane row 4 by0 + r < pr except the last
+			// four rows when the lower block does not exist (those stay zero)
+			const uint32_t* src = planes + warp * plane_words + (size_t)(4 * by0 + rr) * pww + bx + kk;
 #pragma unroll
-			for (int j = 0; j < (WIN_ROWS + RPP - 1) / RPP; ++j)
-				if (rr + RPP * j < WIN_ROWS) win[warp][rr + RPP * j][kk] = __ldg(src + (size_t)RPP * j * pww);
+			for (int j = 0; j < (PAIR_ROWS + RPP - 1) / RPP; ++j) {
+				const int r = rr + RPP * j;
+				if (r < PAIR_ROWS) win[warp][r][kk] = 4 * by0 + r < g.pr ? __ldg(src + (size_t)RPP * j * pww) : 0u;
+			}
 		}
 	}
-	uint32_t c[4];
+	uint32_t c0[4], c1[4];
 #pragma unroll
-	for (int i = 0; i < 4; ++i) c[i] = __ldg(cells + 4 * (size_t)blk + i);
+	for (int i = 0; i < 4; ++i) {
+		c0[i] = __ldg(cells + 4 * (size_t)blk0 + i);
+		c1[i] = two ? __ldg(cells + 4 * (size_t)blk1 + i) : 0u;
+	}
 	__syncwarp();
 	const int dx2 = 2 * (lane - 16) + px;
-	uint32_t key = 0xffffffffu;
+	uint32_t key0 = 0xffffffffu, key1 = 0xffffffffu;
 	if (dx2 >= -m && dx2 <= m) {
-		uint32_t cost[32];  // candidate rows A = a - 16
+		uint32_t cost0[32], cost1[32];  // candidate rows A = a - 16 of the upper / lower block
 #pragma unroll
-		for (int a = 0; a < 32; ++a) cost[a] = 0;
+		for (int a = 0; a < 32; ++a) cost0[a] = cost1[a] = 0;
 		const uint32_t* wrow = &win[warp][0][lane >> 2];  // bytes lane .. lane + 3 of each row
 		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(lane & 3);
 #pragma unroll
-		for (int r = 0; r < WIN_ROWS; ++r) {
+		for (int r = 0; r < PAIR_ROWS; ++r) {
 			const uint32_t v = __byte_perm(wrow[r * WIN_WORDS], wrow[r * WIN_WORDS + 1], sel);
 #pragma unroll
 			for (int i = 0; i < 4; ++i) {
-				const int a = r - i;  // window row r = 16 + A + i
-				if (a >= 0 && a < 32) cost[a] = sad4_acc(c[i], v, cost[a]);
+				const int a = r - i, b = r - 4 - i;  // window row r = 16 + A + i (upper), 20 + A + i (lower)
+				if (a >= 0 && a < 32) cost0[a] = sad4_acc(c0[i], v, cost0[a]);
+				if (b >= 0 && b < 32) cost1[b] = sad4_acc(c1[i], v, cost1[b]);
 			}
 		}
-		const uint32_t mn = py ? first_min_row<M, 1>(cost, m) : first_min_row<M, 0>(cost, m);
-		if (mn != 0xffffffffu) {
-			const int a = (int)(mn & 31u), dy2 = 2 * (a - 16) + py, nd = 2 * m + 1;
-			key = ((mn >> 5) << 12) | (uint32_t)((dy2 + m) * nd + dx2 + m);
+		uint32_t mn0, mn1;
+		if constexpr (M >= 0) {
+			mn0 = py ? first_min_row_packed<M, 1>(cost0, k16, k20) : first_min_row_packed<M, 0>(cost0, k16, k20);
+			mn1 = py ? first_min_row_packed<M, 1>(cost1, k16, k20) : first_min_row_packed<M, 0>(cost1, k16, k20);
+		} else {
+			mn0 = py ? first_min_row<M, 1>(cost0, m) : first_min_row<M, 0>(cost0, m);
+			mn1 = py ? first_min_row<M, 1>(cost1, m) : first_min_row<M, 0>(cost1, m);
 		}
+		if (mn0 != 0xffffffffu) key0 = cand_key(mn0, py, dx2, m);
+		if (mn1 != 0xffffffffu) key1 = cand_key(mn1, py, dx2, m);
 	}
 #pragma unroll
-	for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
-	if (lane == 0) best[warp] = key;
+	for (int o = 16; o > 0; o >>= 1) {
+		key0 = min(key0, __shfl_xor_sync(0xffffffffu, key0, o));
+		key1 = min(key1, __shfl_xor_sync(0xffffffffu, key1, o));
+	}
+	if (lane == 0) {
+		best[0][warp] = key0;
+		best[1][warp] = key1;
+	}
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		const uint32_t k = min(min(best[0], best[1]), min(best[2], best[3]));
+	if (threadIdx.x < 2 && (threadIdx.x == 0 || two)) {
+		const int t = threadIdx.x, blk = t ? blk1 : blk0;
+		const uint32_t k = min(min(best[t][0], best[t][1]), min(best[t][2], best[t][3]));
 		const int idx = (int)(k & 4095u), nd = 2 * m + 1;
 		centers[2 * blk] = 2 * (idx / nd - m);
 		centers[2 * blk + 1] = 2 * (idx % nd - m);
@@ -267,7 +335,9 @@ umi_status centers_impl(const uint8_t* cur, const uint8_t* ref, int h, int w, in
 	coarse_cells_kernel<<<grid, NT, 0, st>>>(cur, ref, g, words, K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes));
 	UMI_TRY(umi::launch_status("coarse_cells_kernel"));
 	auto kern = range == 60 ? coarse_search_kernel<30> : coarse_search_kernel<-1>;
-	kern<<<g.nblk, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2, centers);
+	const int pairs = (g.nby + 1) / 2 * g.nbx;
+	kern<<<pairs, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2, 16u, 1u << 20,
+	                            centers);
 	return umi::launch_status("coarse_search_kernel");
 }
 
