@@ -53,40 +53,44 @@ struct Pointers {
 // Physical coordinates of memory `m` at point p (and accumulation index a
 // when `with_a`), folded into a linear element index; `outside` reports a
 // clamped PAD coordinate (inputs only).
-template <bool CLAMP>
-__device__ __forceinline__ int64_t address(const umi_mem_plan& m, const int (&p)[4], const int (&a)[4], bool with_a,
-                                           bool& outside) {
-	int64_t addr = 0;
+// I is the index type of the launch: int32_t when the host has shown that
+// every coordinate and every linear index of the call fits 32 bits
+// (LinearMaps::fit32 and ::idx32), else int64_t.
+template <bool CLAMP, class I>
+__device__ __forceinline__ I address(const umi_mem_plan& m, const int (&p)[4], const int (&a)[4], bool with_a,
+                                     bool& outside) {
+	I addr = 0;
 	outside = false;
 #pragma unroll
 	for (int k = 0; k < 4; ++k) {
-		int64_t c = m.base[k];
+		I c = m.base[k];
 #pragma unroll
 		for (int d = 0; d < 4; ++d) {
-			c += (int64_t)m.pcoef[k][d] * p[d];
-			if (with_a) c += (int64_t)m.acoef[k][d] * a[d];
+			c += (I)m.pcoef[k][d] * p[d];
+			if (with_a) c += (I)m.acoef[k][d] * a[d];
 		}
 		if (CLAMP) {
-			const int64_t cl = c < 0 ? 0 : (c > m.size[k] - 1 ? m.size[k] - 1 : c);
+			const I hi = (I)m.size[k] - 1;
+			const I cl = c < 0 ? 0 : (c > hi ? hi : c);
 			outside |= (cl != c) && ((m.pad_mask >> k) & 1);
 			c = cl;
 		}
 #ifdef UMI_CHECKED
 		if (!CLAMP) outside |= c < 0 || c >= (m.size[k] > 0 ? m.size[k] : 1);  // output outside its extent
 #endif
-		addr += c * m.rowstride[k];
+		addr += c * (I)m.rowstride[k];
 	}
 	return addr;
 }
 
-template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class I, class P, class Arr>
 __device__ __forceinline__ void gather(const umi_plan& plan, const P& ptrs, const int (&p)[4], const int (&a)[4],
                                        bool with_a, Arr& in) {
 #pragma unroll
 	for (int i = 0; i < N; ++i) {
 		const int mem = OFS + i;
 		bool outside;
-		const int64_t addr = address<true>(plan.mem[mem], p, a, with_a, outside);
+		const I addr = address<true, I>(plan.mem[mem], p, a, with_a, outside);
 #pragma unroll
 		for (int j = 0; j < MAX_PTR; ++j) {
 			if (j < (int)Slice(PtrNum, 4, mem)) {
@@ -101,7 +105,16 @@ __device__ __forceinline__ void gather(const umi_plan& plan, const P& ptrs, cons
 //   lin[m] + sum_d p[d] * pstr[m][d] + sum_d a[d] * astr[m][d],
 // and its coordinate k spans [c_k + alo[m][k], c_k + ahi[m][k]] over the
 // accumulation range (c_k its coordinate at a = 0).  fit32: every
-// coordinate of every point and step fits comfortably in 32 bits.
+// coordinate of every point and step fits comfortably in 32 bits; idx32:
+// every linear index (clamped maps and linear forms over the launched points,
+// one expanded block past P included) and every row stride fits 31 bits.
+// gdiv / bdiv: q = (n * mul) >> shift equals n / grid[d] (n / block[d]) for
+// every n < 2^31 (Granlund & Montgomery 1994, the round-up multiplier
+// mul = ceil(2^(31 + l) / d) with l = ceil(log2 d), shift = 31 + l).
+struct FastDiv {
+	uint32_t mul;
+	int32_t shift;
+};
 struct LinearMaps {
 	int64_t lin[UMI_MAX_MEMS];
 	int64_t pstr[UMI_MAX_MEMS][4];
@@ -109,8 +122,26 @@ struct LinearMaps {
 	int64_t alo[UMI_MAX_MEMS][4];
 	int64_t ahi[UMI_MAX_MEMS][4];
 	int32_t fit32;
+	int32_t idx32;
 	int32_t bshift[4];  // log2 of the CTA block along each P dimension, -1 if not a power of two
+	FastDiv gdiv[4], bdiv[4];
 };
+
+inline FastDiv fast_div(int32_t d) {
+	FastDiv f{1u << 31, 31};  // d <= 1: n * 2^31 >> 31 = n
+	if (d > 1) {
+		int l = 0;
+		while (((int64_t)1 << l) < d) ++l;
+		const uint64_t num = (uint64_t)1 << (31 + l);
+		f.mul = (uint32_t)((num + (uint64_t)d - 1) / (uint64_t)d);
+		f.shift = 31 + l;
+	}
+	return f;
+}
+
+__device__ __forceinline__ uint32_t div_by(uint32_t n, FastDiv f) {
+	return (uint32_t)(((uint64_t)n * f.mul) >> f.shift);
+}
 
 inline LinearMaps linear_maps(const umi_plan& plan) {
 	LinearMaps L;
@@ -135,18 +166,37 @@ inline LinearMaps linear_maps(const umi_plan& plan) {
 		}
 	}
 	L.fit32 = fit;
+	bool idx = true;
+	const int64_t lim = (int64_t)1 << 31;
+	auto mag = [](int64_t v) { return v < 0 ? -v : v; };
+	for (int m = 0; m < plan.n_in + plan.n_out && m < UMI_MAX_MEMS; ++m) {
+		const umi_mem_plan& mp = plan.mem[m];
+		int64_t span = 0, lb = mag(L.lin[m]);
+		for (int k = 0; k < 4; ++k) {
+			idx &= mag(mp.rowstride[k]) < lim;
+			span += (int64_t)(mp.size[k] > 0 ? mp.size[k] - 1 : 0) * mag(mp.rowstride[k]);
+		}
+		for (int d = 0; d < 4; ++d) {
+			const int64_t preach = (int64_t)plan.ptotal[d] + (int64_t)plan.block[d] * plan.expand[d];
+			lb += mag(L.pstr[m][d]) * preach + mag(L.astr[m][d]) * (plan.atotal[d] > 0 ? plan.atotal[d] - 1 : 0);
+		}
+		idx &= span < lim && lb < lim;
+	}
+	L.idx32 = fit && idx;
 	for (int d = 0; d < 4; ++d) {
 		const int b = plan.block[d];
 		L.bshift[d] = -1;
 		for (int sh = 0; sh < 31; ++sh)
 			if (b == (1 << sh)) L.bshift[d] = sh;
+		L.gdiv[d] = fast_div(plan.grid[d]);
+		L.bdiv[d] = fast_div(plan.block[d]);
 	}
 	return L;
 }
 
 // A Pre / Post input at point p: the linear form when every coordinate is
 // inside the extent (no clamp, no padding), else the clamped map.
-template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class I, class P, class Arr>
 __device__ __forceinline__ void gather_point(const umi_plan& plan, const LinearMaps& lm, const P& ptrs,
                                              const int (&p)[4], Arr& in) {
 #pragma unroll
@@ -156,19 +206,19 @@ __device__ __forceinline__ void gather_point(const umi_plan& plan, const LinearM
 		bool inside = true;
 #pragma unroll
 		for (int k = 0; k < 4; ++k) {
-			int64_t c = m.base[k];
+			I c = m.base[k];
 #pragma unroll
-			for (int d = 0; d < 4; ++d) c += (int64_t)m.pcoef[k][d] * p[d];
-			inside &= c >= 0 && c <= (int64_t)m.size[k] - 1;
+			for (int d = 0; d < 4; ++d) c += (I)m.pcoef[k][d] * p[d];
+			inside &= c >= 0 && c <= (I)m.size[k] - 1;
 		}
-		int64_t addr;
+		I addr;
 		bool outside = false;
 		if (inside) {
-			addr = lm.lin[mem] + p[0] * lm.pstr[mem][0] + p[1] * lm.pstr[mem][1] + p[2] * lm.pstr[mem][2] +
-			       p[3] * lm.pstr[mem][3];
+			addr = (I)lm.lin[mem] + p[0] * (I)lm.pstr[mem][0] + p[1] * (I)lm.pstr[mem][1] + p[2] * (I)lm.pstr[mem][2] +
+			       p[3] * (I)lm.pstr[mem][3];
 		} else {
 			const int zero[4] = {0, 0, 0, 0};
-			addr = address<true>(m, p, zero, false, outside);
+			addr = address<true, I>(m, p, zero, false, outside);
 		}
 #pragma unroll
 		for (int j = 0; j < MAX_PTR; ++j)
@@ -181,8 +231,9 @@ __device__ __forceinline__ void gather_point(const umi_plan& plan, const LinearM
 // of the point keeps every physical coordinate inside [0, size-1] (no clamp,
 // no padding), the element of step a sits at base + sum_d a[d] * astr[d]:
 // the same element the clamped map reads, without recomputing it per step.
+template <class I>
 struct LinearAddr {
-	int64_t base;
+	I base;
 	bool inside;
 };
 
@@ -199,14 +250,16 @@ __device__ __forceinline__ bool window_inside(const umi_mem_plan& m, const Linea
 	return in;
 }
 
-__device__ __forceinline__ LinearAddr linear_addr(const umi_mem_plan& m, const LinearMaps& L, int mi, const int (&p)[4]) {
-	LinearAddr f;
-	f.base = L.lin[mi] + p[0] * L.pstr[mi][0] + p[1] * L.pstr[mi][1] + p[2] * L.pstr[mi][2] + p[3] * L.pstr[mi][3];
+template <class I>
+__device__ __forceinline__ LinearAddr<I> linear_addr(const umi_mem_plan& m, const LinearMaps& L, int mi, const int (&p)[4]) {
+	LinearAddr<I> f;
+	f.base = (I)L.lin[mi] + p[0] * (I)L.pstr[mi][0] + p[1] * (I)L.pstr[mi][1] + p[2] * (I)L.pstr[mi][2] +
+	         p[3] * (I)L.pstr[mi][3];
 	f.inside = L.fit32 ? window_inside<int32_t>(m, L, mi, p) : window_inside<int64_t>(m, L, mi, p);
 	return f;
 }
 
-template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class P, class Arr>
+template <class Umi, uint64_t PtrNum, int OFS, int N, class EType, class I, class P, class Arr>
 __device__ __forceinline__ void scatter(const umi_plan& plan, const LinearMaps& lm, const P& ptrs, const int (&p)[4],
                                         const int (&a)[4], bool with_a, const Arr& out) {
 #pragma unroll
@@ -214,7 +267,7 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const LinearMaps& 
 		const int mem = OFS + i;
 #ifdef UMI_CHECKED
 		bool outside;
-		const int64_t addr = address<false>(plan.mem[Umi::TOTAL_IN + mem], p, a, with_a, outside);
+		const I addr = address<false, I>(plan.mem[Umi::TOTAL_IN + mem], p, a, with_a, outside);
 		if (outside) {
 			atomicOr(&checked_flags_word, 1u);
 			continue;
@@ -222,9 +275,11 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const LinearMaps& 
 #else
 		// outputs are not clamped: the linear form is the map
 		const int mi = Umi::TOTAL_IN + mem;
-		int64_t addr = lm.lin[mi] + p[0] * lm.pstr[mi][0] + p[1] * lm.pstr[mi][1] + p[2] * lm.pstr[mi][2] +
-		               p[3] * lm.pstr[mi][3];
-		if (with_a) addr += a[0] * lm.astr[mi][0] + a[1] * lm.astr[mi][1] + a[2] * lm.astr[mi][2] + a[3] * lm.astr[mi][3];
+		I addr = (I)lm.lin[mi] + p[0] * (I)lm.pstr[mi][0] + p[1] * (I)lm.pstr[mi][1] + p[2] * (I)lm.pstr[mi][2] +
+		         p[3] * (I)lm.pstr[mi][3];
+		if (with_a)
+			addr += a[0] * (I)lm.astr[mi][0] + a[1] * (I)lm.astr[mi][1] + a[2] * (I)lm.astr[mi][2] +
+			        a[3] * (I)lm.astr[mi][3];
 #endif
 #pragma unroll
 		for (int j = 0; j < MAX_PTR; ++j) {
@@ -238,7 +293,7 @@ __device__ __forceinline__ void scatter(const umi_plan& plan, const LinearMaps& 
 // the Loop over A in blocked row-major order (src/UMI_gpu.h:287-346), then
 // Post; points outside P are skipped (the reference runs them and drops the
 // writes).
-template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType, int MAXT = 1024>
+template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType, int MAXT = 1024, class I = int64_t>
 __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(const umi_plan plan, const CType uc,
                                                         const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT> ptrs,
                                                         const LinearMaps lm) {
@@ -255,9 +310,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 				uint32_t r = (uint32_t)cta;
 #pragma unroll
 				for (int d = 3; d >= 0; --d) {
-					const uint32_t gd = (uint32_t)plan.grid[d];
-					const uint32_t q = r / gd;
-					g[d] = (int)(r - q * gd);
+					const uint32_t q = div_by(r, lm.gdiv[d]);
+					g[d] = (int)(r - q * (uint32_t)plan.grid[d]);
 					r = q;
 				}
 			} else {
@@ -276,8 +330,9 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 					t[d] = s & ((1 << lm.bshift[d]) - 1);
 					s >>= lm.bshift[d];
 				} else {
-					t[d] = s % plan.block[d];
-					s /= plan.block[d];
+					const int q = (int)div_by((uint32_t)s, lm.bdiv[d]);
+					t[d] = s - q * plan.block[d];
+					s = q;
 				}
 			}
 		}
@@ -301,25 +356,25 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			if (!valid[e]) continue;
 			simple_array<EType, Umi::N_PRE_IN * MAX_PTR> in;
 			simple_array<EType, Umi::N_PRE_OUT * MAX_PTR> out;
-			gather_point<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType>(plan, lm, ptrs, pts[e], in);
+			gather_point<Umi, PtrNum, PRE_I, Umi::N_PRE_IN, EType, I>(plan, lm, ptrs, pts[e], in);
 			ctx[e].Pre(uc, in, out);
-			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
+			scatter<Umi, PtrNum, PRE_O, Umi::N_PRE_OUT, EType, I>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
 		// Loop inputs: linear addressing for points whose whole window is inside.
 		constexpr int NLI = SafeArrayLength(Umi::N_LOOP_IN);
-		int64_t lbase[ES][NLI];
-		int64_t astr[NLI][4];
+		I lbase[ES][NLI];
+		I astr[NLI][4];
 		bool fast[ES];
 #pragma unroll
 		for (int i = 0; i < Umi::N_LOOP_IN; ++i)
 #pragma unroll
-			for (int d = 0; d < 4; ++d) astr[i][d] = lm.astr[LOOP_I + i][d];
+			for (int d = 0; d < 4; ++d) astr[i][d] = (I)lm.astr[LOOP_I + i][d];
 #pragma unroll
 		for (int e = 0; e < ES; ++e) {
 			bool f = Umi::N_LOOP_IN > 0;
 #pragma unroll
 			for (int i = 0; i < Umi::N_LOOP_IN; ++i) {
-				const LinearAddr la = linear_addr(plan.mem[LOOP_I + i], lm, LOOP_I + i, pts[e]);
+				const LinearAddr<I> la = linear_addr<I>(plan.mem[LOOP_I + i], lm, LOOP_I + i, pts[e]);
 				lbase[e][i] = la.base;
 				f &= la.inside;
 			}
@@ -345,7 +400,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 					for (int s0 = 0; s0 < lim[0]; ++s0)
 						for (int s1 = 0; s1 < lim[1]; ++s1)
 							for (int s2 = 0; s2 < lim[2]; ++s2) {
-								int64_t row[ES][NLI];
+								I row[ES][NLI];
 								const int ar[4] = {a0[0] + s0, a0[1] + s1, a0[2] + s2, a0[3]};
 #pragma unroll
 								for (int e = 0; e < ES; ++e)
@@ -370,7 +425,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 											row[e][i] += astr[i][3];
 										}
 										ctx[e].Loop(uc, in, out);
-										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
+										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType, I>(plan, lm, ptrs, pts[e], a, true, out);
 									}
 								}
 							}
@@ -386,9 +441,9 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 										if (!valid[e]) continue;
 										simple_array<EType, Umi::N_LOOP_IN * MAX_PTR> in;
 										simple_array<EType, Umi::N_LOOP_OUT * MAX_PTR> out;
-										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType>(plan, ptrs, pts[e], a, true, in);
+										gather<Umi, PtrNum, LOOP_I, Umi::N_LOOP_IN, EType, I>(plan, ptrs, pts[e], a, true, in);
 										ctx[e].Loop(uc, in, out);
-										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType>(plan, lm, ptrs, pts[e], a, true, out);
+										scatter<Umi, PtrNum, LOOP_O, Umi::N_LOOP_OUT, EType, I>(plan, lm, ptrs, pts[e], a, true, out);
 									}
 								}
 				}
@@ -405,10 +460,28 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) generic_kernel(cons
 			if (!valid[e]) continue;
 			simple_array<EType, Umi::N_POST_IN * MAX_PTR> in;
 			simple_array<EType, Umi::N_POST_OUT * MAX_PTR> out;
-			gather_point<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType>(plan, lm, ptrs, pts[e], in);
+			gather_point<Umi, PtrNum, POST_I, Umi::N_POST_IN, EType, I>(plan, lm, ptrs, pts[e], in);
 			ctx[e].Post(uc, in, out);
-			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType>(plan, lm, ptrs, pts[e], zero, false, out);
+			scatter<Umi, PtrNum, POST_O, Umi::N_POST_OUT, EType, I>(plan, lm, ptrs, pts[e], zero, false, out);
 		}
+	}
+}
+
+// Plans of at most 256 threads (the common case) get the variant with a
+// larger register budget; calls whose indices fit 32 bits the int32_t one.
+template <class Umi, uint64_t PtrNum, uint64_t Expand, class EType, class CType>
+void launch_generic(const umi_plan& plan, const CType& c, const Pointers<EType, Umi::TOTAL_IN, Umi::TOTAL_OUT>& ptrs,
+                    const LinearMaps& lm, unsigned grid, cudaStream_t stream) {
+	if (plan.n_threads <= 256) {
+		if (lm.idx32)
+			generic_kernel<Umi, PtrNum, Expand, EType, CType, 256, int32_t><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs, lm);
+		else
+			generic_kernel<Umi, PtrNum, Expand, EType, CType, 256, int64_t><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs, lm);
+	} else {
+		if (lm.idx32)
+			generic_kernel<Umi, PtrNum, Expand, EType, CType, 1024, int32_t><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs, lm);
+		else
+			generic_kernel<Umi, PtrNum, Expand, EType, CType, 1024, int64_t><<<grid, plan.n_threads, 0, stream>>>(plan, c, ptrs, lm);
 	}
 }
 
@@ -499,13 +572,8 @@ umi_status Execute(
 				return UMI_ERR_INVALID_ARG;
 	if (plan.n_cta == 0) return UMI_OK;
 	const unsigned grid = (unsigned)(plan.n_cta < 0x7fffffff ? plan.n_cta : 0x7fffffff);
-	// plans of at most 256 threads (the common case) get the variant with a larger register budget
-	if (plan.n_threads <= 256)
-		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType, 256><<<grid, plan.n_threads, 0, stream>>>(
-			plan, c, ptrs, gpu_detail::linear_maps(plan));
-	else
-		gpu_detail::generic_kernel<Umi, PtrNum, Expand, EType, CType><<<grid, plan.n_threads, 0, stream>>>(
-			plan, c, ptrs, gpu_detail::linear_maps(plan));
+	const gpu_detail::LinearMaps lm = gpu_detail::linear_maps(plan);
+	gpu_detail::launch_generic<Umi, PtrNum, Expand, EType, CType>(plan, c, ptrs, lm, grid, stream);
 	return cudaGetLastError() == cudaSuccess ? UMI_OK : UMI_ERR_CUDA;
 }
 

@@ -4,7 +4,8 @@
 //
 // Each trial draws parallel / accumulation spaces, tilings (valid per the
 // reference's rules), Expand words, view maps (offsets, negative strides,
-// several view dimensions folded onto one physical dimension), physical
+// several view dimensions folded onto one physical dimension, offsets 2^30
+// outside the extent that take the 64-bit index path), physical
 // sizes and PAD/WRAP modes, then runs three strategies that exercise every
 // stage and memory kind: multi-pointer Loop inputs with several Post outputs,
 // Pre and Post inputs and outputs, and Loop outputs (a running sum).  Integer
@@ -158,6 +159,13 @@ void trial_twoptr(Rng& r) {
 	std::vector<int> c0 = init, c1 = init;
 	const int pv = r.uni(-9, 9), pw = r.uni(-9, 9);
 	UnrolledI<int> im{rand_view(r, true), rand_view(r, true), ph.dims, DEFAULT_SHM, {g0, g1}, {pv, pw}};
+	if (r.uni(0, 3) == 0) {
+		// a view offset 2^30 outside the extent: every coordinate on that physical
+		// dimension clamps, and the call no longer fits 32-bit indices, so the
+		// launch takes the 64-bit instantiation of the kernel
+		const int d = r.uni(0, 3);
+		im.p_view_dims[d].ofs += r.uni(0, 1) ? (1 << 30) : -(1 << 30);
+	}
 	UnrolledI<int> imc{im.p_view_dims, im.a_view_dims, ph.dims, DEFAULT_SHM, {d0.data(), d1.data()}, {pv, pw}};
 	UnrolledO<int> om0{identity_view(), rand_view(r, false), p_shaped(tot), {o0}};
 	UnrolledO<int> om1{identity_view(), rand_view(r, false), p_shaped(tot), {o1}};

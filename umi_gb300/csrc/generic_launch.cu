@@ -191,10 +191,7 @@ umi_status launch_as(const umi_plan& plan0, const void* const* in, const void* p
 	if (n_cta == 0) return umi::ok();
 	const unsigned grid = (unsigned)(n_cta < 0x7fffffff ? n_cta : 0x7fffffff);
 	const gpu_detail::LinearMaps lm = gpu_detail::linear_maps(plan);
-	if (plan.n_threads <= 256)
-		gpu_detail::generic_kernel<Umi, kOnePtr, 0x1111, E, C, 256><<<grid, plan.n_threads, 0, st>>>(plan, c, ptrs, lm);
-	else
-		gpu_detail::generic_kernel<Umi, kOnePtr, 0x1111, E, C><<<grid, plan.n_threads, 0, st>>>(plan, c, ptrs, lm);
+	gpu_detail::launch_generic<Umi, kOnePtr, 0x1111, E, C>(plan, c, ptrs, lm, grid, st);
 	return umi::launch_status("generic_kernel");
 }
 
