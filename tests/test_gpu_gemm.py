@@ -17,8 +17,10 @@ def _check(got, want, scale, tol):
     assert err.max() <= tol, err.max()
 
 
+# tile widths: 4096^3 and most small shapes take 224-column tiles (ragged last
+# column), 2048 x 2048 the 256-column ones (fewer rounds of persistent tiles)
 @pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 1024), (128, 256, 8), (200, 300, 72), (1, 1, 16),
-                                   (384, 256, 4096), (130, 520, 136)])
+                                   (384, 256, 4096), (130, 520, 136), (2048, 2048, 256)])
 @pytest.mark.parametrize("dt", ["bf16", "f16"])
 def test_gemm_half(umi, orc, dev, M, N, K, dt):
     import torch

@@ -44,9 +44,11 @@ struct GemmArgs {
 	unsigned long long acc_wait_ns;  // limit of the epilogue's wait for a finished accumulator (kWaitNs)
 };
 
-// C[M,N] = A[M,K] B[N,K]^T: grid (N/BN, M/BM).
-struct GemmPolicy {
-	static constexpr int BN = 256, STAGES = 4;
+// C[M,N] = A[M,K] B[N,K]^T: grid (N/BN, M/BM).  BN = 256, or 224 where it
+// fills the last round of persistent tiles better (gemm_launch chooses).
+template <int BN_>
+struct GemmPolicyT {
+	static constexpr int BN = BN_, STAGES = 4;
 	static constexpr bool RESIDENT_B = false;
 	static constexpr int NK_RES = 0;
 	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
@@ -87,6 +89,16 @@ struct GemmPolicy {
 		}
 	}
 };
+using GemmPolicy = GemmPolicyT<256>;
+using GemmPolicy224 = GemmPolicyT<224>;
+
+// TMEM columns of two accumulators of BN columns: the allocation unit is a
+// power of two of at least 32 columns.
+__host__ __device__ constexpr uint32_t tmem_cols_for(int bn) {
+	uint32_t c = 32;
+	while (c < 2u * (uint32_t)bn) c <<= 1;
+	return c;
+}
 
 // 2-D convolution, stride 1, zero padding r/2, as an implicit GEMM:
 // rows = 128 output pixels of one image row (n, y, x0..x0+127), columns =
@@ -341,7 +353,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		tma_prefetch(&tb);
 	}
 	if (warp == 1) {
-		tmem_alloc(tmem_slot, 2 * BN);
+		tmem_alloc(tmem_slot, tmem_cols_for(BN));
 		tmem_relinquish();
 	}
 	tc_fence_before();
@@ -482,7 +494,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	__syncthreads();
 	if (warp == 1) {
 		tc_fence_after();
-		tmem_dealloc(tmem, 2 * BN);
+		tmem_dealloc(tmem, tmem_cols_for(BN));
 	}
 }
 
@@ -884,7 +896,6 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 	const CUtensorMapDataType dt = ab_type ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 	CUtensorMap ta, tb;
 	UMI_TRY(map_kmajor(&ta, A, dt, M, K, BM));
-	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
 	GemmArgs g{C, M, N, K, N, umi::aligned(C, 16) && N % 4 == 0, err, acc_wait_ns};
 	CUtensorMap tc;
 	std::memset(&tc, 0, sizeof(tc));
@@ -899,12 +910,33 @@ umi_status gemm_launch(const void* A, const void* B, float* C, int M, int N, int
 		                       CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 		if (r != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "gemm: C tensor map (%d)", (int)r);
 	}
-	if ((int64_t)umi::ceil_div(M, BM) * umi::ceil_div(N, GemmPolicy::BN) > INT32_MAX)
+	if ((int64_t)umi::ceil_div(M, BM) * umi::ceil_div(N, GemmPolicy224::BN) > INT32_MAX)
 		return umi::fail(UMI_ERR_UNSUPPORTED, "gemm: too many tiles");
+	// One CTA per SM works through the tiles in rounds; a round costs about the
+	// same for every tile (the MMAs run the full width), so pick the width
+	// whose rounds x width is smaller: 4096^3 is 512 tiles of 256 (3.4 rounds
+	// on 152 SMs, 4 x 256 column-units) or 608 of 224 (exactly 4 rounds,
+	// 4 x 224).
+	int dev = 0, sms = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	const int64_t mt = umi::ceil_div(M, BM);
+	const int64_t r256 = umi::ceil_div(mt * umi::ceil_div(N, 256), (int64_t)sms);
+	const int64_t r224 = umi::ceil_div(mt * umi::ceil_div(N, 224), (int64_t)sms);
+	if (r224 * 224 < r256 * 256) {
+		UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy224::BN));
+		constexpr size_t SMEM = smem_bytes<GemmPolicy224>();
+		auto kern = tc_kernel<GemmPolicy224>;
+		int grid = 0;
+		UMI_TRY(persistent_grid(kern, SMEM, GemmPolicy224::ntiles(g), tmem_cols_for(GemmPolicy224::BN), &grid));
+		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tc, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy224::BN));
+		return umi::launch_status("tc_kernel<gemm 224>");
+	}
+	UMI_TRY(map_kmajor(&tb, B, dt, N, K, GemmPolicy::BN));
 	constexpr size_t SMEM = smem_bytes<GemmPolicy>();
 	auto kern = tc_kernel<GemmPolicy>;
 	int grid = 0;
-	UMI_TRY(persistent_grid(kern, SMEM, GemmPolicy::ntiles(g), 2 * GemmPolicy::BN, &grid));
+	UMI_TRY(persistent_grid(kern, SMEM, GemmPolicy::ntiles(g), tmem_cols_for(GemmPolicy::BN), &grid));
 	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tc, g, idesc_f16((uint32_t)ab_type, BM, GemmPolicy::BN));
 	return umi::launch_status("tc_kernel<gemm>");
 }
@@ -1142,20 +1174,20 @@ umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, 
 	if (strip) {
 		constexpr size_t SMEM = smem_bytes<ConvStripPolicy>();
 		auto kern = tc_kernel<ConvStripPolicy>;
-		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvStripPolicy::BN, &grid));
+		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, tmem_cols_for(ConvStripPolicy::BN), &grid));
 		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvStripPolicy::BN));
 		return umi::launch_status("tc_kernel<conv, strips>");
 	}
 	if (g.ktiles == 1 && r * r * (c / BK) <= ConvResPolicy::NK_RES) {
 		constexpr size_t SMEM = smem_bytes<ConvResPolicy>();
 		auto kern = tc_kernel<ConvResPolicy>;
-		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvResPolicy::BN, &grid));
+		UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, tmem_cols_for(ConvResPolicy::BN), &grid));
 		kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvResPolicy::BN));
 		return umi::launch_status("tc_kernel<conv, resident weights>");
 	}
 	constexpr size_t SMEM = smem_bytes<ConvPolicy>();
 	auto kern = tc_kernel<ConvPolicy>;
-	UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, 2 * ConvPolicy::BN, &grid));
+	UMI_TRY(persistent_grid(kern, SMEM, (int)tiles, tmem_cols_for(ConvPolicy::BN), &grid));
 	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, ConvPolicy::BN));
 	return umi::launch_status("tc_kernel<conv>");
 }
@@ -1199,7 +1231,7 @@ umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const flo
 	constexpr size_t SMEM = smem_bytes<MenetConvPolicy>();
 	auto kern = tc_kernel<MenetConvPolicy>;
 	int grid = 0;
-	UMI_TRY(persistent_grid(kern, SMEM, MenetConvPolicy::ntiles(g), 2 * MenetConvPolicy::BN, &grid));
+	UMI_TRY(persistent_grid(kern, SMEM, MenetConvPolicy::ntiles(g), tmem_cols_for(MenetConvPolicy::BN), &grid));
 	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, MenetConvPolicy::BN));
 	return umi::launch_status("tc_kernel<menet conv>");
 }
