@@ -43,7 +43,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # captured).  batched_uneven's fused launch was captured on its 4-image case
 # (8 725 530 px): its traffic grows with the pixel count, so it is kept per
 # pixel and scaled to the configured batch.
-NCU_TRAFFIC = {"int_pair_1080p": (4178432, 0), "filter3x3_1024": (4204544, 0), "gemm_4096": (76233472, 35101184),
+NCU_TRAFFIC = {"int_pair_1080p": (4178432, 0), "filter3x3_1024": (4204544, 0), "gemm_4096": (72876544, 36060160),
                "fprop_n32": (67321088, 206541312), "learned_me_4k": None,
                # the proposal: cells kernel (both frames read once) + coarse search (planes and cells)
                "coarse_me_4k": (16615680 + 2795520, 0),
