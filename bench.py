@@ -4,10 +4,10 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
 Default workload `int_pair_1080p` (the integer-pair configuration): one step =
-the integral image of a 1920x1080 uint8 frame (umi_iimg_u8_i32) plus
-full-search motion estimation of a 1920x1080 uint8 pair, 16x16 blocks, +-32,
-fused argmin (umi_full_me_u8).  Metric: full_me Mblocks/s (8040 blocks per
-step).  Other workloads: `filter3x3_1024` (1024x1024 float32, 3x3 N(0,1)
+the integral image of a 1920x1080 uint8 frame (umi_iimg_u8_i32, on a second
+stream) beside full-search motion estimation of a 1920x1080 uint8 pair,
+16x16 blocks, +-32, fused argmin (umi_full_me_u8), joined every step.
+Metric: full_me Mblocks/s (8040 blocks per step).  Other workloads: `filter3x3_1024` (1024x1024 float32, 3x3 N(0,1)
 weights, zero pad; metric GB/s).
 
 Prints ONE JSON line (rank 0).  `value` is timed with CUDA events around
@@ -198,7 +198,8 @@ class IntPair:
 
     def config(self):
         return {"workload": self.name, "frame": f"{self.W}x{self.H} u8", "block": self.B, "search": f"+-{self.R}",
-                "argmin": "fused, first in raster order", "step": "iimg(cur) + full_me(cur, ref)",
+                "argmin": "fused, first in raster order",
+                "step": "iimg(cur) on a second stream beside full_me(cur, ref), joined every step",
                 "l2": "rotating input copies, consecutive steps touch > L2"}
 
     def units_per_step(self):
@@ -224,11 +225,21 @@ class IntPair:
         self.h_ii = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
         self.h_mv = torch.empty((self.nblk, 3), dtype=torch.int32).pin_memory()
         self.launches_per_step = 3  # iimg: 2 kernels (group column sums, output pass), full_me: 1
+        self.side = torch.cuda.Stream(device=dev)
 
     def step(self, i):
+        """The two operators are independent: the integral image (memory-latency
+        bound) runs on a second stream beside the search (integer-ALU bound),
+        both through the C ABI, joined before the step ends (the workspace
+        and buffers of one step are not reused before the join)."""
+        import torch
         k = i % self.n_rot
-        self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k], workspace=self.ws)
+        cur = torch.cuda.current_stream()
+        self.side.wait_stream(cur)
+        with torch.cuda.stream(self.side):
+            self.U.iimg_u8_i32(self.d_cur[k], out=self.d_ii[k], workspace=self.ws)
         self.U.full_me_u8(self.d_cur[k], self.d_ref[k], self.B, self.R, out=self.d_mv[k])
+        cur.wait_stream(self.side)
 
     def h2d(self, k):
         self.d_cur[k].copy_(self.h_cur, non_blocking=True)
