@@ -1049,6 +1049,7 @@ class Apps1080p:
         self.h_out = torch.empty((self.H, self.W), dtype=torch.int32).pin_memory()
         # census + dilate + (iimg 2 kernels + J copy + box) + gaussian 2
         self.launches_per_step = 1 + 1 + 4 + 2
+        self.s1, self.s2 = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
         for k in range(self.n_rot):  # constants made before any graph capture
             self.step(k)
 
@@ -1064,9 +1065,22 @@ class Apps1080p:
             a.gaussian(self.f32[k], 2.0, out=self.o_g[k], tmp=self.tmp[k])
 
     def step(self, i):
+        """The four operators are independent: census and dilation on one
+        stream, the box sums (integral image, copy, generic launch) on a
+        second, the Gaussian passes on the caller's, joined every step."""
+        import torch
         k = i % self.n_rot
-        for name in ("census", "dilate", "box_sum", "gaussian"):
-            self._op(name, k)
+        cur = torch.cuda.current_stream()
+        self.s1.wait_stream(cur)
+        self.s2.wait_stream(cur)
+        with torch.cuda.stream(self.s1):
+            self._op("census", k)
+            self._op("dilate", k)
+        with torch.cuda.stream(self.s2):
+            self._op("box_sum", k)
+        self._op("gaussian", k)
+        cur.wait_stream(self.s1)
+        cur.wait_stream(self.s2)
 
     def h2d(self, k):
         self.u8[k].copy_(self.h_u8[k], non_blocking=True)
