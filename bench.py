@@ -1024,7 +1024,8 @@ class Apps1080p:
     def config(self):
         return {"workload": self.name, "frame": f"{self.W}x{self.H}", "ops": "census r2, dilate r1, box r7 "
                 "(integral image + 4 corner reads), gaussian sigma 2 (13 taps, two passes)",
-                "bytes_per_px": self.BYTES, "l2": "4 frame sets rotated (> L2)"}
+                "bytes_per_px": self.BYTES, "l2": "4 frame sets rotated (> L2)",
+                "streams": "census + dilate | box | gaussian, joined every step"}
 
     def units_per_step(self):
         return self.px / 1e6
