@@ -507,35 +507,70 @@ constexpr size_t smem_bytes() {
 	           : (size_t)P::STAGES * (BM * BK * 2 + P::BN * BK * 2) + epi + 1024 + 256;
 }
 
-// 3x3 convolution in the strip form (64 input channels, resident weights)
-// with one output-channel block, walking output rows in runs.  Tiles are
-// ordered id = (n * xtiles + xt) * h + y (y fastest) and CTA c takes the
-// contiguous run [c * per, (c + 1) * per); a run splits into segments of
-// consecutive rows of one (image, x tile).  Output row y reads the strips of
-// input rows y - 1, y, y + 1, so consecutive rows share two of their three:
-// the producer loads each strip of a segment once (rows y_a - 1 .. y_b + 1)
-// and the MMA warp frees a strip's ring slot after the last row that reads
-// it (a row's MMAs complete in issue order, so committing after row y frees
-// the strip of row y - 1, and after a segment's last row the two strips
-// below it).  One strip load per row instead of three, and the four ring
-// slots beside the 144 KB of weights hold a whole row of lookahead.  The
-// epilogue, whose NCHW stores (256 MiB at the benchmark shape) bound the
-// kernel, runs on RUN_EPI_WARPS warps: RUN_EPI_WARPS / 4 per TMEM lane
-// quadrant, each storing an equal share of the output channels.  Waits,
-// abort and drain as in tc_kernel.
-constexpr int RUN_EPI_WARPS = 8;
-constexpr int RUN_THREADS = 64 + 32 * RUN_EPI_WARPS;
-__global__ void __launch_bounds__(RUN_THREADS, 1)
-	conv_run_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const ConvArgs g,
-	                const uint32_t idesc, const int per) {
-	using P = ConvStripPolicy;
-	constexpr int BN = P::BN, STAGES = P::STAGES;
-	constexpr uint32_t B_TILE = BN * BK * 2, SS = P::STRIP_STAGE;
+// 3x3 convolution in the strip form (64 input channels, at most 128 outputs,
+// resident weights, one TMA box per filter row) walking output rows in runs;
+// T supplies the geometry (ConvRun).  The tiles of a block of columns (image
+// and x tile) are ordered by row class (y mod d, one class for d = 1) and
+// then by y, id = block * h + pos, and CTA c takes the contiguous run
+// [c * per, (c + 1) * per); a run splits into segments of consecutive
+// positions of one block and one class, whose output rows step by d.  Output
+// row y reads the strips of input rows y - d, y, y + d, so consecutive rows of
+// a segment share two of their three: the producer loads each strip of a
+// segment once (rows y_a - d .. y_b + d) and the MMA warp frees a strip's
+// ring slot after the last row that reads it (a row's MMAs complete in issue
+// order, so committing after row y frees the strip of row y - d, and after a
+// segment's last row the two strips below it).  One strip load per row
+// instead of three.  The epilogue, whose NCHW stores (256 MiB at the
+// benchmark shape) bound the kernel, runs on T::EPI_WARPS warps,
+// T::EPI_WARPS / 4 per TMEM lane quadrant, each storing an equal share of the
+// output channels.  Waits, abort and drain as in tc_kernel.
+struct ConvRun {
+	using Args = ConvArgs;
+	static constexpr int BN = ConvStripPolicy::BN, STAGES = ConvStripPolicy::STAGES, NK_RES = 9, EPI_WARPS = 8;
+	static constexpr uint32_t STRIP_STAGE = ConvStripPolicy::STRIP_STAGE;
+	__device__ static uint32_t strip_bytes(const Args&) { return ConvStripPolicy::STRIP_BYTES; }
+	__device__ static int dil(const Args&) { return 1; }
+	__host__ __device__ static int rows(const Args& g) { return g.h; }
+	__host__ __device__ static int blocks(const Args& g) { return g.n * g.xtiles; }
+	// output row of position pos, and the end of its row class (one class)
+	__device__ static void row_of(const Args& g, int pos, int& y, int& class_end) {
+		y = pos;
+		class_end = g.h;
+	}
+	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, int blk, int row, void* dst, uint64_t* bar) {
+		const int n = blk / g.xtiles, x0 = (blk - n * g.xtiles) * BM;
+		tma_load_4d(dst, ta, bar, 0, x0 - 1, row, n);
+	}
+	__device__ static void load_b(const CUtensorMap* tb, const Args& g, int ks, void* b, uint64_t* bar) {
+		ConvStripPolicy::load_b(tb, g, ks, b, bar);
+	}
+	__device__ static void store(const Args& g, int blk, int y, int rl, int c, const float (&v)[32]) {
+		ConvPolicy::Tile t;
+		t.n = blk / g.xtiles;
+		t.y = y;
+		t.x0 = (blk - t.n * g.xtiles) * BM;
+		t.k0 = 0;
+		ConvPolicy::store(g, t, rl, c, v);
+	}
+};
+template <class T>
+constexpr int run_threads() { return 64 + 32 * T::EPI_WARPS; }
+template <class T>
+constexpr size_t run_smem_bytes() {
+	return (size_t)T::STAGES * T::STRIP_STAGE + (size_t)T::NK_RES * (T::BN * BK * 2) + 1024 + 256;
+}
+
+template <class T>
+__global__ void __launch_bounds__(run_threads<T>(), 1)
+	strip_run_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+	                 const typename T::Args g, const uint32_t idesc, const int per) {
+	constexpr int BN = T::BN, STAGES = T::STAGES, NKR = T::NK_RES;
+	constexpr uint32_t B_TILE = BN * BK * 2, SS = T::STRIP_STAGE;
 	static_assert(STAGES >= 3, "an output row reads three strips at once");
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* bres = base + STAGES * SS;
-	uint64_t* full = reinterpret_cast<uint64_t*>(bres + P::NK_RES * B_TILE);
+	uint64_t* full = reinterpret_cast<uint64_t*>(bres + NKR * B_TILE);
 	uint64_t* empty = full + STAGES;
 	uint64_t* accfull = empty + STAGES;  // [2]
 	uint64_t* accempty = accfull + 2;    // [2]
@@ -544,10 +579,15 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bready + 1);
 	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int ntiles = g.n * g.xtiles * g.h;
+	const int H = T::rows(g), ntiles = T::blocks(g) * H, d = T::dil(g);
 	const int t0 = blockIdx.x * per, t1 = min(ntiles, t0 + per);
-	// the segment of the run starting at tile s0: [s0, seg_end(s0))
-	auto seg_end = [&](int s0) { return min(t1, (s0 / g.h + 1) * g.h); };
+	// the segment of the run starting at tile s0: block, first output row, end
+	auto segment = [&](int s0, int& blk, int& y0, int& s1) {
+		blk = s0 / H;
+		int pend;
+		T::row_of(g, s0 - blk * H, y0, pend);
+		s1 = min(t1, blk * H + pend);
+	};
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < STAGES; ++s) {
@@ -556,7 +596,7 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 		}
 		for (int a = 0; a < 2; ++a) {
 			mbar_init(&accfull[a], 1);
-			mbar_init(&accempty[a], RUN_EPI_WARPS);
+			mbar_init(&accempty[a], T::EPI_WARPS);
 		}
 		mbar_init(drain, 1);
 		mbar_init(bready, 1);
@@ -578,20 +618,21 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 		// ---- producer: weights once, then every strip of every segment once
 		int armed[STAGES];
 		for (int s = 0; s < STAGES; ++s) armed[s] = -1;
-		mbar_arrive_expect_tx(bready, (uint32_t)P::NK_RES * B_TILE);
-		for (int ks = 0; ks < P::NK_RES; ++ks) P::load_b(&tb, g, ks, bres + ks * B_TILE, bready);
+		mbar_arrive_expect_tx(bready, (uint32_t)NKR * B_TILE);
+		for (int ks = 0; ks < NKR; ++ks) T::load_b(&tb, g, ks, bres + ks * B_TILE, bready);
+		const uint32_t sbytes = T::strip_bytes(g);
 		uint32_t q = 0;
 		bool go = true;
 		for (int s0 = t0; go && s0 < t1 && !*abort_flag;) {
-			const int s1 = seg_end(s0), hb = s0 / g.h, n = hb / g.xtiles, x0 = (hb - n * g.xtiles) * BM;
-			const int y0 = s0 - hb * g.h;
-			for (int i = 0; i < s1 - s0 + 2; ++i, ++q) {  // input row y0 - 1 + i
+			int blk, y0, s1;
+			segment(s0, blk, y0, s1);
+			for (int i = 0; i < s1 - s0 + 2; ++i, ++q) {  // input row y0 + (i - 1) d
 				const int s = (int)(q % STAGES);
 				const uint32_t round = q / STAGES;
 				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) { go = false; break; }
-				mbar_arrive_expect_tx(&full[s], P::STRIP_BYTES);
+				mbar_arrive_expect_tx(&full[s], sbytes);
 				armed[s] = (int)round;
-				tma_load_4d(base + s * SS, &ta, &full[s], 0, x0 - 1, y0 - 1 + i, n);
+				T::load_strip(&ta, g, blk, y0 + (i - 1) * d, base + s * SS, &full[s]);
 			}
 			s0 = s1;
 		}
@@ -607,8 +648,10 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 		uint32_t q0 = 0;  // first strip of the segment
 		int i = 0;        // tiles so far (accumulator a = i & 1)
 		for (int s0 = t0; ok && s0 < t1 && !*abort_flag;) {
-			const int s1 = seg_end(s0), rows = s1 - s0;
-			for (int k = 0; ok && k < rows; ++k, ++i) {  // output row y0 + k: strips q0 + k .. q0 + k + 2
+			int blk, y0, s1;
+			segment(s0, blk, y0, s1);
+			const int rows = s1 - s0;
+			for (int k = 0; ok && k < rows; ++k, ++i) {  // output row y0 + k d: strips q0 + k .. q0 + k + 2
 				const int a = i & 1;
 				const uint32_t use = (uint32_t)(i >> 1);
 				if (!mbar_wait(&accempty[a], (use & 1) ^ 1, abort_flag, g.err, kErrTimeoutAccEmpty)) { ok = false; break; }
@@ -623,7 +666,7 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 					tc_fence_after();
 #pragma unroll
 					for (int dx = 0; dx < 3; ++dx) {
-						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * SS), dx);
+						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * SS), dx * d);
 						const uint64_t bd = desc_kmajor_sw128(smem_u32(bres + (dy * 3 + dx) * B_TILE));
 #pragma unroll
 						for (int kk = 0; kk < BK / 16; ++kk)
@@ -631,7 +674,7 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 					}
 				}
 				if (!ok) break;
-				mma_commit(&empty[(q0 + (uint32_t)k) % STAGES]);  // the strip of row y0 + k - 1: last read here
+				mma_commit(&empty[(q0 + (uint32_t)k) % STAGES]);  // the strip of row y0 + (k - 1) d: last read here
 				if (k == rows - 1) {
 					mma_commit(&empty[(q0 + (uint32_t)k + 1) % STAGES]);
 					mma_commit(&empty[(q0 + (uint32_t)k + 2) % STAGES]);
@@ -647,8 +690,8 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 	} else if (warp >= 2) {
 		// ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (pixels of the
 		// row), output channels [part * SPAN, +SPAN) with part = (w - 2) / 4
-		constexpr int SPAN = BN / (RUN_EPI_WARPS / 4);
-		static_assert(RUN_EPI_WARPS % 4 == 0 && SPAN % 32 == 0, "whole 32-column TMEM loads per warp");
+		constexpr int SPAN = BN / (T::EPI_WARPS / 4);
+		static_assert(T::EPI_WARPS % 4 == 0 && SPAN % 32 == 0, "whole 32-column TMEM loads per warp");
 		const int qd = warp & 3, part = (warp - 2) >> 2;
 		int i = 0;
 		for (int id = t0; id < t1; ++id, ++i) {
@@ -656,17 +699,14 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 			const uint32_t use = (uint32_t)(i >> 1);
 			if (!mbar_wait(&accfull[a], use & 1, abort_flag, g.err, kErrTimeoutAccum)) break;
 			tc_fence_after();
-			const int hb = id / g.h, n = hb / g.xtiles;
-			ConvPolicy::Tile t;
-			t.n = n;
-			t.y = id - hb * g.h;
-			t.x0 = (hb - n * g.xtiles) * BM;
-			t.k0 = 0;
+			const int blk = id / H;
+			int y, pend;
+			T::row_of(g, id - blk * H, y, pend);
 #pragma unroll 1
 			for (int c = part * SPAN; c < (part + 1) * SPAN; c += 32) {
 				float v[32];
 				tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * BN + c), v);
-				P::store(g, t, 32 * qd + lane, c, v);
+				T::store(g, blk, y, 32 * qd + lane, c, v);
 			}
 			tc_fence_before();
 			__syncwarp();
@@ -679,6 +719,29 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
 		tc_fence_after();
 		tmem_dealloc(tmem, tmem_cols_for(BN));
 	}
+}
+
+// Launch of strip_run_kernel<T> over `tiles` tiles: one CTA per SM, each a
+// contiguous run of ceil(tiles / CTAs) tiles.
+template <class T>
+umi_status launch_strip_run(const CUtensorMap& ta, const CUtensorMap& tb, const typename T::Args& g, int64_t tiles,
+                            cudaStream_t st, const char* what) {
+	constexpr size_t SMEM = run_smem_bytes<T>();
+	auto kern = strip_run_kernel<T>;
+	UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
+	                         "cudaFuncSetAttribute"));
+	int dev = 0, sms = 0, per_sm = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, run_threads<T>(), SMEM),
+	                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
+	per_sm = std::min(per_sm, 512 / (int)tmem_cols_for(T::BN));
+	if (per_sm < 1) return umi::fail(UMI_ERR_UNSUPPORTED, "%s: does not fit an SM", what);
+	int grid = (int)std::min<int64_t>(tiles, (int64_t)per_sm * sms);
+	const int per = (int)umi::ceil_div(tiles, (int64_t)grid);
+	grid = (int)umi::ceil_div(tiles, (int64_t)per);
+	kern<<<grid, run_threads<T>(), SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, T::BN), per);
+	return umi::launch_status(what);
 }
 
 // Persistent grid: as many CTAs as fit on the GPU at once (each holds 2*BN of
@@ -1345,24 +1408,8 @@ umi_status conv_launch(const void* x, const void* wt, float* out, int n, int c, 
 	const int64_t tiles = (int64_t)n * h * g.xtiles * g.ktiles;
 	if (tiles > INT32_MAX) return umi::fail(UMI_ERR_UNSUPPORTED, "conv: too many tiles");
 	int grid = 0;
-	if (strip) {  // k <= BN: one output-channel block; runs of output rows, each input row's strip loaded once per run
-		constexpr size_t SMEM = smem_bytes<ConvStripPolicy>();
-		UMI_TRY(umi::cuda_status(cudaFuncSetAttribute(conv_run_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                              (int)SMEM), "cudaFuncSetAttribute"));
-		int dev = 0, sms = 0, per_sm = 0;
-		UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
-		UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
-		                         "cudaDeviceGetAttribute"));
-		UMI_TRY(umi::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_run_kernel, RUN_THREADS, SMEM),
-		                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor"));
-		per_sm = std::min(per_sm, 512 / (int)tmem_cols_for(ConvStripPolicy::BN));
-		if (per_sm < 1) return umi::fail(UMI_ERR_UNSUPPORTED, "conv_run_kernel: does not fit an SM");
-		grid = (int)std::min<int64_t>(tiles, (int64_t)per_sm * sms);
-		const int per = (int)umi::ceil_div(tiles, (int64_t)grid);
-		grid = (int)umi::ceil_div(tiles, (int64_t)per);
-		conv_run_kernel<<<grid, RUN_THREADS, SMEM, st>>>(ta, tb, g, idesc_f16(1u, BM, ConvStripPolicy::BN), per);
-		return umi::launch_status("conv_run_kernel");
-	}
+	if (strip)  // k <= BN: one output-channel block; runs of output rows, each input row's strip loaded once per run
+		return launch_strip_run<ConvRun>(ta, tb, g, tiles, st, "strip_run_kernel<conv>");
 	if (g.ktiles == 1 && r * r * (c / BK) <= ConvResPolicy::NK_RES) {
 		constexpr size_t SMEM = smem_bytes<ConvResPolicy>();
 		auto kern = tc_kernel<ConvResPolicy>;
