@@ -22,10 +22,10 @@
 // the four cells of a row are one unaligned word, one vabsdiff4 per cell row.
 // cur's cells are four words per block.
 //
-// Search kernel: one CTA per pair of vertically adjacent blocks, one warp per
-// plane, one lane per candidate column B holding 32 candidate rows of each
-// block in registers; the argmin key (sad << 12) | raster index is reduced
-// per warp, then over the four warps.
+// Search kernel: one CTA per run of three vertically adjacent blocks, one
+// warp per plane, one lane per candidate column B holding 32 candidate rows of
+// each block in registers; the argmin key (sad << 12) | raster index is
+// reduced per warp, then over the four warps.
 #include <algorithm>
 #include <climits>
 
@@ -208,26 +208,26 @@ __device__ __forceinline__ uint32_t cand_key(uint32_t mn, int py, int dx2, int m
 	return ((mn >> 5) << 12) | (uint32_t)((dy2 + m) * nd + dx2 + m);
 }
 
-// One CTA per pair of vertically adjacent blocks (2 p, 2 p + 1) of one block
-// column, one warp per plane (py, px), one lane per candidate column
-// B = lane - 16.  The lane streams the 39 plane rows the pair's windows cover
-// once: one realigned word per row (two shared loads and a prmt) meets the
-// four cell rows i of the upper block at candidate rows A = row - 16 - i and
-// those of the lower block at A = row - 20 - i, so a candidate costs four
-// vabsdiff4 and about a fifth of a prmt; 64 costs stay in registers.
-// M = range / 2 at compile time (the default range 60: packed 16-bit argmin),
-// or M < 0 for any range (runtime masks).
-constexpr int PAIR_ROWS = WIN_ROWS + 4;
+// One CTA per run of NBK vertically adjacent blocks (NBK p .. NBK p + NBK - 1)
+// of one block column, one warp per plane (py, px), one lane per candidate
+// column B = lane - 16.  The lane streams the 35 + 4 (NBK - 1) plane rows the
+// run's windows cover once: one realigned word per row (two shared loads and
+// a prmt) meets the four cell rows i of block bb at candidate rows
+// A = row - 16 - 4 bb - i, so a candidate costs four vabsdiff4 and a small
+// share of a prmt; 32 NBK costs stay in registers.  M = range / 2 at compile
+// time (the default range 60: packed 16-bit argmin), or M < 0 for any range
+// (runtime masks).  Three blocks per CTA: 61.5 us at 4K against 65.6 us for
+// two (four: the same as three, with 159 registers).
+constexpr int NBK = 3;
+constexpr int RUN_ROWS = WIN_ROWS + 4 * (NBK - 1);
 template <int M>
 __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __restrict__ cells,
                                                             const uint32_t* __restrict__ planes, CoarseGeom g, int m_rt,
                                                             uint32_t k16, uint32_t k20, int32_t* __restrict__ centers) {
 	const int m = M >= 0 ? M : m_rt;
-	__shared__ uint32_t win[4][PAIR_ROWS][WIN_WORDS];
-	__shared__ uint32_t best[2][4];
-	const int pr = blockIdx.x / g.nbx, bx = blockIdx.x - pr * g.nbx, by0 = 2 * pr;
-	const bool two = by0 + 1 < g.nby;
-	const int blk0 = by0 * g.nbx + bx, blk1 = blk0 + g.nbx;
+	__shared__ uint32_t win[4][RUN_ROWS][WIN_WORDS];
+	__shared__ uint32_t best[NBK][4];
+	const int run = blockIdx.x / g.nbx, bx = blockIdx.x - run * g.nbx, by0 = NBK * run;
 	const int pww = g.pw / 4;
 	const size_t plane_words = (size_t)g.pr * pww;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, py = warp >> 1, px = warp & 1;
@@ -236,63 +236,65 @@ __global__ void __launch_bounds__(128) coarse_search_kernel(const uint32_t* __re
 		const int kk = lane % WIN_WORDS, rr = lane / WIN_WORDS;
 		if (rr < RPP) {
 			// word bx + k <= nbx + 7 < pww; plane row 4 by0 + r < pr except the last
-			// four rows when the lower block does not exist (those stay zero)
+			// rows of a run whose lower blocks do not exist (those stay zero)
 			const uint32_t* src = planes + warp * plane_words + (size_t)(4 * by0 + rr) * pww + bx + kk;
 #pragma unroll
-			for (int j = 0; j < (PAIR_ROWS + RPP - 1) / RPP; ++j) {
+			for (int j = 0; j < (RUN_ROWS + RPP - 1) / RPP; ++j) {
 				const int r = rr + RPP * j;
-				if (r < PAIR_ROWS) win[warp][r][kk] = 4 * by0 + r < g.pr ? __ldg(src + (size_t)RPP * j * pww) : 0u;
+				if (r < RUN_ROWS) win[warp][r][kk] = 4 * by0 + r < g.pr ? __ldg(src + (size_t)RPP * j * pww) : 0u;
 			}
 		}
 	}
-	uint32_t c0[4], c1[4];
+	uint32_t c[NBK][4];
 #pragma unroll
-	for (int i = 0; i < 4; ++i) {
-		c0[i] = __ldg(cells + 4 * (size_t)blk0 + i);
-		c1[i] = two ? __ldg(cells + 4 * (size_t)blk1 + i) : 0u;
-	}
+	for (int bb = 0; bb < NBK; ++bb)
+#pragma unroll
+		for (int i = 0; i < 4; ++i)
+			c[bb][i] = by0 + bb < g.nby ? __ldg(cells + 4 * (size_t)((by0 + bb) * g.nbx + bx) + i) : 0u;
 	__syncwarp();
 	const int dx2 = 2 * (lane - 16) + px;
-	uint32_t key0 = 0xffffffffu, key1 = 0xffffffffu;
-	if (dx2 >= -m && dx2 <= m) {
-		uint32_t cost0[32], cost1[32];  // candidate rows A = a - 16 of the upper / lower block
+	uint32_t key[NBK];
 #pragma unroll
-		for (int a = 0; a < 32; ++a) cost0[a] = cost1[a] = 0;
+	for (int bb = 0; bb < NBK; ++bb) key[bb] = 0xffffffffu;
+	if (dx2 >= -m && dx2 <= m) {
+		uint32_t cost[NBK][32];  // candidate rows A = a - 16 of block bb
+#pragma unroll
+		for (int bb = 0; bb < NBK; ++bb)
+#pragma unroll
+			for (int a = 0; a < 32; ++a) cost[bb][a] = 0;
 		const uint32_t* wrow = &win[warp][0][lane >> 2];  // bytes lane .. lane + 3 of each row
 		const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(lane & 3);
 #pragma unroll
-		for (int r = 0; r < PAIR_ROWS; ++r) {
+		for (int r = 0; r < RUN_ROWS; ++r) {
 			const uint32_t v = __byte_perm(wrow[r * WIN_WORDS], wrow[r * WIN_WORDS + 1], sel);
 #pragma unroll
-			for (int i = 0; i < 4; ++i) {
-				const int a = r - i, b = r - 4 - i;  // window row r = 16 + A + i (upper), 20 + A + i (lower)
-				if (a >= 0 && a < 32) cost0[a] = sad4_acc(c0[i], v, cost0[a]);
-				if (b >= 0 && b < 32) cost1[b] = sad4_acc(c1[i], v, cost1[b]);
-			}
+			for (int bb = 0; bb < NBK; ++bb)
+#pragma unroll
+				for (int i = 0; i < 4; ++i) {
+					const int a = r - 4 * bb - i;  // window row r = 16 + 4 bb + A + i
+					if (a >= 0 && a < 32) cost[bb][a] = sad4_acc(c[bb][i], v, cost[bb][a]);
+				}
 		}
-		uint32_t mn0, mn1;
-		if constexpr (M >= 0) {
-			mn0 = py ? first_min_row_packed<M, 1>(cost0, k16, k20) : first_min_row_packed<M, 0>(cost0, k16, k20);
-			mn1 = py ? first_min_row_packed<M, 1>(cost1, k16, k20) : first_min_row_packed<M, 0>(cost1, k16, k20);
-		} else {
-			mn0 = py ? first_min_row<M, 1>(cost0, m) : first_min_row<M, 0>(cost0, m);
-			mn1 = py ? first_min_row<M, 1>(cost1, m) : first_min_row<M, 0>(cost1, m);
+#pragma unroll
+		for (int bb = 0; bb < NBK; ++bb) {
+			uint32_t mn;
+			if constexpr (M >= 0)
+				mn = py ? first_min_row_packed<M, 1>(cost[bb], k16, k20) : first_min_row_packed<M, 0>(cost[bb], k16, k20);
+			else
+				mn = py ? first_min_row<M, 1>(cost[bb], m) : first_min_row<M, 0>(cost[bb], m);
+			if (mn != 0xffffffffu) key[bb] = cand_key(mn, py, dx2, m);
 		}
-		if (mn0 != 0xffffffffu) key0 = cand_key(mn0, py, dx2, m);
-		if (mn1 != 0xffffffffu) key1 = cand_key(mn1, py, dx2, m);
 	}
 #pragma unroll
-	for (int o = 16; o > 0; o >>= 1) {
-		key0 = min(key0, __shfl_xor_sync(0xffffffffu, key0, o));
-		key1 = min(key1, __shfl_xor_sync(0xffffffffu, key1, o));
-	}
-	if (lane == 0) {
-		best[0][warp] = key0;
-		best[1][warp] = key1;
-	}
+	for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+		for (int bb = 0; bb < NBK; ++bb) key[bb] = min(key[bb], __shfl_xor_sync(0xffffffffu, key[bb], o));
+	if (lane == 0)
+#pragma unroll
+		for (int bb = 0; bb < NBK; ++bb) best[bb][warp] = key[bb];
 	__syncthreads();
-	if (threadIdx.x < 2 && (threadIdx.x == 0 || two)) {
-		const int t = threadIdx.x, blk = t ? blk1 : blk0;
+	if (threadIdx.x < NBK && by0 + (int)threadIdx.x < g.nby) {
+		const int t = threadIdx.x, blk = (by0 + t) * g.nbx + bx;
 		const uint32_t k = min(min(best[t][0], best[t][1]), min(best[t][2], best[t][3]));
 		const int idx = (int)(k & 4095u), nd = 2 * m + 1;
 		centers[2 * blk] = 2 * (idx / nd - m);
@@ -335,9 +337,9 @@ umi_status centers_impl(const uint8_t* cur, const uint8_t* ref, int h, int w, in
 	coarse_cells_kernel<<<grid, NT, 0, st>>>(cur, ref, g, words, K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes));
 	UMI_TRY(umi::launch_status("coarse_cells_kernel"));
 	auto kern = range == 60 ? coarse_search_kernel<30> : coarse_search_kernel<-1>;
-	const int pairs = (g.nby + 1) / 2 * g.nbx;
-	kern<<<pairs, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2, 16u, 1u << 20,
-	                            centers);
+	const int runs = (g.nby + NBK - 1) / NBK * g.nbx;
+	kern<<<runs, 128, 0, st>>>(K.at<uint32_t>(ws, K.cells), K.at<uint32_t>(ws, K.planes), g, range / 2, 16u, 1u << 20,
+	                           centers);
 	return umi::launch_status("coarse_search_kernel");
 }
 
