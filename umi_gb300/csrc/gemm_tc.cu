@@ -51,12 +51,7 @@ struct GemmPolicyT {
 	static constexpr int BN = BN_, STAGES = 4;
 	static constexpr bool RESIDENT_B = false;
 	static constexpr int NK_RES = 0;
-	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
-	static constexpr int R = 1;
-	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
 	static constexpr bool EPI_TMA = true;  // epilogue through shared memory + TMA tile stores
-	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
-	template <class A> __device__ static int dil(const A&) { return 1; }
 	__device__ static unsigned long long acc_wait_ns(const GemmArgs& g) { return g.acc_wait_ns; }
 	using Args = GemmArgs;
 	struct Tile { int m0, n0; };
@@ -117,12 +112,7 @@ struct ConvPolicy {
 	static constexpr int BN = 128, STAGES = 3;
 	static constexpr bool RESIDENT_B = false;
 	static constexpr int NK_RES = 0;
-	static constexpr bool STRIP = false;  // one A load per filter row (conv only)
-	static constexpr int R = 1;
-	static constexpr uint32_t STRIP_BYTES = 0, STRIP_STAGE = 0;
 	static constexpr bool EPI_TMA = false;
-	template <class A> __device__ static uint32_t strip_bytes(const A&) { return STRIP_BYTES; }
-	template <class A> __device__ static int dil(const A&) { return 1; }
 	template <class A> __device__ static unsigned long long acc_wait_ns(const A&) { return kWaitNs; }
 	using Args = ConvArgs;
 	struct Tile { int n, y, x0, k0; };
@@ -219,78 +209,23 @@ struct ConvResPolicy : ConvPolicy {
 };
 
 // 3x3 convolution over 64 input channels with resident weights and one A
-// load per filter row: the strip of BM + 2 input pixels of row y + dy - 1
-// (one TMA box, zero fill outside the image) serves the three horizontal
-// taps, whose operands start 0, 1 and 2 rows into the strip.  A traffic per
-// tile drops from 9 to 3 boxes.
+// load per filter row (strip_run_kernel with ConvRun, below): the strip of
+// BM + 2 input pixels of row y + dy - 1 (one TMA box, zero fill outside the
+// image) serves the three horizontal taps, whose operands start 0, 1 and 2
+// rows into the strip.
 struct ConvStripPolicy : ConvResPolicy {
-	static constexpr bool STRIP = true;
 	static constexpr int R = 3;
 	static constexpr int STRIP_ROWS = BM + R - 1;                          // 130
 	static constexpr uint32_t STRIP_BYTES = STRIP_ROWS * BK * 2;          // 16 640 (the box)
 	static constexpr uint32_t STRIP_STAGE = (STRIP_BYTES + 1023) & ~1023u;  // 17 408
-	// (defined here: the inherited hook would read ConvPolicy::STRIP_BYTES)
-	__device__ static uint32_t strip_bytes(const Args&) { return STRIP_BYTES; }
-	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, const Tile& t, int dy, void* a,
-	                                  uint64_t* bar) {
-		tma_load_4d(a, ta, bar, 0, t.x0 - 1, t.y + dy - 1, t.n);
-	}
 };
 
-// One 3x3 layer of the motion-proposal network (32 -> 32 channels, dilation
-// d <= 8) on the tensor cores.  Activations are bf16 NHWC with 64-channel
-// pixels (channels 32..63 are zero, so one 128-byte row per pixel feeds
-// K = 64 per tap; the weights of those channels are zero too).  A tile is
-// 128 pixels of one row x 32 output channels (MMA M=128, N=32); the strip of
-// filter row dy holds the 128 + 2d input pixels of row y + (dy-1)d and the
-// three taps start 0, d, 2d rows into it.  Epilogue: + bias, ReLU, bf16, one
-// 128-byte NHWC pixel per thread (upper 64 bytes written as zeros).
+// Arguments of one motion-proposal layer (MenetRun, below).
 struct MenetArgs {
-	__nv_bfloat16* out;  // (h, w, 64) bf16
+	__nv_bfloat16* out;  // (h, w, 32) bf16
 	const float* bias;   // 32
 	int h, w, dil, xtiles;
 	int* err;
-};
-struct MenetConvPolicy {
-	static constexpr int BN = 32, STAGES = 8;
-	static constexpr bool EPI_TMA = false;
-	static constexpr bool RESIDENT_B = true;
-	static constexpr int NK_RES = 9;
-	static constexpr bool STRIP = true;
-	static constexpr int R = 3, MAXD = 8;
-	static constexpr uint32_t STRIP_BYTES = 0;  // per layer: strip_bytes()
-	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * BK * 2 + 1023) & ~1023u;  // 18 432
-	template <class A> __device__ static unsigned long long acc_wait_ns(const A&) { return kWaitNs; }
-	using Args = MenetArgs;
-	struct Tile { int y, x0; };
-	__host__ __device__ static int ntiles(const Args& g) { return g.h * g.xtiles; }
-	__device__ static Tile tile(const Args& g, int id) { return {id / g.xtiles, (id % g.xtiles) * BM}; }
-	__device__ static int nk(const Args&) { return 9; }
-	__device__ static uint32_t strip_bytes(const Args& g) { return (uint32_t)(BM + 2 * g.dil) * BK * 2; }
-	__device__ static int dil(const Args& g) { return g.dil; }
-	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, const Tile& t, int dy, void* a,
-	                                  uint64_t* bar) {
-		tma_load_4d(a, ta, bar, 0, t.x0 - g.dil, t.y + (dy - 1) * g.dil, 0);
-	}
-	__device__ static void load_b(const CUtensorMap* tb, const Args&, int ks, void* b, uint64_t* bar) {
-		tma_load_2d(b, tb, bar, ks * BK, 0);
-	}
-	__device__ static void store(const Args& g, const Tile& t, int rl, int c, const float (&v)[32]) {
-		const int x = t.x0 + rl;
-		if (c != 0 || x >= g.w) return;
-		uint32_t q[16];
-#pragma unroll
-		for (int i = 0; i < 16; ++i) {
-			const float a0 = fmaxf(v[2 * i] + g.bias[2 * i], 0.0f), a1 = fmaxf(v[2 * i + 1] + g.bias[2 * i + 1], 0.0f);
-			const __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
-			q[i] = *reinterpret_cast<const uint32_t*>(&b2);
-		}
-		uint4* dst = reinterpret_cast<uint4*>(g.out + ((size_t)t.y * g.w + x) * 64);
-#pragma unroll
-		for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
-#pragma unroll
-		for (int i = 4; i < 8; ++i) dst[i] = make_uint4(0u, 0u, 0u, 0u);
-	}
 };
 
 // Persistent CTAs, each looping over tiles id = blockIdx.x, +gridDim.x, ...:
@@ -312,11 +247,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	          const __grid_constant__ CUtensorMap tcm, const typename P::Args g, const uint32_t idesc) {
 	constexpr int BN = P::BN, STAGES = P::STAGES;
 	constexpr bool RES = P::RESIDENT_B;
-	constexpr bool STRIP = P::STRIP;
 	constexpr uint32_t A_TILE = BM * BK * 2, B_TILE = BN * BK * 2;
-	constexpr uint32_t STAGE_BYTES = STRIP ? P::STRIP_STAGE : (RES ? A_TILE : A_TILE + B_TILE);
-	const uint32_t load_bytes = STRIP ? P::strip_bytes(g) : STAGE_BYTES;  // bytes one ring load brings
-	static_assert(!STRIP || P::STRIP_STAGE > 0, "strip policies define their stage size");
+	constexpr uint32_t STAGE_BYTES = RES ? A_TILE : A_TILE + B_TILE;  // bytes one ring load brings
 	extern __shared__ uint8_t smem_raw[];
 	// 1024-byte aligned start (128-byte swizzled TMA tiles), formed by indexing
 	// the shared array so that the compiler keeps shared-memory accesses
@@ -333,8 +265,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int ntiles = P::ntiles(g);
-	const int nk = P::nk(g);                   // K-slices of B (and of A, unless STRIP)
-	const int nload = STRIP ? P::R : nk;       // ring loads per tile
+	const int nk = P::nk(g);  // K-slices of A and B: ring loads per tile
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < STAGES; ++s) {
@@ -372,15 +303,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 		uint32_t q = 0;  // slices issued by this CTA
 		for (int id = blockIdx.x; id < ntiles && !*abort_flag; id += gridDim.x) {
 			const typename P::Tile t = P::tile(g, id);
-			for (int ks = 0; ks < nload; ++ks, ++q) {
+			for (int ks = 0; ks < nk; ++ks, ++q) {
 				const int s = (int)(q % STAGES);
 				const uint32_t round = q / STAGES;
 				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) break;
-				mbar_arrive_expect_tx(&full[s], load_bytes);
+				mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
 				armed[s] = (int)round;
-				if constexpr (STRIP)
-					P::load_strip(&ta, g, t, ks, base + s * STAGE_BYTES, &full[s]);
-				else if constexpr (RES)
+				if constexpr (RES)
 					P::load_a(&ta, g, t, ks, base + s * STAGE_BYTES, &full[s]);
 				else
 					P::load(&ta, &tb, g, t, ks, base + s * STAGE_BYTES, base + s * STAGE_BYTES + A_TILE, &full[s]);
@@ -406,29 +335,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 			tc_fence_after();
 			const uint32_t acc = tmem + (uint32_t)(a * BN);
 			bool ok = true;
-			for (int ks = 0; ks < nload; ++ks, ++q) {
+			for (int ks = 0; ks < nk; ++ks, ++q) {
 				const int s = (int)(q % STAGES);
 				const uint32_t round = q / STAGES;
 				if (!mbar_wait(&full[s], round & 1, abort_flag, g.err, kErrTimeoutFull)) { ok = false; break; }
 				tc_fence_after();
-				if constexpr (STRIP) {
-					// strip ks = filter row dy; taps dx = 0..R-1 start dx rows into it
+				const uint64_t ad = desc_kmajor_sw128(smem_u32(base + s * STAGE_BYTES));
+				const uint64_t bd =
+					desc_kmajor_sw128(smem_u32(RES ? bres + ks * B_TILE : base + s * STAGE_BYTES + A_TILE));
 #pragma unroll
-					for (int dx = 0; dx < P::R; ++dx) {
-						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * STAGE_BYTES), dx * P::dil(g));
-						const uint64_t bd = desc_kmajor_sw128(smem_u32(bres + (ks * P::R + dx) * B_TILE));
-#pragma unroll
-						for (int kk = 0; kk < BK / 16; ++kk)
-							mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || dx > 0 || kk > 0);
-					}
-				} else {
-					const uint64_t ad = desc_kmajor_sw128(smem_u32(base + s * STAGE_BYTES));
-					const uint64_t bd =
-						desc_kmajor_sw128(smem_u32(RES ? bres + ks * B_TILE : base + s * STAGE_BYTES + A_TILE));
-#pragma unroll
-					for (int kk = 0; kk < BK / 16; ++kk)
-						mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || kk > 0);
-				}
+				for (int kk = 0; kk < BK / 16; ++kk) mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, ks > 0 || kk > 0);
 				mma_commit(&empty[s]);
 			}
 			if (!ok) break;
@@ -500,7 +416,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 template <class P>
 constexpr size_t smem_bytes() {
-	const size_t stage = P::STRIP ? (size_t)P::STRIP_STAGE : (size_t)(BM * BK * 2);
+	const size_t stage = (size_t)(BM * BK * 2);
 	const size_t epi = P::EPI_TMA ? 8 * 4096 : 0;
 	return P::RESIDENT_B
 	           ? (size_t)P::STAGES * stage + (size_t)P::NK_RES * (P::BN * BK * 2) + epi + 1024 + 256
@@ -527,7 +443,10 @@ constexpr size_t smem_bytes() {
 struct ConvRun {
 	using Args = ConvArgs;
 	static constexpr int BN = ConvStripPolicy::BN, STAGES = ConvStripPolicy::STAGES, NK_RES = 9, EPI_WARPS = 8;
+	static constexpr int KT = BK;  // K per tap: 64 channels, 128-byte rows
 	static constexpr uint32_t STRIP_STAGE = ConvStripPolicy::STRIP_STAGE;
+	__device__ static uint64_t desc_a(uint32_t strip, int row) { return desc_kmajor_sw128_rows(strip, row); }
+	__device__ static uint64_t desc_b(uint32_t slice) { return desc_kmajor_sw128(slice); }
 	__device__ static uint32_t strip_bytes(const Args&) { return ConvStripPolicy::STRIP_BYTES; }
 	__device__ static int dil(const Args&) { return 1; }
 	__host__ __device__ static int rows(const Args& g) { return g.h; }
@@ -553,11 +472,66 @@ struct ConvRun {
 		ConvPolicy::store(g, t, rl, c, v);
 	}
 };
+// One 3x3 layer of the motion-proposal network (32 -> 32 channels, dilation
+// d <= 8) in the same run order.  Activations are bf16 NHWC with 32-channel
+// pixels (64 bytes, TMA boxes with the 64-byte swizzle), so a tap is one
+// K = 32 slice: two M=128 x N=32 x K=16 MMAs, half the MMAs of 64-channel
+// pixels (the layer is bound by its MMA count).  The strip of filter row dy
+// holds the 128 + 2d input pixels of row y + (dy-1)d and the three taps
+// start 0, d, 2d rows into it.  Epilogue: + bias, ReLU, bf16, one 64-byte
+// pixel per thread.
+struct MenetRun {
+	using Args = MenetArgs;
+	static constexpr int BN = 32, STAGES = 16, NK_RES = 9, EPI_WARPS = 4, MAXD = 8;
+	static constexpr int KT = 32;  // K per tap: 32 channels, 64-byte rows
+	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * KT * 2 + 1023) & ~1023u;  // 9 216
+	__device__ static uint64_t desc_a(uint32_t strip, int row) { return desc_kmajor_sw64(strip + 64u * (uint32_t)row); }
+	__device__ static uint64_t desc_b(uint32_t slice) { return desc_kmajor_sw64(slice); }
+	__device__ static uint32_t strip_bytes(const Args& g) { return (uint32_t)(BM + 2 * g.dil) * KT * 2; }
+	__device__ static int dil(const Args& g) { return g.dil; }
+	__host__ __device__ static int rows(const Args& g) { return g.h; }
+	__host__ __device__ static int blocks(const Args& g) { return g.xtiles; }
+	// classes c = y mod d in order, y ascending within a class: classes
+	// 0 .. rm-1 hold q+1 rows, the others q (q = h / d, rm = h mod d)
+	__device__ static void row_of(const Args& g, int pos, int& y, int& class_end) {
+		const int d = g.dil, q = g.h / d, rm = g.h - q * d, big = rm * (q + 1);
+		if (pos < big) {
+			const int c = pos / (q + 1), k = pos - c * (q + 1);
+			y = c + k * d;
+			class_end = (c + 1) * (q + 1);
+		} else {
+			const int p2 = pos - big, c = p2 / q, k = p2 - c * q;
+			y = rm + c + k * d;
+			class_end = big + (c + 1) * q;
+		}
+	}
+	__device__ static void load_strip(const CUtensorMap* ta, const Args& g, int blk, int row, void* dst, uint64_t* bar) {
+		tma_load_4d(dst, ta, bar, 0, blk * BM - g.dil, row, 0);
+	}
+	__device__ static void load_b(const CUtensorMap* tb, const Args&, int ks, void* b, uint64_t* bar) {
+		tma_load_2d(b, tb, bar, ks * KT, 0);
+	}
+	__device__ static void store(const Args& g, int blk, int y, int rl, int c, const float (&v)[32]) {
+		const int x = blk * BM + rl;
+		if (c != 0 || x >= g.w) return;
+		uint32_t q[16];
+#pragma unroll
+		for (int i = 0; i < 16; ++i) {
+			const float a0 = fmaxf(v[2 * i] + g.bias[2 * i], 0.0f), a1 = fmaxf(v[2 * i + 1] + g.bias[2 * i + 1], 0.0f);
+			const __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
+			q[i] = *reinterpret_cast<const uint32_t*>(&b2);
+		}
+		uint4* dst = reinterpret_cast<uint4*>(g.out + ((size_t)y * g.w + x) * 32);
+#pragma unroll
+		for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+	}
+};
+
 template <class T>
 constexpr int run_threads() { return 64 + 32 * T::EPI_WARPS; }
 template <class T>
 constexpr size_t run_smem_bytes() {
-	return (size_t)T::STAGES * T::STRIP_STAGE + (size_t)T::NK_RES * (T::BN * BK * 2) + 1024 + 256;
+	return (size_t)T::STAGES * T::STRIP_STAGE + (size_t)T::NK_RES * (T::BN * T::KT * 2) + 1024 + 256;
 }
 
 template <class T>
@@ -565,8 +539,9 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 	strip_run_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
 	                 const typename T::Args g, const uint32_t idesc, const int per) {
 	constexpr int BN = T::BN, STAGES = T::STAGES, NKR = T::NK_RES;
-	constexpr uint32_t B_TILE = BN * BK * 2, SS = T::STRIP_STAGE;
+	constexpr uint32_t B_TILE = BN * T::KT * 2, SS = T::STRIP_STAGE;
 	static_assert(STAGES >= 3, "an output row reads three strips at once");
+	static_assert(SS % 1024 == 0 && B_TILE % 512 == 0, "operand tiles start on a swizzle atom");
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* bres = base + STAGES * SS;
@@ -666,10 +641,10 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 					tc_fence_after();
 #pragma unroll
 					for (int dx = 0; dx < 3; ++dx) {
-						const uint64_t ad = desc_kmajor_sw128_rows(smem_u32(base + s * SS), dx * d);
-						const uint64_t bd = desc_kmajor_sw128(smem_u32(bres + (dy * 3 + dx) * B_TILE));
+						const uint64_t ad = T::desc_a(smem_u32(base + s * SS), dx * d);
+						const uint64_t bd = T::desc_b(smem_u32(bres + (dy * 3 + dx) * B_TILE));
 #pragma unroll
-						for (int kk = 0; kk < BK / 16; ++kk)
+						for (int kk = 0; kk < T::KT / 16; ++kk)
 							mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, dy > 0 || dx > 0 || kk > 0);
 					}
 				}
@@ -1437,35 +1412,40 @@ namespace umi {
 // cuTensorMapEncodeTiled for the other translation units (full_me.cu).
 void* tma_encode_fn() { return reinterpret_cast<void*>(encode_fn()); }
 
-// One tensor-core layer of the motion-proposal network (see MenetConvPolicy):
-// in/out (h, w, 64) bf16 NHWC, wpack (32, 9*64) bf16 K-major (tap-major, then
-// input channel; channels >= 32 zero), bias 32 fp32.  Used by learned_me.cu.
+// One tensor-core layer of the motion-proposal network (see MenetRun):
+// in/out (h, w, 32) bf16 NHWC, wpack (32, 9*32) bf16 K-major (tap-major, then
+// input channel), bias 32 fp32.  Used by learned_me.cu.
 umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const float* bias, int h, int w, int dil,
                          int* err, cudaStream_t st) {
-	if (dil < 1 || dil > MenetConvPolicy::MAXD) return umi::fail(UMI_ERR_UNSUPPORTED, "menet conv: dilation %d", dil);
+	if (dil < 1 || dil > MenetRun::MAXD) return umi::fail(UMI_ERR_UNSUPPORTED, "menet conv: dilation %d", dil);
 	if (!umi::aligned(in, 16) || !umi::aligned(out, 16) || !umi::aligned(wpack, 16))
 		return umi::fail(UMI_ERR_INVALID_ARG, "menet conv: misaligned buffer");
 	auto enc = encode_fn();
 	if (!enc) return umi::fail(UMI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
 	CUtensorMap ta, tb;
 	{
-		const cuuint64_t dims[4] = {64, (cuuint64_t)w, (cuuint64_t)h, 1};
-		const cuuint64_t strides[3] = {128, (cuuint64_t)w * 128, (cuuint64_t)h * w * 128};
-		const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)(BM + 2 * dil), 1, 1};
+		const cuuint64_t dims[4] = {32, (cuuint64_t)w, (cuuint64_t)h, 1};
+		const cuuint64_t strides[3] = {64, (cuuint64_t)w * 64, (cuuint64_t)h * w * 64};
+		const cuuint32_t box[4] = {32, (cuuint32_t)(BM + 2 * dil), 1, 1};
 		const cuuint32_t es[4] = {1, 1, 1, 1};
 		const CUresult rr = enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(in), dims, strides, box, es,
-		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
 		                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "menet conv: activation tensor map (%d)", (int)rr);
 	}
-	UMI_TRY(map_kmajor(&tb, wpack, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 32, 9 * BK, 32));
+	{
+		const cuuint64_t dims[2] = {9 * 32, 32};
+		const cuuint64_t strides[1] = {9 * 32 * 2};
+		const cuuint32_t box[2] = {32, 32};
+		const cuuint32_t es[2] = {1, 1};
+		const CUresult rr = enc(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(wpack), dims, strides, box, es,
+		                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+		                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+		if (rr != CUDA_SUCCESS) return umi::fail(UMI_ERR_CUDA, "menet conv: weight tensor map (%d)", (int)rr);
+	}
 	MenetArgs g{static_cast<__nv_bfloat16*>(out), bias, h, w, dil, umi::ceil_div(w, BM), err};
-	constexpr size_t SMEM = smem_bytes<MenetConvPolicy>();
-	auto kern = tc_kernel<MenetConvPolicy>;
-	int grid = 0;
-	UMI_TRY(persistent_grid(kern, SMEM, MenetConvPolicy::ntiles(g), tmem_cols_for(MenetConvPolicy::BN), &grid));
-	kern<<<grid, NTHREADS, SMEM, st>>>(ta, tb, tb, g, idesc_f16(1u, BM, MenetConvPolicy::BN));
-	return umi::launch_status("tc_kernel<menet conv>");
+	// runs of output rows y, y + d, y + 2d, ...: each input row's strip loaded once per run
+	return launch_strip_run<MenetRun>(ta, tb, g, (int64_t)h * g.xtiles, st, "strip_run_kernel<menet conv>");
 }
 
 }  // namespace umi

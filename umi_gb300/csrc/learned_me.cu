@@ -54,7 +54,7 @@ struct Layout {
 struct Work {
 	int H4, W4, P, nbx, nby, nblk, tiles_wg;
 	size_t x0, act[NL], dA[2], wb[NL], wt[NL], pred, centers, list, count, alist, amv, wpart, hpart, lpart;
-	size_t nhwc[2], wtc[NL], err;  // tensor-core inference: bf16 (H4, W4, 64) activations, packed weights
+	size_t nhwc[2], wtc[NL], err;  // tensor-core inference: bf16 (H4, W4, 32) activations, packed weights
 	size_t bytes;
 	Work(int h, int w) {
 		H4 = h / 4; W4 = w / 4; P = H4 * W4;
@@ -76,8 +76,8 @@ struct Work {
 		wpart = take(sizeof(float) * (size_t)tiles_wg * (CH * CH * 9 + CH));
 		hpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8) * (2 * HEADF + 2));
 		lpart = take(sizeof(float) * (size_t)umi::ceil_div(nblk, 8));
-		for (int i = 0; i < 2; ++i) nhwc[i] = take((size_t)P * 128);
-		for (int l = 0; l < NL; ++l) wtc[l] = take(2 * CH * 9 * 64);
+		for (int i = 0; i < 2; ++i) nhwc[i] = take((size_t)P * 64);
+		for (int l = 0; l < NL; ++l) wtc[l] = take(2 * CH * 9 * CH);
 		err = take(sizeof(int32_t));
 		bytes = o;
 	}
@@ -426,20 +426,20 @@ __global__ void audit_merge_kernel(int32_t* __restrict__ mv, const int32_t* __re
 	}
 }
 
-// ---- tensor-core inference path: bf16 NHWC activations, 64 channels per
-// pixel (32 used, 32 zero), layers 2-4 on tcgen05 (umi::menet_conv_tc).
+// ---- tensor-core inference path: bf16 NHWC activations, 32 channels (64
+// bytes) per pixel, layers 2-4 on tcgen05 (umi::menet_conv_tc).
 
-// Weights of layer l >= 1 as a (32, 9*64) bf16 K-major matrix: column
-// tap*64 + ci, zero for ci >= 32.
+// Weights of layer l >= 1 as a (32, 9*32) bf16 K-major matrix: column
+// tap*32 + ci.
 __global__ void pack_tc_weights_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ out) {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < CH * 9 * 64; i += gridDim.x * blockDim.x) {
-		const int co = i / (9 * 64), r = i - co * 9 * 64, tap = r >> 6, ci = r & 63;
-		out[i] = ci < CH ? __float2bfloat16_rn(w[(co * CH + ci) * 9 + tap]) : __float2bfloat16_rn(0.0f);
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < CH * 9 * CH; i += gridDim.x * blockDim.x) {
+		const int co = i / (9 * CH), r = i - co * 9 * CH, tap = r / CH, ci = r - tap * CH;
+		out[i] = __float2bfloat16_rn(w[(co * CH + ci) * 9 + tap]);
 	}
 }
 
 // Layer 1 (2 -> 32 channels, dilation 1) on the FP32 pipe, one pixel per
-// thread: + bias, ReLU, bf16, one 128-byte NHWC pixel.
+// thread: + bias, ReLU, bf16, one 64-byte NHWC pixel.
 __global__ void __launch_bounds__(NT) conv1_nhwc_kernel(const float* __restrict__ x0, const __nv_bfloat16* __restrict__ w,
                                                         const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
                                                         int H, int W) {
@@ -473,11 +473,9 @@ __global__ void __launch_bounds__(NT) conv1_nhwc_kernel(const float* __restrict_
 		const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(a0, 0.0f), fmaxf(a1, 0.0f));
 		q[c2] = *reinterpret_cast<const uint32_t*>(&b2);
 	}
-	uint4* dst = reinterpret_cast<uint4*>(out + (size_t)p * 64);
+	uint4* dst = reinterpret_cast<uint4*>(out + (size_t)p * CH);
 #pragma unroll
 	for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
-#pragma unroll
-	for (int i = 4; i < 8; ++i) dst[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // Head on the bf16 NHWC layer-4 activations: one warp per block, lane = channel.
@@ -490,7 +488,7 @@ __global__ void head_nhwc_kernel(const __nv_bfloat16* __restrict__ a4, const flo
 #pragma unroll
 	for (int cell = 0; cell < 16; ++cell) {
 		const int i = cell >> 2, k = cell & 3;
-		const float v = __bfloat162float(a4[((size_t)(4 * by + i) * W4 + 4 * bx + k) * 64 + c]);
+		const float v = __bfloat162float(a4[((size_t)(4 * by + i) * W4 + 4 * bx + k) * CH + c]);
 		const int f = c * 16 + cell;
 		s0 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + f])), v, s0);
 		s1 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + HEADF + f])), v, s1);
@@ -560,7 +558,7 @@ umi_status infer(const uint8_t* cur, const uint8_t* ref, int h, int w, const flo
 	                                                          2);
 	UMI_TRY(umi::launch_status("pack_weights_kernel"));
 	for (int l = 1; l < NL; ++l) {
-		pack_tc_weights_kernel<<<grid_for(CH * 9 * 64), NT, 0, st>>>(params + L.w[l], K.at<__nv_bfloat16>(ws, K.wtc[l]));
+		pack_tc_weights_kernel<<<grid_for(CH * 9 * CH), NT, 0, st>>>(params + L.w[l], K.at<__nv_bfloat16>(ws, K.wtc[l]));
 		UMI_TRY(umi::launch_status("pack_tc_weights_kernel"));
 	}
 	__nv_bfloat16* a = K.at<__nv_bfloat16>(ws, K.nhwc[0]);

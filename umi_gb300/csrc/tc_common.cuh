@@ -204,6 +204,23 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128_rows(uint32_t tile_saddr, 
 	return desc_kmajor_sw128(tile_saddr + 128u * (uint32_t)row);
 }
 
+// The same for K-major tiles written by TMA with 64-byte swizzling: rows of
+// 64 bytes (32 two-byte elements, one K slice of a 3x3 tap over 32
+// channels), 8-row groups 512 bytes apart, layout SWIZZLE_64B (4, bits
+// 61-63).  The tile base must be 512-byte aligned; the K sub-block kk of 16
+// elements starts 32*kk bytes further.  An operand that starts `row` rows
+// into such a tile moves only the start address (64 bytes per row), as for
+// the 128-byte swizzle.
+__device__ __forceinline__ uint64_t desc_kmajor_sw64(uint32_t saddr) {
+	uint64_t d = 0;
+	d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+	d |= (uint64_t)1 << 16;            // leading byte offset (unused for this layout)
+	d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
+	d |= (uint64_t)1 << 46;            // descriptor version
+	d |= (uint64_t)4 << 61;            // 64-byte swizzle
+	return d;
+}
+
 // Instruction descriptor, kind::f16: fp32 accumulator, A and B of one type
 // (0 = f16, 1 = bf16), both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, int m, int n) {
