@@ -78,7 +78,7 @@ def test_menet_infer_matches_oracle(umi, dev, shape):
     p = _params(5)
     net = umi.MeNet(h, w, device=dev, params=p)
     # every workspace byte 0xff (bf16 NaN): the pass must write every value it
-    # reads, including the zero channels 32-63 of both activation buffers
+    # reads (activations, packed weights, predictions)
     net.ws.fill_(0xFF)
     err = torch.zeros(1, dtype=torch.int32, device=dev)
     got = net.infer(_t(cur, dev), _t(ref, dev), err=err).cpu().numpy()

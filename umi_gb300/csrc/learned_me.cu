@@ -429,78 +429,157 @@ __global__ void audit_merge_kernel(int32_t* __restrict__ mv, const int32_t* __re
 // ---- tensor-core inference path: bf16 NHWC activations, 32 channels (64
 // bytes) per pixel, layers 2-4 on tcgen05 (umi::menet_conv_tc).
 
-// Weights of layer l >= 1 as a (32, 9*32) bf16 K-major matrix: column
-// tap*32 + ci.
-__global__ void pack_tc_weights_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ out) {
+// Weights of layers 1..3 as (32, 9*32) bf16 K-major matrices (column
+// tap*32 + ci), all three in one launch: blockIdx.y = layer - 1.
+static_assert(NL == 4, "pack_tc_weights_kernel selects among three layers");
+struct TcWeights {
+	const float* w[NL - 1];
+	__nv_bfloat16* out[NL - 1];
+};
+__global__ void pack_tc_weights_kernel(TcWeights p) {
+	const int l = blockIdx.y;
+	const float* w = l == 0 ? p.w[0] : l == 1 ? p.w[1] : p.w[2];
+	__nv_bfloat16* out = l == 0 ? p.out[0] : l == 1 ? p.out[1] : p.out[2];
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < CH * 9 * CH; i += gridDim.x * blockDim.x) {
 		const int co = i / (9 * CH), r = i - co * 9 * CH, tap = r / CH, ci = r - tap * CH;
 		out[i] = __float2bfloat16_rn(w[(co * CH + ci) * 9 + tap]);
 	}
 }
 
-// Layer 1 (2 -> 32 channels, dilation 1) on the FP32 pipe, one pixel per
-// thread: + bias, ReLU, bf16, one 64-byte NHWC pixel.
-__global__ void __launch_bounds__(NT) conv1_nhwc_kernel(const float* __restrict__ x0, const __nv_bfloat16* __restrict__ w,
+// Layer 1 (2 -> 32 channels, dilation 1) on the FP32 pipe: + bias, ReLU,
+// bf16, 64-byte NHWC pixels.  Weights come straight from the parameters
+// ([co][ci][tap], rounded to bf16 here).  A thread computes one 16-byte
+// quarter of the output pixel (8 channels, q = thread & 3) for four adjacent
+// pixels x .. x+3 (x a multiple of 4, W a multiple of 4), from a 3 x 6 window
+// per input channel: one 16-byte load and two edge loads per window row.
+// Each accumulator sums bias, then the 18 products in (ci, tap) order.
+__global__ void __launch_bounds__(NT) conv1_nhwc_kernel(const float* __restrict__ x0, const float* __restrict__ w,
                                                         const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
                                                         int H, int W) {
-	__shared__ float ws[2 * 9 * CH];  // [ci][tap][co]
-	for (int i = threadIdx.x; i < CH * 2 * 9; i += NT) {
-		const int co = i / 18, r = i - co * 18;
-		ws[r * CH + co] = __bfloat162float(w[i]);
+	__shared__ float4 ws[18][CH / 4];  // [ci * 9 + tap][co / 4]
+	__shared__ float4 bs[CH / 4];
+	for (int i = threadIdx.x; i < CH * 18; i += NT) {
+		const int co = i / 18, k = i - co * 18;
+		reinterpret_cast<float*>(ws)[k * CH + co] = __bfloat162float(__float2bfloat16_rn(w[i]));
 	}
+	if (threadIdx.x < CH) reinterpret_cast<float*>(bs)[threadIdx.x] = bias[threadIdx.x];
 	__syncthreads();
-	const int P = H * W;
-	const int p = blockIdx.x * NT + threadIdx.x;
-	if (p >= P) return;
-	const int y = p / W, x = p - y * W;
-	float in[18];
+	const int P = H * W, groups_x = W >> 2;
+	const int t = blockIdx.x * NT + threadIdx.x, q = t & 3, pg = t >> 2;
+	if (pg >= H * groups_x) return;
+	const int y = pg / groups_x, x = (pg - y * groups_x) * 4;
+	float in[2][3][6];
+#pragma unroll
+	for (int ci = 0; ci < 2; ++ci)
+#pragma unroll
+		for (int r = 0; r < 3; ++r) {
+			const int yy = y + r - 1;
+			if (yy >= 0 && yy < H) {
+				const float* row = x0 + (size_t)ci * P + (size_t)yy * W + x;
+				const float4 m = *reinterpret_cast<const float4*>(row);
+				in[ci][r][0] = x > 0 ? row[-1] : 0.0f;
+				in[ci][r][1] = m.x; in[ci][r][2] = m.y; in[ci][r][3] = m.z; in[ci][r][4] = m.w;
+				in[ci][r][5] = x + 4 < W ? row[4] : 0.0f;
+			} else {
+#pragma unroll
+				for (int c = 0; c < 6; ++c) in[ci][r][c] = 0.0f;
+			}
+		}
+	float acc[4][8];
+	{
+		const float4 b0 = bs[2 * q], b1 = bs[2 * q + 1];
+#pragma unroll
+		for (int px = 0; px < 4; ++px) {
+			acc[px][0] = b0.x; acc[px][1] = b0.y; acc[px][2] = b0.z; acc[px][3] = b0.w;
+			acc[px][4] = b1.x; acc[px][5] = b1.y; acc[px][6] = b1.z; acc[px][7] = b1.w;
+		}
+	}
 #pragma unroll
 	for (int ci = 0; ci < 2; ++ci)
 #pragma unroll
 		for (int tap = 0; tap < 9; ++tap) {
-			const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-			in[ci * 9 + tap] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? x0[(size_t)ci * P + (size_t)yy * W + xx] : 0.0f;
-		}
-	uint32_t q[16];
+			const float4 wa = ws[ci * 9 + tap][2 * q], wb = ws[ci * 9 + tap][2 * q + 1];
+			const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
 #pragma unroll
-	for (int c2 = 0; c2 < CH / 2; ++c2) {
-		float a0 = bias[2 * c2], a1 = bias[2 * c2 + 1];
+			for (int px = 0; px < 4; ++px) {
+				const float v = in[ci][tap / 3][px + tap % 3];
 #pragma unroll
-		for (int k = 0; k < 18; ++k) {
-			a0 = fmaf(ws[k * CH + 2 * c2], in[k], a0);
-			a1 = fmaf(ws[k * CH + 2 * c2 + 1], in[k], a1);
+				for (int c = 0; c < 8; ++c) acc[px][c] = fmaf(wv[c], v, acc[px][c]);
+			}
 		}
-		const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(a0, 0.0f), fmaxf(a1, 0.0f));
-		q[c2] = *reinterpret_cast<const uint32_t*>(&b2);
+#pragma unroll
+	for (int px = 0; px < 4; ++px) {
+		uint32_t pk[4];
+#pragma unroll
+		for (int c2 = 0; c2 < 4; ++c2) {
+			const __nv_bfloat162 b2 =
+				__floats2bfloat162_rn(fmaxf(acc[px][2 * c2], 0.0f), fmaxf(acc[px][2 * c2 + 1], 0.0f));
+			pk[c2] = *reinterpret_cast<const uint32_t*>(&b2);
+		}
+		*reinterpret_cast<uint4*>(out + ((size_t)y * W + x + px) * CH + q * 8) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 	}
-	uint4* dst = reinterpret_cast<uint4*>(out + (size_t)p * CH);
-#pragma unroll
-	for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
 }
 
-// Head on the bf16 NHWC layer-4 activations: one warp per block, lane = channel.
-__global__ void head_nhwc_kernel(const __nv_bfloat16* __restrict__ a4, const float* __restrict__ params, int wh_off,
-                                 int bh_off, float* __restrict__ pred, int W4, int nbx, int nblk) {
-	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, c = threadIdx.x & 31;
-	if (warp >= nblk) return;
-	const int by = warp / nbx, bx = warp - by * nbx;
-	float s0 = 0.0f, s1 = 0.0f;
-#pragma unroll
-	for (int cell = 0; cell < 16; ++cell) {
-		const int i = cell >> 2, k = cell & 3;
-		const float v = __bfloat162float(a4[((size_t)(4 * by + i) * W4 + 4 * bx + k) * CH + c]);
-		const int f = c * 16 + cell;
-		s0 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + f])), v, s0);
-		s1 = fmaf(__bfloat162float(__float2bfloat16_rn(params[wh_off + HEADF + f])), v, s1);
+// Head on the bf16 NHWC layer-4 activations.  A block's 16 cells are four
+// rows of 256 contiguous bytes; a warp reads them as two 16-byte pieces per
+// lane (piece j = lane + 32 s: row j >> 4, cell (j >> 2) & 3, channels
+// 8 (j & 3) .. +7), so each lane keeps the 32 head weights of its pieces in
+// registers for every block it serves.  HEAD_BPW blocks per warp, all their
+// loads issued before the first product.
+constexpr int HEAD_WARPS = 8, HEAD_BPW = 4;
+__global__ void __launch_bounds__(HEAD_WARPS * 32)
+	head_nhwc_kernel(const __nv_bfloat16* __restrict__ a4, const float* __restrict__ params, int wh_off, int bh_off,
+                     float* __restrict__ pred, int W4, int nbx, int nblk) {
+	__shared__ float4 wsm[2][64][2];  // [output][piece][channels 0-3, 4-7 of the piece], bf16-rounded
+	for (int t = threadIdx.x; t < 2 * HEADF; t += blockDim.x) {
+		const int o = t / HEADF, f = t - o * HEADF, c = f >> 4, cell = f & 15;
+		const int j = (cell >> 2) * 16 + (cell & 3) * 4 + (c >> 3);
+		reinterpret_cast<float*>(&wsm[o][j][0])[c & 7] = __bfloat162float(__float2bfloat16_rn(params[wh_off + t]));
 	}
+	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const int first = (blockIdx.x * HEAD_WARPS + (threadIdx.x >> 5)) * HEAD_BPW;
+	if (first >= nblk) return;
+	float wt[2][2][8];  // [output][piece s][channel in the piece]
 #pragma unroll
-	for (int o = 16; o > 0; o >>= 1) {
-		s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-		s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+	for (int o = 0; o < 2; ++o)
+#pragma unroll
+		for (int s = 0; s < 2; ++s) {
+			const float4 a = wsm[o][lane + 32 * s][0], b = wsm[o][lane + 32 * s][1];
+			wt[o][s][0] = a.x; wt[o][s][1] = a.y; wt[o][s][2] = a.z; wt[o][s][3] = a.w;
+			wt[o][s][4] = b.x; wt[o][s][5] = b.y; wt[o][s][6] = b.z; wt[o][s][7] = b.w;
+		}
+	const size_t row_pieces = (size_t)W4 * CH * sizeof(__nv_bfloat16) / 16;
+	uint4 v[HEAD_BPW][2];
+#pragma unroll
+	for (int u = 0; u < HEAD_BPW; ++u) {
+		const int blk = min(first + u, nblk - 1);  // past the end: reload the last block, store nothing
+		const int by = blk / nbx, bx = blk - by * nbx;
+		const uint4* base = reinterpret_cast<const uint4*>(a4 + ((size_t)(4 * by) * W4 + 4 * bx) * CH) + (lane & 15);
+#pragma unroll
+		for (int s = 0; s < 2; ++s) v[u][s] = __ldg(base + ((lane >> 4) + 2 * s) * row_pieces);
 	}
-	if (c == 0) {
-		pred[2 * warp] = s0 + params[bh_off];
-		pred[2 * warp + 1] = s1 + params[bh_off + 1];
+	const float b0 = params[bh_off], b1 = params[bh_off + 1];
+#pragma unroll
+	for (int u = 0; u < HEAD_BPW; ++u) {
+		float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+		for (int s = 0; s < 2; ++s) {
+			const uint32_t word[4] = {v[u][s].x, v[u][s].y, v[u][s].z, v[u][s].w};
+#pragma unroll
+			for (int e = 0; e < 8; ++e) {
+				const float a = __uint_as_float(e & 1 ? word[e >> 1] & 0xffff0000u : word[e >> 1] << 16);
+				s0 = fmaf(wt[0][s][e], a, s0);
+				s1 = fmaf(wt[1][s][e], a, s1);
+			}
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+			s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+		}
+		if (lane == 0 && first + u < nblk)
+			*reinterpret_cast<float2*>(pred + 2 * (size_t)(first + u)) = make_float2(s0 + b0, s1 + b1);
 	}
 }
 
@@ -554,24 +633,24 @@ umi_status infer(const uint8_t* cur, const uint8_t* ref, int h, int w, const flo
 	const Work K(h, w);
 	downsample4_kernel<<<grid_for(2 * (size_t)K.P), NT, 0, st>>>(cur, ref, K.at<float>(ws, K.x0), w, K.H4, K.W4);
 	UMI_TRY(umi::launch_status("downsample4_kernel"));
-	pack_weights_kernel<<<grid_for(CH * 2 * 9), NT, 0, st>>>(params + L.w[0], K.at<__nv_bfloat16>(ws, K.wb[0]), nullptr,
-	                                                          2);
-	UMI_TRY(umi::launch_status("pack_weights_kernel"));
+	TcWeights tw;
 	for (int l = 1; l < NL; ++l) {
-		pack_tc_weights_kernel<<<grid_for(CH * 9 * CH), NT, 0, st>>>(params + L.w[l], K.at<__nv_bfloat16>(ws, K.wtc[l]));
-		UMI_TRY(umi::launch_status("pack_tc_weights_kernel"));
+		tw.w[l - 1] = params + L.w[l];
+		tw.out[l - 1] = K.at<__nv_bfloat16>(ws, K.wtc[l]);
 	}
+	pack_tc_weights_kernel<<<dim3(grid_for(CH * 9 * CH), NL - 1), NT, 0, st>>>(tw);
+	UMI_TRY(umi::launch_status("pack_tc_weights_kernel"));
 	__nv_bfloat16* a = K.at<__nv_bfloat16>(ws, K.nhwc[0]);
 	__nv_bfloat16* b = K.at<__nv_bfloat16>(ws, K.nhwc[1]);
-	conv1_nhwc_kernel<<<umi::ceil_div(K.P, NT), NT, 0, st>>>(K.at<float>(ws, K.x0), K.at<__nv_bfloat16>(ws, K.wb[0]),
-	                                                         params + L.b[0], a, K.H4, K.W4);
+	conv1_nhwc_kernel<<<umi::ceil_div(K.P, NT), NT, 0, st>>>(K.at<float>(ws, K.x0), params + L.w[0], params + L.b[0], a,
+	                                                         K.H4, K.W4);
 	UMI_TRY(umi::launch_status("conv1_nhwc_kernel"));
 	for (int l = 1; l < NL; ++l) {
 		UMI_TRY(umi::menet_conv_tc(a, b, K.at<__nv_bfloat16>(ws, K.wtc[l]), params + L.b[l], K.H4, K.W4, DIL[l], err, st));
 		std::swap(a, b);
 	}
-	head_nhwc_kernel<<<umi::ceil_div(K.nblk * 32, NT), NT, 0, st>>>(a, params, L.wh, L.bh, K.at<float>(ws, K.pred),
-	                                                                K.W4, K.nbx, K.nblk);
+	head_nhwc_kernel<<<umi::ceil_div(K.nblk, HEAD_WARPS * HEAD_BPW), HEAD_WARPS * 32, 0, st>>>(
+		a, params, L.wh, L.bh, K.at<float>(ws, K.pred), K.W4, K.nbx, K.nblk);
 	return umi::launch_status("head_nhwc_kernel");
 }
 
