@@ -443,7 +443,8 @@ constexpr size_t smem_bytes() {
 struct ConvRun {
 	using Args = ConvArgs;
 	static constexpr int BN = ConvStripPolicy::BN, STAGES = ConvStripPolicy::STAGES, NK_RES = 9, EPI_WARPS = 8;
-	static constexpr int KT = BK;  // K per tap: 64 channels, 128-byte rows
+	static constexpr int KT = BK;          // K per tap: 64 channels, 128-byte rows
+	static constexpr int ROW_BYTES = 128;  // one strip row (pixel) in shared memory
 	static constexpr uint32_t STRIP_STAGE = ConvStripPolicy::STRIP_STAGE;
 	__device__ static uint64_t desc_a(uint32_t strip, int row) { return desc_kmajor_sw128_rows(strip, row); }
 	__device__ static uint64_t desc_b(uint32_t slice) { return desc_kmajor_sw128(slice); }
@@ -471,19 +472,25 @@ struct ConvRun {
 		t.k0 = 0;
 		ConvPolicy::store(g, t, rl, c, v);
 	}
+	struct Epi {
+		__device__ explicit Epi(const Args&) {}
+		__device__ void store(const Args& g, int blk, int y, int rl, int c, const float (&v)[32]) const {
+			ConvRun::store(g, blk, y, rl, c, v);
+		}
+	};
 };
 // One 3x3 layer of the motion-proposal network (32 -> 32 channels, dilation
 // d <= 8) in the same run order.  Activations are bf16 NHWC with 32-channel
 // pixels (64 bytes, TMA boxes with the 64-byte swizzle), so a tap is one
-// K = 32 slice: two M=128 x N=32 x K=16 MMAs, half the MMAs of 64-channel
-// pixels (the layer is bound by its MMA count).  The strip of filter row dy
+// K = 32 slice: two M=128 x N=32 x K=16 MMAs.  The strip of filter row dy
 // holds the 128 + 2d input pixels of row y + (dy-1)d and the three taps
 // start 0, d, 2d rows into it.  Epilogue: + bias, ReLU, bf16, one 64-byte
 // pixel per thread.
 struct MenetRun {
 	using Args = MenetArgs;
 	static constexpr int BN = 32, STAGES = 16, NK_RES = 9, EPI_WARPS = 4, MAXD = 8;
-	static constexpr int KT = 32;  // K per tap: 32 channels, 64-byte rows
+	static constexpr int KT = 32;         // K per tap: 32 channels, 64-byte rows
+	static constexpr int ROW_BYTES = 64;  // one strip row (pixel) in shared memory
 	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * KT * 2 + 1023) & ~1023u;  // 9 216
 	__device__ static uint64_t desc_a(uint32_t strip, int row) { return desc_kmajor_sw64(strip + 64u * (uint32_t)row); }
 	__device__ static uint64_t desc_b(uint32_t slice) { return desc_kmajor_sw64(slice); }
@@ -511,20 +518,29 @@ struct MenetRun {
 	__device__ static void load_b(const CUtensorMap* tb, const Args&, int ks, void* b, uint64_t* bar) {
 		tma_load_2d(b, tb, bar, ks * KT, 0);
 	}
-	__device__ static void store(const Args& g, int blk, int y, int rl, int c, const float (&v)[32]) {
-		const int x = blk * BM + rl;
-		if (c != 0 || x >= g.w) return;
-		uint32_t q[16];
+	// epilogue: the layer's 32 biases held in registers, + bias, ReLU, bf16,
+	// one 64-byte pixel per thread
+	struct Epi {
+		float bias[32];
+		__device__ explicit Epi(const Args& g) {
 #pragma unroll
-		for (int i = 0; i < 16; ++i) {
-			const float a0 = fmaxf(v[2 * i] + g.bias[2 * i], 0.0f), a1 = fmaxf(v[2 * i + 1] + g.bias[2 * i + 1], 0.0f);
-			const __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
-			q[i] = *reinterpret_cast<const uint32_t*>(&b2);
+			for (int i = 0; i < 32; ++i) bias[i] = g.bias[i];
 		}
-		uint4* dst = reinterpret_cast<uint4*>(g.out + ((size_t)y * g.w + x) * 32);
+		__device__ void store(const Args& g, int blk, int y, int rl, int c, const float (&v)[32]) const {
+			const int x = blk * BM + rl;
+			if (c != 0 || x >= g.w) return;
+			uint32_t q[16];
 #pragma unroll
-		for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
-	}
+			for (int i = 0; i < 16; ++i) {
+				const float a0 = fmaxf(v[2 * i] + bias[2 * i], 0.0f), a1 = fmaxf(v[2 * i + 1] + bias[2 * i + 1], 0.0f);
+				const __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
+				q[i] = *reinterpret_cast<const uint32_t*>(&b2);
+			}
+			uint4* dst = reinterpret_cast<uint4*>(g.out + ((size_t)y * g.w + x) * 32);
+#pragma unroll
+			for (int i = 0; i < 4; ++i) dst[i] = make_uint4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+		}
+	};
 };
 
 template <class T>
@@ -542,6 +558,7 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 	constexpr uint32_t B_TILE = BN * T::KT * 2, SS = T::STRIP_STAGE;
 	static_assert(STAGES >= 3, "an output row reads three strips at once");
 	static_assert(SS % 1024 == 0 && B_TILE % 512 == 0, "operand tiles start on a swizzle atom");
+	constexpr uint32_t TCOLS = tmem_cols_for(BN);
 	extern __shared__ uint8_t smem_raw[];
 	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
 	uint8_t* bres = base + STAGES * SS;
@@ -581,7 +598,7 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 		tma_prefetch(&tb);
 	}
 	if (warp == 1) {
-		tmem_alloc(tmem_slot, tmem_cols_for(BN));
+		tmem_alloc(tmem_slot, TCOLS);
 		tmem_relinquish();
 	}
 	tc_fence_before();
@@ -620,8 +637,15 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 	} else if (warp == 1 && lane == 0) {
 		// ---- MMA issuer
 		bool ok = mbar_wait(bready, 0, abort_flag, g.err, kErrTimeoutFull);
-		uint32_t q0 = 0;  // first strip of the segment
-		int i = 0;        // tiles so far (accumulator a = i & 1)
+		// Descriptors of strip slot 0, row 0 and of weight slice 0; every
+		// operand below is one of them plus a byte offset / 16 in the start
+		// address field (bits 0-13: shared addresses stay below 2^18, so the
+		// sum never carries out of the field).
+		const uint64_t a_base = T::desc_a(smem_u32(base), 0), b_base = T::desc_b(smem_u32(bres));
+		const uint32_t a_row = (uint32_t)(d * T::ROW_BYTES) >> 4;
+		uint32_t q0 = 0;      // first strip of the segment
+		uint32_t waited = 0;  // strips 0 .. waited - 1 have landed
+		int i = 0;            // tiles so far (accumulator a = i & 1)
 		for (int s0 = t0; ok && s0 < t1 && !*abort_flag;) {
 			int blk, y0, s1;
 			segment(s0, blk, y0, s1);
@@ -636,13 +660,16 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 				for (int dy = 0; dy < 3; ++dy) {
 					const uint32_t q = q0 + (uint32_t)(k + dy);
 					const int s = (int)(q % STAGES);
-					// a strip already waited for by the row before completes at once
-					if (!mbar_wait(&full[s], (q / STAGES) & 1, abort_flag, g.err, kErrTimeoutFull)) { ok = false; break; }
-					tc_fence_after();
+					if (q >= waited) {  // the row before waited for the first two strips of this one
+						if (!mbar_wait(&full[s], (q / STAGES) & 1, abort_flag, g.err, kErrTimeoutFull)) { ok = false; break; }
+						tc_fence_after();
+						waited = q + 1;
+					}
+					const uint64_t as = a_base + ((uint32_t)s * (SS >> 4));
+					const uint64_t bs = b_base + (uint32_t)dy * (3 * B_TILE >> 4);
 #pragma unroll
 					for (int dx = 0; dx < 3; ++dx) {
-						const uint64_t ad = T::desc_a(smem_u32(base + s * SS), dx * d);
-						const uint64_t bd = T::desc_b(smem_u32(bres + (dy * 3 + dx) * B_TILE));
+						const uint64_t ad = as + (uint32_t)dx * a_row, bd = bs + (uint32_t)dx * (B_TILE >> 4);
 #pragma unroll
 						for (int kk = 0; kk < T::KT / 16; ++kk)
 							mma_f16(acc, ad + 2 * kk, bd + 2 * kk, idesc, dy > 0 || dx > 0 || kk > 0);
@@ -668,6 +695,7 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 		constexpr int SPAN = BN / (T::EPI_WARPS / 4);
 		static_assert(T::EPI_WARPS % 4 == 0 && SPAN % 32 == 0, "whole 32-column TMEM loads per warp");
 		const int qd = warp & 3, part = (warp - 2) >> 2;
+		const typename T::Epi epi(g);
 		int i = 0;
 		for (int id = t0; id < t1; ++id, ++i) {
 			const int a = i & 1;
@@ -681,7 +709,7 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 			for (int c = part * SPAN; c < (part + 1) * SPAN; c += 32) {
 				float v[32];
 				tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * BN + c), v);
-				T::store(g, blk, y, 32 * qd + lane, c, v);
+				epi.store(g, blk, y, 32 * qd + lane, c, v);
 			}
 			tc_fence_before();
 			__syncwarp();
@@ -692,7 +720,7 @@ __global__ void __launch_bounds__(run_threads<T>(), 1)
 	__syncthreads();
 	if (warp == 1) {
 		tc_fence_after();
-		tmem_dealloc(tmem, tmem_cols_for(BN));
+		tmem_dealloc(tmem, TCOLS);
 	}
 }
 

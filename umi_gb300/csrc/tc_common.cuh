@@ -81,9 +81,11 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, 
 
 // Waits for the phase with the given parity.  Returns false (after raising
 // *abort and recording `code` in *err) when the limit passes or another role
-// has aborted.
+// has aborted.  A phase that has already completed costs one test: the clock
+// is read only when the first test fails.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* err, int code,
                                           unsigned long long limit_ns = kWaitNs) {
+	if (mbar_try_wait(bar, parity)) return true;
 	const unsigned long long t0 = gtimer();
 	while (!mbar_try_wait(bar, parity)) {
 		if (*abort) return false;
