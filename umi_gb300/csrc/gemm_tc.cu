@@ -480,24 +480,20 @@ struct ConvRun {
 	};
 };
 // One 3x3 layer of the motion-proposal network (32 -> 32 channels, dilation
-// d <= 8) in the same run order.  Activations are bf16 NHWC with 32-channel
-// pixels (64 bytes, TMA boxes with the 64-byte swizzle), so a tap is one
-// K = 32 slice: two M=128 x N=32 x K=16 MMAs.  The strip of filter row dy
-// holds the 128 + 2d input pixels of row y + (dy-1)d and the three taps
-// start 0, d, 2d rows into it.  Epilogue: + bias, ReLU, bf16, one 64-byte
-// pixel per thread.
+// d <= 8) in the same run order (menet_rows_kernel below).  Activations are
+// bf16 NHWC with 32-channel pixels (64 bytes, TMA boxes with the 64-byte
+// swizzle), so a tap is one K = 32 slice.  The strip of input row y' holds
+// its 128 + 2d pixels around the block; taps dx = 0, 1, 2 start 0, d, 2d rows
+// into it.  Epilogue: + bias, ReLU, bf16, one 64-byte pixel per thread.
 struct MenetRun {
 	using Args = MenetArgs;
-	static constexpr int BN = 32, STAGES = 16, NK_RES = 9, EPI_WARPS = 4, MAXD = 8;
+	static constexpr int STAGES = 16, NK_RES = 9, MAXD = 8;
 	static constexpr int KT = 32;         // K per tap: 32 channels, 64-byte rows
 	static constexpr int ROW_BYTES = 64;  // one strip row (pixel) in shared memory
 	static constexpr uint32_t STRIP_STAGE = ((BM + 2 * MAXD) * KT * 2 + 1023) & ~1023u;  // 9 216
 	__device__ static uint64_t desc_a(uint32_t strip, int row) { return desc_kmajor_sw64(strip + 64u * (uint32_t)row); }
 	__device__ static uint64_t desc_b(uint32_t slice) { return desc_kmajor_sw64(slice); }
 	__device__ static uint32_t strip_bytes(const Args& g) { return (uint32_t)(BM + 2 * g.dil) * KT * 2; }
-	__device__ static int dil(const Args& g) { return g.dil; }
-	__host__ __device__ static int rows(const Args& g) { return g.h; }
-	__host__ __device__ static int blocks(const Args& g) { return g.xtiles; }
 	// classes c = y mod d in order, y ascending within a class: classes
 	// 0 .. rm-1 hold q+1 rows, the others q (q = h / d, rm = h mod d)
 	__device__ static void row_of(const Args& g, int pos, int& y, int& class_end) {
@@ -1443,6 +1439,219 @@ void* tma_encode_fn() { return reinterpret_cast<void*>(encode_fn()); }
 // One tensor-core layer of the motion-proposal network (see MenetRun):
 // in/out (h, w, 32) bf16 NHWC, wpack (32, 9*32) bf16 K-major (tap-major, then
 // input channel), bias 32 fp32.  Used by learned_me.cu.
+// The 32-channel layers in rolling-accumulator form.  A tcgen05.mma of
+// M = 128, K = 16 takes the same 75 clocks for every N up to 144 (then about
+// half a clock per column), so an N = 32 MMA runs at a fifth of the tensor
+// rate.  Here each strip (input row m of a run) is multiplied once by the
+// stacked weights of every filter row that reads it: for tap column dx,
+// B = [W(dy, dx) for dy = lo .. hi] (32 rows each, N = 32 (hi - lo + 1))
+// and D = the accumulators of output rows m - lo .. m - hi side by side.
+// Sixteen 32-column accumulators (all of TMEM) take consecutive output rows
+// in descending column order (row r at 32 (15 - r mod 16)), so those rows
+// are adjacent columns except where the ring wraps (then two MMAs).  Every
+// MMA accumulates: the accumulators are cleared at launch and by the
+// epilogue after it drains one.  Six MMAs per output row (3 dx x 2 K = 16
+// slices) instead of 18; a strip is read by its own six MMAs only.
+namespace {
+constexpr int ROLL_SLOTS = 16;
+constexpr int ROLL_EPI_WARPS = 8;  // two groups of four, taking alternate rows
+__host__ __device__ constexpr int roll_threads() { return 64 + 32 * ROLL_EPI_WARPS; }
+constexpr size_t roll_smem_bytes() {
+	return (size_t)MenetRun::STAGES * MenetRun::STRIP_STAGE + (size_t)MenetRun::NK_RES * (32 * MenetRun::KT * 2) + 1024 +
+	       1024;
+}
+__device__ __forceinline__ int roll_slot(int r) { return ROLL_SLOTS - 1 - (r & (ROLL_SLOTS - 1)); }
+
+__global__ void __launch_bounds__(roll_threads(), 1)
+	menet_rows_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const MenetArgs g,
+	                  const int per) {
+	using T = MenetRun;
+	constexpr int STAGES = T::STAGES, NKR = T::NK_RES;
+	constexpr uint32_t B_TILE = 32 * T::KT * 2, SS = T::STRIP_STAGE;  // 2 KB per tap, 9 KB per strip
+	static_assert(ROLL_SLOTS * 32 == 512 && ROLL_EPI_WARPS == 8, "sixteen accumulators fill TMEM; two epilogue groups");
+	extern __shared__ uint8_t smem_raw[];
+	uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+	uint8_t* bres = base + STAGES * SS;  // tap (dy, dx) at (3 dx + dy) * 2 KB: the dy of one dx adjacent
+	uint64_t* full = reinterpret_cast<uint64_t*>(bres + NKR * B_TILE);
+	uint64_t* empty = full + STAGES;
+	uint64_t* accfull = empty + STAGES;          // [ROLL_SLOTS]
+	uint64_t* accempty = accfull + ROLL_SLOTS;  // [ROLL_SLOTS]
+	uint64_t* drain = accempty + ROLL_SLOTS;
+	uint64_t* bready = drain + 1;
+	uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bready + 1);
+	volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int H = g.h, ntiles = g.xtiles * H, d = g.dil;
+	const int t0 = blockIdx.x * per, t1 = min(ntiles, t0 + per);
+	auto segment = [&](int s0, int& blk, int& y0, int& s1) {
+		blk = s0 / H;
+		int pend;
+		T::row_of(g, s0 - blk * H, y0, pend);
+		s1 = min(t1, blk * H + pend);
+	};
+
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < STAGES; ++s) {
+			mbar_init(&full[s], 1);
+			mbar_init(&empty[s], 1);
+		}
+		for (int a = 0; a < ROLL_SLOTS; ++a) {
+			mbar_init(&accfull[a], 1);
+			mbar_init(&accempty[a], 4);
+		}
+		mbar_init(drain, 1);
+		mbar_init(bready, 1);
+		*abort_flag = 0;
+		fence_mbar_init();
+		tma_prefetch(&ta);
+		tma_prefetch(&tb);
+	}
+	if (warp == 1) {
+		tmem_alloc(tmem_slot, 512);
+		tmem_relinquish();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = *tmem_slot;
+	if (warp >= 2 && warp < 6) {  // one warp per lane quadrant clears every accumulator
+#pragma unroll 1
+		for (uint32_t c = 0; c < 512; c += 32) tmem_zero32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + c);
+		tmem_wait_st();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+
+	if (warp == 0 && lane == 0) {
+		// ---- producer: weights once (tap ks = 3 dy + dx to slot 3 dx + dy), then every strip once
+		int armed[STAGES];
+		for (int s = 0; s < STAGES; ++s) armed[s] = -1;
+		mbar_arrive_expect_tx(bready, (uint32_t)NKR * B_TILE);
+		for (int ks = 0; ks < NKR; ++ks) T::load_b(&tb, g, ks, bres + (3 * (ks % 3) + ks / 3) * B_TILE, bready);
+		const uint32_t sbytes = T::strip_bytes(g);
+		uint32_t q = 0;
+		bool go = true;
+		for (int s0 = t0; go && s0 < t1 && !*abort_flag;) {
+			int blk, y0, s1;
+			segment(s0, blk, y0, s1);
+			for (int i = 0; i < s1 - s0 + 2; ++i, ++q) {  // input row y0 + (i - 1) d
+				const int s = (int)(q % STAGES);
+				const uint32_t round = q / STAGES;
+				if (!mbar_wait(&empty[s], (round & 1) ^ 1, abort_flag, g.err, kErrTimeoutEmpty)) { go = false; break; }
+				mbar_arrive_expect_tx(&full[s], sbytes);
+				armed[s] = (int)round;
+				T::load_strip(&ta, g, blk, y0 + (i - 1) * d, base + s * SS, &full[s]);
+			}
+			s0 = s1;
+		}
+		if (*abort_flag) {
+			volatile int own = 0;
+			for (int s = 0; s < STAGES; ++s)
+				if (armed[s] >= 0) mbar_wait(&full[s], (uint32_t)armed[s] & 1, &own, g.err, kErrTimeoutFull);
+			mbar_wait(bready, 0, &own, g.err, kErrTimeoutFull);
+		}
+	} else if (warp == 1 && lane == 0) {
+		// ---- MMA issuer: strip m of a run of `rows` output rows feeds rows
+		// m - dy for dy in [lo, hi] = [max(0, m - rows + 1), min(2, m)]
+		bool ok = mbar_wait(bready, 0, abort_flag, g.err, kErrTimeoutFull);
+		const uint64_t a_base = T::desc_a(smem_u32(base), 0), b_base = T::desc_b(smem_u32(bres));
+		const uint32_t a_row = (uint32_t)(d * T::ROW_BYTES) >> 4;
+		uint32_t q = 0;  // strips so far
+		int r0 = 0;      // output rows of the earlier runs
+		for (int s0 = t0; ok && s0 < t1 && !*abort_flag;) {
+			int blk, y0, s1;
+			segment(s0, blk, y0, s1);
+			const int rows = s1 - s0;
+			for (int m = 0; m < rows + 2; ++m, ++q) {
+				const int lo = max(0, m - rows + 1), hi = min(2, m), cnt = hi - lo + 1;
+				if (lo == 0) {  // row r0 + m starts here: its accumulator must be drained and cleared
+					const int r = r0 + m;
+					if (!mbar_wait(&accempty[roll_slot(r)], ((uint32_t)(r / ROLL_SLOTS) & 1) ^ 1, abort_flag, g.err,
+					               kErrTimeoutAccEmpty)) {
+						ok = false;
+						break;
+					}
+					tc_fence_after();
+				}
+				const int s = (int)(q % STAGES);
+				if (!mbar_wait(&full[s], (q / STAGES) & 1, abort_flag, g.err, kErrTimeoutFull)) {
+					ok = false;
+					break;
+				}
+				tc_fence_after();
+				const int first = roll_slot(r0 + m - lo);
+				const int c1 = min(cnt, ROLL_SLOTS - first);  // blocks before the ring wraps to column 0
+				const uint32_t id1 = idesc_f16(1u, BM, 32 * c1), id2 = idesc_f16(1u, BM, 32 * (cnt - c1));
+				const uint64_t as = a_base + ((uint32_t)s * (SS >> 4));
+#pragma unroll
+				for (int dx = 0; dx < 3; ++dx) {
+					const uint64_t ad = as + (uint32_t)dx * a_row;
+					const uint64_t bd = b_base + (uint32_t)(3 * dx + lo) * (B_TILE >> 4);
+#pragma unroll
+					for (int kk = 0; kk < T::KT / 16; ++kk) {
+						mma_f16(tmem + 32u * (uint32_t)first, ad + 2 * kk, bd + 2 * kk, id1, true);
+						if (c1 < cnt) mma_f16(tmem, ad + 2 * kk, bd + (uint32_t)c1 * (B_TILE >> 4) + 2 * kk, id2, true);
+					}
+				}
+				mma_commit(&empty[s]);                                      // the strip's only reader
+				if (m >= 2) mma_commit(&accfull[roll_slot(r0 + m - 2)]);  // row m - 2 has all nine taps
+			}
+			r0 += rows;
+			s0 = s1;
+		}
+		mma_commit(drain);
+		volatile int own = 0;
+		mbar_wait(drain, 0, &own, g.err, kErrTimeoutAccum);
+	} else if (warp >= 2) {
+		// ---- epilogue: group (w - 2) / 4 takes rows r = group mod 2; warp w
+		// reads TMEM lanes 32 (w%4) .. +31 (pixels), clears the accumulator,
+		// releases it, then + bias, ReLU, bf16 and the 64-byte pixel store
+		const int qd = warp & 3, grp = (warp - 2) >> 2;
+		const T::Epi epi(g);
+		for (int r = grp; t0 + r < t1; r += 2) {
+			const int id = t0 + r, sl = roll_slot(r);
+			if (!mbar_wait(&accfull[sl], (uint32_t)(r / ROLL_SLOTS) & 1, abort_flag, g.err, kErrTimeoutAccum)) break;
+			tc_fence_after();
+			const uint32_t ta_ = tmem + ((uint32_t)(32 * qd) << 16) + 32u * (uint32_t)sl;
+			float v[32];
+			tmem_ld32(ta_, v);
+			tmem_zero32(ta_);
+			tmem_wait_st();
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&accempty[sl]);
+			const int blk = id / H;
+			int y, pend;
+			T::row_of(g, id - blk * H, y, pend);
+			epi.store(g, blk, y, 32 * qd + lane, 0, v);
+		}
+	}
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 1) {
+		tc_fence_after();
+		tmem_dealloc(tmem, 512);
+	}
+}
+
+umi_status launch_menet_rows(const CUtensorMap& ta, const CUtensorMap& tb, const MenetArgs& g, int64_t tiles,
+                             cudaStream_t st) {
+	constexpr size_t SMEM = roll_smem_bytes();
+	UMI_TRY(umi::cuda_status(
+		cudaFuncSetAttribute(menet_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM),
+		"cudaFuncSetAttribute"));
+	int dev = 0, sms = 0;
+	UMI_TRY(umi::cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+	UMI_TRY(umi::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+	int grid = (int)std::min<int64_t>(tiles, (int64_t)sms);  // all of TMEM: one CTA per SM
+	const int per = (int)umi::ceil_div(tiles, (int64_t)grid);
+	grid = (int)umi::ceil_div(tiles, (int64_t)per);
+	menet_rows_kernel<<<grid, roll_threads(), SMEM, st>>>(ta, tb, g, per);
+	return umi::launch_status("menet_rows_kernel");
+}
+}  // namespace
+
 umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const float* bias, int h, int w, int dil,
                          int* err, cudaStream_t st) {
 	if (dil < 1 || dil > MenetRun::MAXD) return umi::fail(UMI_ERR_UNSUPPORTED, "menet conv: dilation %d", dil);
@@ -1473,7 +1682,7 @@ umi_status menet_conv_tc(const void* in, void* out, const void* wpack, const flo
 	}
 	MenetArgs g{static_cast<__nv_bfloat16*>(out), bias, h, w, dil, umi::ceil_div(w, BM), err};
 	// runs of output rows y, y + d, y + 2d, ...: each input row's strip loaded once per run
-	return launch_strip_run<MenetRun>(ta, tb, g, (int64_t)h * g.xtiles, st, "strip_run_kernel<menet conv>");
+	return launch_menet_rows(ta, tb, g, (int64_t)h * g.xtiles, st);
 }
 
 }  // namespace umi

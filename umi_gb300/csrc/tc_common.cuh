@@ -161,6 +161,17 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 	             : "memory");
 }
 
+// Zero into 32 consecutive columns of the warp's 32 TMEM lanes, and the wait
+// for this thread's TMEM stores.
+__device__ __forceinline__ void tmem_zero32(uint32_t taddr) {
+	asm volatile(
+		"tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+		"{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+		"r"(0u)
+		: "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // 32 consecutive fp32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 	uint32_t r[32];
