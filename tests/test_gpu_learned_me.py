@@ -95,6 +95,35 @@ def test_menet_infer_matches_oracle(umi, dev, shape):
     assert np.abs(fp32 - got).max() <= 0.05 * scale
 
 
+def test_menet_infer_4k_equals_cropped_frame(umi, dev):
+    """At 4K each CTA of a tensor-core layer runs about 29 output rows, so
+    its ring of sixteen accumulators wraps (the split MMAs); a 272 x 1040
+    crop (a shape checked against the oracle above) runs two rows per CTA.
+    A block at least 64 pixels from the crop's edges sees the same inputs
+    in both (receptive field: 15 quarter-resolution pixels), and every
+    output value is summed in the same order, so its prediction must be
+    bit-identical."""
+    import torch
+    h, w = 2160, 3840
+    g = np.random.default_rng(11)
+    cur = g.integers(0, 256, (h, w), dtype=np.uint8)
+    ref = g.integers(0, 256, (h, w), dtype=np.uint8)
+    p = _params(7)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    net = umi.MeNet(h, w, device=dev, params=p)
+    full = net.infer(_t(cur, dev), _t(ref, dev), err=err).cpu().numpy().reshape(h // 16, w // 16, 2)
+    y0, x0, ch, cw = 1024, 1600, 272, 1040
+    small = umi.MeNet(ch, cw, device=dev, params=p)
+    crop = small.infer(_t(cur[y0:y0 + ch, x0:x0 + cw], dev), _t(ref[y0:y0 + ch, x0:x0 + cw], dev),
+                       err=err).cpu().numpy().reshape(ch // 16, cw // 16, 2)
+    assert int(err.item()) == 0
+    m = 4  # blocks of margin: 64 pixels
+    a = full[y0 // 16 + m:(y0 + ch) // 16 - m, x0 // 16 + m:(x0 + cw) // 16 - m]
+    b = crop[m:-m, m:-m]
+    assert a.shape == (9, 57, 2) and np.isfinite(a).all()
+    assert np.array_equal(a, b), np.abs(a - b).max()
+
+
 def test_menet_backward_matches_oracle(umi, dev):
     import torch
     h, w = 64, 96
