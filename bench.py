@@ -1539,13 +1539,13 @@ def run_ours(args, wl, dist):
                                              "note": "fp32 inputs split f16 hi/lo (3 products), fp32-level accuracy"}
         k = kernels["conv2d_fprop_bf16"]
         if k["hbm_floor_ms"] >= k["tensor_floor_ms"]:  # the fp32 output makes the launch HBM-bound
-            roof = {"bound": "hbm", "kernel": "conv_run_kernel (bf16)", "achieved": gbs, "peak": pk["hbm_gbs"],
+            roof = {"bound": "hbm", "kernel": "strip_run_kernel<ConvRun> (bf16)", "achieved": gbs, "peak": pk["hbm_gbs"],
                     "unit": "GB/s", "frac": gbs / pk["hbm_gbs"],
                     **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.N * wl.K * wl.H * wl.W),
                     "peak_source": pk["source"], "bytes_per_launch": nbytes, "ms_per_launch": kt,
                     "tensor_frac": k["frac"]}
         else:
-            roof = dict(k, bound="tensor", kernel="conv_run_kernel (bf16)", peak=pk["bf16_tflops"],
+            roof = dict(k, bound="tensor", kernel="strip_run_kernel<ConvRun> (bf16)", peak=pk["bf16_tflops"],
                         **traffic_fields(NCU_TRAFFIC.get(wl.name), 4 * wl.N * wl.K * wl.H * wl.W),
                         peak_source=pk["source"] + " (burst)",
                         flops_per_launch=wl.flops)
