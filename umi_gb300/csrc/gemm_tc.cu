@@ -26,6 +26,7 @@
 
 #include "common.h"
 #include "tc_common.cuh"
+#include "menet_roll.h"
 
 namespace {
 
@@ -1453,14 +1454,14 @@ void* tma_encode_fn() { return reinterpret_cast<void*>(encode_fn()); }
 // epilogue after it drains one.  Six MMAs per output row (3 dx x 2 K = 16
 // slices) instead of 18; a strip is read by its own six MMAs only.
 namespace {
-constexpr int ROLL_SLOTS = 16;
+constexpr int ROLL_SLOTS = umi_roll::kSlots;
 constexpr int ROLL_EPI_WARPS = 8;  // two groups of four, taking alternate rows
 __host__ __device__ constexpr int roll_threads() { return 64 + 32 * ROLL_EPI_WARPS; }
 constexpr size_t roll_smem_bytes() {
 	return (size_t)MenetRun::STAGES * MenetRun::STRIP_STAGE + (size_t)MenetRun::NK_RES * (32 * MenetRun::KT * 2) + 1024 +
 	       1024;
 }
-__device__ __forceinline__ int roll_slot(int r) { return ROLL_SLOTS - 1 - (r & (ROLL_SLOTS - 1)); }
+__device__ __forceinline__ int roll_slot(int r) { return umi_roll::slot(r); }
 
 __global__ void __launch_bounds__(roll_threads(), 1)
 	menet_rows_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const MenetArgs g,
@@ -1564,7 +1565,8 @@ __global__ void __launch_bounds__(roll_threads(), 1)
 			segment(s0, blk, y0, s1);
 			const int rows = s1 - s0;
 			for (int m = 0; m < rows + 2; ++m, ++q) {
-				const int lo = max(0, m - rows + 1), hi = min(2, m), cnt = hi - lo + 1;
+				const umi_roll::Step st = umi_roll::step(m, rows, r0);
+				const int lo = st.lo, cnt = st.hi - st.lo + 1;
 				if (lo == 0) {  // row r0 + m starts here: its accumulator must be drained and cleared
 					const int r = r0 + m;
 					if (!mbar_wait(&accempty[roll_slot(r)], ((uint32_t)(r / ROLL_SLOTS) & 1) ^ 1, abort_flag, g.err,
@@ -1580,8 +1582,7 @@ __global__ void __launch_bounds__(roll_threads(), 1)
 					break;
 				}
 				tc_fence_after();
-				const int first = roll_slot(r0 + m - lo);
-				const int c1 = min(cnt, ROLL_SLOTS - first);  // blocks before the ring wraps to column 0
+				const int first = st.first, c1 = st.c1;  // c1 blocks before the ring wraps to column 0
 				const uint32_t id1 = idesc_f16(1u, BM, 32 * c1), id2 = idesc_f16(1u, BM, 32 * (cnt - c1));
 				const uint64_t as = a_base + ((uint32_t)s * (SS >> 4));
 #pragma unroll
